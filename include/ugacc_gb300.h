@@ -1,0 +1,119 @@
+/*
+ * C ABI of the GB300 (sm_103a) RHF coupled-cluster library.
+ *
+ * The reference is a psi4 plugin whose hot path is a stack of C++ classes
+ * (ugacc hamiltonian.h:12-34, ccwfn.h:12-106, hbar.h:11-36, cclambda.h:13-63,
+ * ccdensity.h:12-50, ccpert.h:17-80, ccresp.h:10-28) that share raw double**** arrays.
+ * This header is the boundary those classes are rebuilt on: plain pointers and sizes,
+ * no C++ or torch types, every call returns a ucc_status and never throws.
+ *
+ * Array layouts (row-major, float64, host memory unless stated):
+ *   fock        [nact][nact], occupied orbitals first (QT order), nact = no + nv
+ *   ints        [nact][nact][nact][nact], ints[p][q][r][s] = <pq|rs> = (pr|qs)
+ *   B           [naux][nact][nact], (pq|rs) = sum_Q B[Q][p][q] B[Q][r][s]
+ *   t1, l1, X1, Y1     [no][nv];    t2, l2, X2, Y2    [no][no][nv][nv]
+ *   pert        [nact][nact] one-electron perturbation matrix
+ */
+#ifndef UGACC_GB300_H
+#define UGACC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum ucc_status {
+  UCC_OK = 0,
+  UCC_NOT_CONVERGED = 1,   /* reference: PSIEXCEPTION("Computation has not converged.") */
+  UCC_NAN_DETECTED = 2,
+  UCC_OUT_OF_MEMORY = 3,
+  UCC_BAD_ARGS = 4,
+  UCC_BAD_STATE = 5,       /* a stage was called before the stage it depends on */
+  UCC_CUDA_ERROR = 6,
+  UCC_DEVICE_TIMEOUT = 7,  /* a bounded device-side wait gave up */
+  UCC_UNSUPPORTED = 8
+} ucc_status;
+
+typedef struct ucc_ctx ucc_ctx;
+
+/* Arithmetic of the contractions. FP64 is the plain form; MIXED runs the large
+ * contractions (particle ladder, rings, (T)) as BF16 hi+lo split products with FP32
+ * accumulation on the tensor cores and keeps denominators, updates, DIIS, norms and
+ * energies in FP64, followed by FP64 refinement sweeps. */
+typedef enum ucc_precision { UCC_FP64 = 0, UCC_MIXED = 1 } ucc_precision;
+
+/* Solver options: the reference's psi4 options (ugacc.cc:57-68) plus the new ones. */
+typedef struct ucc_options {
+  int maxiter;            /* MAXITER, default 100 */
+  double r_convergence;   /* R_CONVERGENCE on the 2-norm of the residual, default 1e-7 */
+  int diis;               /* DIIS on/off, default 1 (8 vectors) */
+  int precision;          /* ucc_precision, default UCC_FP64 */
+  int refine_sweeps;      /* FP64 sweeps after a MIXED solve, default 2 */
+  int print;              /* 0 silent, 1 iteration table on stdout */
+} ucc_options;
+
+void ucc_options_default(ucc_options* opt);
+
+/* Replaces: psi::ugacc::Hamiltonian::Hamiltonian (hamiltonian.cc:19-104). */
+ucc_status ucc_ctx_create(ucc_ctx** ctx, int device);
+ucc_status ucc_ctx_destroy(ucc_ctx* ctx);
+ucc_status ucc_set_options(ucc_ctx* ctx, const ucc_options* opt);
+ucc_status ucc_load_hamiltonian(ucc_ctx* ctx, int no, int nv, const double* fock, const double* ints);
+ucc_status ucc_load_hamiltonian_df(ucc_ctx* ctx, int no, int nv, int naux, const double* fock, const double* B);
+
+/* Replaces: CCWfn::CCWfn + CCWfn::compute_energy, CCSD part (ccwfn.cc:12-120, :188-235).
+ * e_ccsd is the energy of the amplitudes before the final update, as the reference
+ * reports it (ccwfn.cc:224,233). */
+ucc_status ucc_ccsd(ucc_ctx* ctx, double* e_ccsd, int* iterations);
+
+/* Replaces: CCWfn::tcorr_ooc_TJL (ccwfn.cc:795-852) with W3_ijk (:1388-1418); the value
+ * equals tcorr_ooc (:745-793) and tcorr (:647-743). */
+ucc_status ucc_triples(ucc_ctx* ctx, double* e_t);
+
+/* Replaces: HBAR::HBAR (hbar.cc:8-228). */
+ucc_status ucc_hbar(ucc_ctx* ctx);
+
+/* Replaces: CCLambda::CCLambda + compute_lambda (cclambda.cc:13-45, :93-129). */
+ucc_status ucc_lambda(ucc_ctx* ctx, double* pseudoenergy, int* iterations);
+
+/* Replaces: CCDensity::onepdm + twopdm (ccdensity.cc:89-339). */
+ucc_status ucc_density(ucc_ctx* ctx, double* e_onepdm, double* e_twopdm);
+
+/* Replaces: CCPert::CCPert (ccpert.cc:11-77); returns a handle >= 0. */
+ucc_status ucc_pert_create(ucc_ctx* ctx, const double* pert, double omega, int* handle);
+/* Replaces: CCPert::solve (ccpert.cc:177-229); hand 0 = left, 1 = right (ccpert.h:15). */
+ucc_status ucc_pert_solve(ucc_ctx* ctx, int handle, int hand, double* pseudoresponse, int* iterations);
+/* Replaces: CCResp::linresp(X, Y) (ccresp.cc:28-124). */
+ucc_status ucc_linresp(ucc_ctx* ctx, int handle_x, int handle_y, double* value);
+
+/* Copy-out of named arrays: "t1" "t2" "tau" "l1" "l2" "Doo" "Dvv" "Dov" "Dvo" and the
+ * HBAR blocks "Hov" "Hoo" "Hvv" "Hoooo" "Hvvvv" "Hvovv" "Hooov" "Hovvo" "Hovov" "Hvvvo"
+ * "Hovoo"; per perturbation "X1:<h>" "X2:<h>" "Y1:<h>" "Y2:<h>".  count = elements. */
+ucc_status ucc_get_tensor(ucc_ctx* ctx, const char* name, double* host_out, size_t count);
+/* Copy-in (restart files, learned guesses): "t1" "t2" "l1" "l2". */
+ucc_status ucc_set_tensor(ucc_ctx* ctx, const char* name, const double* host_in, size_t count);
+
+/* Per-stage device timings (CUDA events on the library's stream) and FLOP counts. */
+typedef struct ucc_stats {
+  double ccsd_ms, triples_ms, hbar_ms, lambda_ms, density_ms, pert_ms;
+  double ccsd_flops, triples_flops;
+  int ccsd_iterations, lambda_iterations;
+  int64_t kernel_launches;   /* kernels of this library launched since the last reset */
+  double ladder_ms;          /* particle-ladder GEMM time, summed over iterations */
+  double ladder_bytes;       /* its algorithmic operand bytes, summed */
+  double ladder_flops;       /* its algorithmic FLOPs, summed */
+  int64_t ladder_launches;
+} ucc_stats;
+ucc_status ucc_get_stats(ucc_ctx* ctx, ucc_stats* out);
+ucc_status ucc_reset_stats(ucc_ctx* ctx);
+
+/* Last error message of this context (empty if none). */
+const char* ucc_last_error(ucc_ctx* ctx);
+const char* ucc_status_string(ucc_status s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UGACC_GB300_H */

@@ -1,0 +1,373 @@
+"""GB300-native RHF coupled-cluster solver behind ugacc's class surface.
+
+The classes mirror the reference's pipeline (ugacc.cc:108-241): ``Hamiltonian`` ->
+``CCWfn.compute_energy`` -> ``HBAR`` -> ``CCLambda.compute_lambda`` ->
+``CCDensity.onepdm/twopdm`` -> ``CCPert.solve`` -> ``CCResp.linresp``, with the same
+option names (ugacc.cc:57-68) and the same error behaviour (non-convergence raises
+``ConvergenceError("Computation has not converged.")`` like ccwfn.cc:231).  Every call
+goes through the C ABI of ``lib/libugacc_gb300.so`` (include/ugacc_gb300.h); there is no
+CPU fallback: without the library or a GPU the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "lib", "libugacc_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "ugacc_gb300.h")
+
+UCC_OK, UCC_NOT_CONVERGED = 0, 1
+STATUS = {0: "ok", 1: "not converged", 2: "nan detected", 3: "out of memory", 4: "bad arguments",
+          5: "bad state", 6: "cuda error", 7: "device timeout", 8: "unsupported"}
+FP64, MIXED = 0, 1
+LEFT, RIGHT = 0, 1
+
+
+class UccError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class ConvergenceError(UccError):
+    """The reference's PSIEXCEPTION("Computation has not converged.")."""
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [("maxiter", ctypes.c_int), ("r_convergence", ctypes.c_double), ("diis", ctypes.c_int),
+                ("precision", ctypes.c_int), ("refine_sweeps", ctypes.c_int), ("print", ctypes.c_int)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("ccsd_ms", ctypes.c_double), ("triples_ms", ctypes.c_double), ("hbar_ms", ctypes.c_double),
+                ("lambda_ms", ctypes.c_double), ("density_ms", ctypes.c_double), ("pert_ms", ctypes.c_double),
+                ("ccsd_flops", ctypes.c_double), ("triples_flops", ctypes.c_double),
+                ("ccsd_iterations", ctypes.c_int), ("lambda_iterations", ctypes.c_int),
+                ("kernel_launches", ctypes.c_int64), ("ladder_ms", ctypes.c_double),
+                ("ladder_bytes", ctypes.c_double), ("ladder_flops", ctypes.c_double),
+                ("ladder_launches", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def declared_functions() -> list[str]:
+    """Names of the functions include/ugacc_gb300.h declares."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:[\w\s\*]+?)\b(ucc_\w+)\s*\(", text, flags=re.M)))
+
+
+def load_library(path: str | None = None):
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIBPATH
+    if not os.path.exists(path):
+        raise UccError(6, f"GPU library not built: {path} (run python -m ugacc_gb300.build)")
+    lib = ctypes.CDLL(path)
+    P = ctypes.POINTER
+    d, i, vp, cp = ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_char_p
+    dp = P(d)
+    sig = {
+        "ucc_options_default": (None, [P(_Options)]),
+        "ucc_ctx_create": (i, [P(vp), i]),
+        "ucc_ctx_destroy": (i, [vp]),
+        "ucc_set_options": (i, [vp, P(_Options)]),
+        "ucc_load_hamiltonian": (i, [vp, i, i, dp, dp]),
+        "ucc_load_hamiltonian_df": (i, [vp, i, i, i, dp, dp]),
+        "ucc_ccsd": (i, [vp, dp, P(i)]),
+        "ucc_triples": (i, [vp, dp]),
+        "ucc_hbar": (i, [vp]),
+        "ucc_lambda": (i, [vp, dp, P(i)]),
+        "ucc_density": (i, [vp, dp, dp]),
+        "ucc_pert_create": (i, [vp, dp, d, P(i)]),
+        "ucc_pert_solve": (i, [vp, i, i, dp, P(i)]),
+        "ucc_linresp": (i, [vp, i, i, dp]),
+        "ucc_get_tensor": (i, [vp, cp, dp, ctypes.c_size_t]),
+        "ucc_set_tensor": (i, [vp, cp, dp, ctypes.c_size_t]),
+        "ucc_get_stats": (i, [vp, P(Stats)]),
+        "ucc_reset_stats": (i, [vp]),
+        "ucc_last_error": (cp, [vp]),
+        "ucc_status_string": (cp, [i]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Context:
+    """One device context (``ucc_ctx``) holding a Hamiltonian and every stage's arrays."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        st = self.lib.ucc_ctx_create(ctypes.byref(h), device)
+        if st != UCC_OK:
+            raise UccError(st, "cannot create a context on CUDA device %d" % device)
+        self.h = h
+
+    def check(self, st: int):
+        if st == UCC_OK:
+            return
+        msg = (self.lib.ucc_last_error(self.h) or b"").decode()
+        if st == UCC_NOT_CONVERGED:
+            raise ConvergenceError(st, msg or "Computation has not converged.")
+        raise UccError(st, msg)
+
+    def set_options(self, maxiter=100, r_convergence=1e-7, diis=True, precision=FP64, refine_sweeps=2, printing=0):
+        o = _Options(maxiter, r_convergence, int(diis), precision, refine_sweeps, printing)
+        self.check(self.lib.ucc_set_options(self.h, ctypes.byref(o)))
+
+    def get(self, name: str, shape) -> np.ndarray:
+        out = np.empty(shape, dtype=np.float64)
+        self.check(self.lib.ucc_get_tensor(self.h, name.encode(), _ptr(out), out.size))
+        return out
+
+    def set(self, name: str, arr: np.ndarray):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        self.check(self.lib.ucc_set_tensor(self.h, name.encode(), _ptr(a), a.size))
+
+    def stats(self) -> dict:
+        s = Stats()
+        self.check(self.lib.ucc_get_stats(self.h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def reset_stats(self):
+        self.check(self.lib.ucc_reset_stats(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ucc_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------------------------
+# Mirror of the reference's classes
+# ------------------------------------------------------------------------------------
+DEFAULT_OPTIONS = {"WFN": "CCSD", "DERTYPE": "NONE", "MAXITER": 100, "R_CONVERGENCE": 1e-7, "DIIS": True,
+                   "MYHAND": "RIGHT", "MY_OMEGA": 0.0, "PRECISION": "FP64", "REFINE_SWEEPS": 2, "PRINT": 0}
+
+
+class Hamiltonian:
+    """hamiltonian.h:12-34: Fock matrix (QT order) and two-electron integrals.
+
+    Either ``ints`` ([nact]^4, ``ints[p,q,r,s] = <pq|rs>``, the reference's layout) or the
+    density-fitting factors ``B`` ([naux][nact][nact]) are accepted."""
+
+    def __init__(self, no: int, nv: int, fock: np.ndarray, ints: np.ndarray | None = None,
+                 B: np.ndarray | None = None, device: int = 0, context: Context | None = None):
+        self.no, self.nv = no, nv
+        self.ctx = context or Context(device)
+        f = np.ascontiguousarray(fock, dtype=np.float64)
+        if ints is not None:
+            x = np.ascontiguousarray(ints, dtype=np.float64)
+            self.ctx.check(self.ctx.lib.ucc_load_hamiltonian(self.ctx.h, no, nv, _ptr(f), _ptr(x)))
+        elif B is not None:
+            b = np.ascontiguousarray(B, dtype=np.float64)
+            self.ctx.check(self.ctx.lib.ucc_load_hamiltonian_df(self.ctx.h, no, nv, b.shape[0], _ptr(f), _ptr(b)))
+        else:
+            raise ValueError("need ints or B")
+
+    @classmethod
+    def from_synthetic(cls, ham, use_ints: bool = False, **kw):
+        if use_ints:
+            return cls(ham.no, ham.nv, ham.fock, ints=ham.ints_physicist(), **kw)
+        return cls(ham.no, ham.nv, ham.fock, B=ham.B, **kw)
+
+
+class CCWfn:
+    """ccwfn.h:12-106: CCSD (and (T) for WFN=CCSD_T) ground state."""
+
+    def __init__(self, H: Hamiltonian, options: dict | None = None):
+        self.H, self.ctx = H, H.ctx
+        self.options = dict(DEFAULT_OPTIONS, **(options or {}))
+        o = self.options
+        self.ctx.set_options(maxiter=int(o["MAXITER"]), r_convergence=float(o["R_CONVERGENCE"]), diis=bool(o["DIIS"]),
+                             precision=MIXED if str(o["PRECISION"]).upper() == "MIXED" else FP64,
+                             refine_sweeps=int(o["REFINE_SWEEPS"]), printing=int(o["PRINT"]))
+        self.no, self.nv = H.no, H.nv
+        self.eccsd = self.et = None
+        self.iterations = 0
+
+    def compute_energy(self) -> float:
+        """ccwfn.cc:188-258: CCSD correlation energy, plus (T) when WFN == CCSD_T."""
+        e = ctypes.c_double()
+        it = ctypes.c_int()
+        st = self.ctx.lib.ucc_ccsd(self.ctx.h, ctypes.byref(e), ctypes.byref(it))
+        self.iterations = it.value
+        self.ctx.check(st)
+        self.eccsd = e.value
+        total = self.eccsd
+        if self.options["WFN"] == "CCSD_T":
+            self.et = self.triples()
+            total += self.et
+        return total
+
+    def triples(self) -> float:
+        """ccwfn.cc:795-852 (tcorr_ooc_TJL)."""
+        e = ctypes.c_double()
+        self.ctx.check(self.ctx.lib.ucc_triples(self.ctx.h, ctypes.byref(e)))
+        return e.value
+
+    @property
+    def t1(self):
+        return self.ctx.get("t1", (self.no, self.nv))
+
+    @property
+    def t2(self):
+        return self.ctx.get("t2", (self.no, self.no, self.nv, self.nv))
+
+
+class HBAR:
+    """hbar.h:11-36: similarity-transformed Hamiltonian blocks."""
+
+    SHAPES = {"Hov": "ov", "Hoo": "oo", "Hvv": "vv", "Hoooo": "oooo", "Hvvvv": "vvvv", "Hvovv": "vovv",
+              "Hooov": "ooov", "Hovvo": "ovvo", "Hovov": "ovov", "Hvvvo": "vvvo", "Hovoo": "ovoo"}
+
+    def __init__(self, H: Hamiltonian, cc: CCWfn):
+        self.H, self.cc, self.ctx = H, cc, cc.ctx
+        self.ctx.check(self.ctx.lib.ucc_hbar(self.ctx.h))
+
+    def block(self, name: str) -> np.ndarray:
+        shape = tuple(self.H.no if ch == "o" else self.H.nv for ch in self.SHAPES[name])
+        return self.ctx.get(name, shape)
+
+
+class CCLambda:
+    """cclambda.h:13-63."""
+
+    def __init__(self, cc: CCWfn, hbar: HBAR):
+        self.cc, self.hbar, self.ctx = cc, hbar, cc.ctx
+        self.pseudo = None
+        self.iterations = 0
+
+    def compute_lambda(self):
+        e = ctypes.c_double()
+        it = ctypes.c_int()
+        st = self.ctx.lib.ucc_lambda(self.ctx.h, ctypes.byref(e), ctypes.byref(it))
+        self.iterations = it.value
+        self.ctx.check(st)
+        self.pseudo = e.value
+
+    def pseudoenergy(self):
+        return self.pseudo
+
+    @property
+    def l1(self):
+        return self.ctx.get("l1", (self.cc.no, self.cc.nv))
+
+    @property
+    def l2(self):
+        return self.ctx.get("l2", (self.cc.no, self.cc.no, self.cc.nv, self.cc.nv))
+
+
+class CCDensity:
+    """ccdensity.h:12-50.  onepdm() and twopdm() return the energy contributions."""
+
+    def __init__(self, cc: CCWfn, lam: CCLambda):
+        self.cc, self.lam, self.ctx = cc, lam, cc.ctx
+        self._e = None
+
+    def _run(self):
+        if self._e is None:
+            a, b = ctypes.c_double(), ctypes.c_double()
+            self.ctx.check(self.ctx.lib.ucc_density(self.ctx.h, ctypes.byref(a), ctypes.byref(b)))
+            self._e = (a.value, b.value)
+        return self._e
+
+    def onepdm(self) -> float:
+        return self._run()[0]
+
+    def twopdm(self) -> float:
+        return self._run()[1]
+
+    def block(self, name: str) -> np.ndarray:
+        no, nv = self.cc.no, self.cc.nv
+        shape = {"Doo": (no, no), "Dvv": (nv, nv), "Dov": (no, nv), "Dvo": (nv, no)}[name]
+        self._run()
+        return self.ctx.get(name, shape)
+
+
+class CCPert:
+    """ccpert.h:17-80: perturbed wavefunction for one operator at frequency omega."""
+
+    def __init__(self, pert: np.ndarray, omega: float, cc: CCWfn, hbar: HBAR, lam: CCLambda):
+        self.cc, self.ctx, self.omega = cc, cc.ctx, omega
+        p = np.ascontiguousarray(pert, dtype=np.float64)
+        h = ctypes.c_int()
+        self.ctx.check(self.ctx.lib.ucc_pert_create(self.ctx.h, _ptr(p), float(omega), ctypes.byref(h)))
+        self.handle = h.value
+        self.iterations = {}
+
+    def solve(self, hand: str = "right") -> float:
+        e = ctypes.c_double()
+        it = ctypes.c_int()
+        hd = RIGHT if hand in ("right", RIGHT) else LEFT
+        st = self.ctx.lib.ucc_pert_solve(self.ctx.h, self.handle, hd, ctypes.byref(e), ctypes.byref(it))
+        self.iterations["right" if hd == RIGHT else "left"] = it.value
+        self.ctx.check(st)
+        return e.value
+
+    def amp(self, name: str) -> np.ndarray:
+        no, nv = self.cc.no, self.cc.nv
+        shape = (no, nv) if name.endswith("1") else (no, no, nv, nv)
+        return self.ctx.get(f"{name}:{self.handle}", shape)
+
+
+class CCResp:
+    """ccresp.h:10-28."""
+
+    def __init__(self, X: CCPert, Y: CCPert):
+        self.X, self.Y, self.ctx = X, Y, X.ctx
+
+    def linresp(self, X: CCPert, Y: CCPert) -> float:
+        v = ctypes.c_double()
+        self.ctx.check(self.ctx.lib.ucc_linresp(self.ctx.h, X.handle, Y.handle, ctypes.byref(v)))
+        return v.value
+
+
+def response(cc: CCWfn, hbar: HBAR, lam: CCLambda, perts, omega: float, hand: str = "right"):
+    """The recipe of ugacc.cc:158-227 for 3 dipole and 3 angular-momentum operators:
+    returns the symmetrised polarizability and the length-gauge rotation tensors."""
+    axes = "XYZ"
+    P = {}
+    for x in range(3):
+        P["Mu" + axes[x]] = CCPert(perts[x], omega, cc, hbar, lam)
+        P["Mu" + axes[x]].solve("right")
+        P["L" + axes[x]] = CCPert(perts[3 + x], omega, cc, hbar, lam)
+        P["L" + axes[x]].solve("right")
+        if hand == "left":
+            P["Mu" + axes[x]].solve("left")
+            P["L" + axes[x]].solve("left")
+    alpha, rot = {}, {}
+    for p in range(3):
+        for q in range(p + 1):
+            A, B = P["Mu" + axes[p]], P["Mu" + axes[q]]
+            r = CCResp(A, B)
+            alpha[axes[p] + axes[q]] = r.linresp(A, B) if p == q else 0.5 * r.linresp(A, B) + 0.5 * r.linresp(B, A)
+    for p in range(3):
+        for q in range(3):
+            A, B = P["Mu" + axes[p]], P["L" + axes[q]]
+            r = CCResp(A, B)
+            rot[axes[p] + axes[q]] = -(0.5 * r.linresp(A, B) - 0.5 * r.linresp(B, A))
+    return alpha, rot, P

@@ -1,0 +1,71 @@
+// Equation layer of the RHF-CC solver: integral blocks, DIIS and the solver stages.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+namespace ucc {
+
+// ---- integral blocks (physicist <pq|rs>, occupied indices first) ----------------------
+void load_from_ints(Ctx& c, int no, int nv, const double* fock, const double* ints);
+void load_from_df(Ctx& c, int no, int nv, int naux, const double* fock, const double* B);
+// <pq|rs> block view, e.g. V(c,"ovvv")[m,a,e,f] = <ma|ef>; stored blocks are oooo ooov oovv
+// ovov ovvv vvvv, the rest are permuted views of them
+Tensor V(Ctx& c, const std::string& blk);
+// L = 2<pq|rs> - <pq|sr> blocks: oovv ooov ovvv ovvo stored, oovo vovv as views
+Tensor L(Ctx& c, const std::string& blk);
+Tensor Fk(Ctx& c, const std::string& blk);  // Fock blocks oo ov vo vv
+Tensor narrow(const Tensor& t, int axis, int64_t start, int64_t len);
+
+// ---- DIIS over packed [x1 | x2] vectors ---------------------------------------------
+// Circular 8-slot Pulay subspace, error = new - old, B scaled by max|B_pq|, -1 border,
+// partial-pivot Gaussian elimination: the procedure of the reference's attic/diis.cc
+// used through psi4's DIISManager at ccwfn.cc:206-221.
+class Diis {
+ public:
+  Diis(Ctx& c, int64_t n, int nmax = 8);
+  ~Diis();
+  void add(const double* vnew, const double* vold);
+  int size() const { return count_; }
+  void extrapolate(double* out);
+
+ private:
+  Ctx& c_;
+  int64_t n_;
+  int nmax_, count_ = 0;
+  long nadded_ = 0;
+  DeviceBuffer err_, vec_;
+  const double** d_errp_ = nullptr;
+  const double** d_vecp_ = nullptr;
+  std::vector<double> B_;
+};
+
+// Solve B x = rhs for the bordered DIIS system (same elimination as the oracle's shim).
+std::vector<double> diis_coefficients(const std::vector<double>& Bfull, int n);
+
+// ---- solver stages ---------------------------------------------------------------------
+struct CCSDResult {
+  double e_ccsd = 0.0, e_mp2 = 0.0;
+  int iterations = 0;
+  bool converged = false;
+};
+CCSDResult run_ccsd(Ctx& c);
+double run_triples(Ctx& c);
+void run_hbar(Ctx& c);
+CCSDResult run_lambda(Ctx& c);
+void run_density(Ctx& c, double* e1, double* e2);
+
+// amplitude views into a packed [t1 | t2] buffer
+inline Tensor amp1(Ctx& c, double* p) { return make_view(p, {c.no, c.nv}); }
+inline Tensor amp2(Ctx& c, double* p) { return make_view(p + (int64_t)c.no * c.nv, {c.no, c.no, c.nv, c.nv}); }
+inline int64_t npacked(const Ctx& c) {
+  return (int64_t)c.no * c.nv + (int64_t)c.no * c.no * c.nv * c.nv;
+}
+
+// algorithmic FLOP counts (2 per multiply-add, no symmetry credit)
+double flops_ccsd_iter(double no, double nv);
+double flops_triples(double no, double nv);
+
+}  // namespace ucc

@@ -1,0 +1,190 @@
+// Internal core of the GB300 RHF-CC library: device tensors, the context, errors,
+// and the launchers of the hand-written kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/ugacc_gb300.h"
+
+namespace ucc {
+
+constexpr int kMaxRank = 6;
+
+// A (possibly strided) view of float64 device memory.  Dense tensors are row-major;
+// views produced by permute() share the pointer and reorder dims/strides.
+struct Tensor {
+  double* p = nullptr;
+  int rank = 0;
+  int64_t d[kMaxRank] = {};
+  int64_t s[kMaxRank] = {};
+
+  int64_t size() const {
+    int64_t n = 1;
+    for (int k = 0; k < rank; k++) n *= d[k];
+    return n;
+  }
+  bool dense() const {
+    int64_t st = 1;
+    for (int k = rank - 1; k >= 0; k--) {
+      if (d[k] != 1 && s[k] != st) return false;
+      st *= d[k];
+    }
+    return true;
+  }
+  // view with axes reordered: result axis k is this tensor's axis perm[k]
+  Tensor permute(const std::vector<int>& perm) const;
+  Tensor slice0(int64_t i) const;  // drop leading axis at index i
+};
+
+Tensor make_view(double* p, const std::vector<int64_t>& dims);
+
+struct Error : std::runtime_error {
+  ucc_status status;
+  Error(ucc_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define UCC_CUDA(call)                                                                     \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      throw ::ucc::Error(e_ == cudaErrorMemoryAllocation ? UCC_OUT_OF_MEMORY : UCC_CUDA_ERROR, \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));             \
+  } while (0)
+
+#define UCC_REQUIRE(cond, status, msg) \
+  do {                                 \
+    if (!(cond)) throw ::ucc::Error(status, msg); \
+  } while (0)
+
+// Owned device buffer (cudaMalloc; freed on destruction).
+struct DeviceBuffer {
+  double* p = nullptr;
+  size_t n = 0;
+  DeviceBuffer() = default;
+  explicit DeviceBuffer(size_t count);
+  ~DeviceBuffer();
+  DeviceBuffer(const DeviceBuffer&) = delete;
+  DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+};
+
+struct Ctx;
+
+// Stream-ordered scratch allocation (CUDA's async pool on the context stream).
+struct Scratch {
+  Ctx* ctx = nullptr;
+  void* p = nullptr;
+  Scratch(Ctx& c, size_t bytes);
+  ~Scratch();
+  double* d() const { return static_cast<double*>(p); }
+  Scratch(const Scratch&) = delete;
+  Scratch& operator=(const Scratch&) = delete;
+};
+
+struct Timer {  // CUDA events on the context stream
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaStream_t st = nullptr;
+  explicit Timer(cudaStream_t s);
+  ~Timer();
+  void start();
+  double stop_ms();  // synchronises
+};
+
+struct Perturbation;  // cc_pert.cpp
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  ucc_options opt{};
+  std::string last_error;
+
+  int no = 0, nv = 0, naux = 0;
+  bool loaded = false, have_ccsd = false, have_hbar = false, have_lambda = false;
+  std::vector<double> eps;  // orbital energies (diagonal of the Fock matrix)
+  std::vector<double> fock;  // [nact][nact]
+
+  // named persistent device arrays (integral blocks, amplitudes, HBAR, ...)
+  std::map<std::string, std::unique_ptr<DeviceBuffer>> store;
+  std::map<std::string, std::vector<int64_t>> shapes;
+  Tensor get(const std::string& name) const;
+  Tensor alloc(const std::string& name, const std::vector<int64_t>& dims, bool zero = true);
+  bool has(const std::string& name) const { return store.count(name) != 0; }
+  void drop(const std::string& name);
+
+  bool force_fp64 = false;  // integral construction and refinement sweeps stay FP64
+  std::vector<std::unique_ptr<Perturbation>> perts;
+  ucc_stats stats{};
+
+  ~Ctx();
+};
+
+// ----------------------------------------------------------------------------------
+// Kernel launchers (kernels_fp64.cu).  All are asynchronous on ctx.stream.
+// ----------------------------------------------------------------------------------
+struct GemmEpilogue {  // C offset of element (m, n): (m / msplit) * s_mhi + (m % msplit) * s_mlo + n * s_n
+  int64_t msplit = 0;  // 0: plain, offset = m * s_mhi + n * s_n
+  int64_t s_mhi = 0, s_mlo = 0, s_n = 1;
+};
+
+struct GemmPtrs {
+  const double* A;
+  const double* B;
+  double* C;
+};
+
+// C = alpha * op(A) op(B) + beta * C, row-major; op(A)[m][k] = ta ? A[k*lda+m] : A[m*lda+k];
+// op(B)[k][n] = tb ? B[n*ldb+k] : B[k*ldb+n].  Batched over `batch` with either strides
+// or a device array of pointer triples.
+void dgemm(Ctx& c, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+           const double* B, int64_t ldb, double beta, double* C, const GemmEpilogue& epi, int batch = 1,
+           int64_t sA = 0, int64_t sB = 0, int64_t sC = 0, const GemmPtrs* ptrs = nullptr);
+
+// Same with arbitrary operand strides: op(A)[m][k] = A[m*sAm + k*sAk], op(B)[k][n] = B[k*sBk + n*sBn].
+void dgemm_strided(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                   const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi,
+                   int batch, int64_t bA, int64_t bB, int64_t bC, const GemmPtrs* ptrs);
+// y[n] = alpha * sum_k x[k*sx] A[k*sk + n*sn] + beta * y[n*sy]
+void dgemv_strided(Ctx& c, int64_t N, int64_t K, double alpha, const double* x, int64_t sx, const double* A,
+                   int64_t sk, int64_t sn, double beta, double* y, int64_t sy);
+
+// out = alpha * in + beta * out over out's dims; both may be strided views.
+void permute_add(Ctx& c, const Tensor& in, double alpha, double beta, const Tensor& out);
+
+// y = alpha * x + beta * y, dense, n elements
+void axpby(Ctx& c, int64_t n, double alpha, const double* x, double beta, double* y);
+void fill(Ctx& c, int64_t n, double v, double* y);
+
+// Sum of x[k] * y[k] (y == nullptr: sum of x) with compensated FP64 accumulation; the
+// result stays on the device.
+void dot_async(Ctx& c, int64_t n, const double* x, const double* y, double* d_out);
+double dot(Ctx& c, int64_t n, const double* x, const double* y);
+// Several dot products x_k . y at once (DIIS B-matrix row), results on the device.
+void multidot_async(Ctx& c, int nvec, const double* const* d_xs, const double* y, int64_t n, double* d_out);
+
+// tau = t2 + f1 * t1(i,a) t1(j,b); ttau = t2 + f2 * t1 t1  (ttau may be null)
+void build_tau(Ctx& c, int no, int nv, const double* t1, const double* t2, double f1, double* tau, double f2,
+               double* ttau);
+
+// Jacobi update t_new = t_old + R / (D + shift), D built on the fly from the diagonals
+// do[no], dv[nv] in the reference's order ((d_i + d_j) - d_a) - d_b; the sum of R^2
+// (compensated) goes to the device scalar d_sumsq.
+void jacobi_update(Ctx& c, int no, int nv, const double* d_do, const double* d_dv, double shift, const double* R1,
+                   const double* R2, const double* t1old, const double* t2old, double* t1new, double* t2new,
+                   double* d_sumsq);
+
+// out = sum_p coef[p] * vecs[p] (device pointers, host coefficients), n elements
+void lincomb(Ctx& c, int nvec, const double* const* d_vecs, const double* coef, int64_t n, double* out);
+
+// (T) energy over a batch of (i>=j>=k) tuples, given W3 for each tuple.
+void triples_energy(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const double* W3,
+                    const double* t1, const double* Voovv, const double* eps, double* d_partial);
+
+int64_t launches();  // kernels launched by this library so far (all contexts)
+
+}  // namespace ucc

@@ -1,0 +1,338 @@
+// Contraction engine and context plumbing (host code).
+#include "engine.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace ucc {
+
+// mixed-precision GEMM path (tc_gemm.cu); returns false if it declines the problem
+bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn);
+
+// ---------------------------------------------------------------------------------------
+Tensor make_view(double* p, const std::vector<int64_t>& dims) {
+  Tensor t;
+  t.p = p;
+  t.rank = (int)dims.size();
+  UCC_REQUIRE(t.rank <= kMaxRank, UCC_BAD_ARGS, "rank too large");
+  int64_t st = 1;
+  for (int k = t.rank - 1; k >= 0; k--) {
+    t.d[k] = dims[k];
+    t.s[k] = st;
+    st *= dims[k];
+  }
+  return t;
+}
+
+Tensor Tensor::permute(const std::vector<int>& perm) const {
+  UCC_REQUIRE((int)perm.size() == rank, UCC_BAD_ARGS, "permute: wrong length");
+  Tensor r = *this;
+  for (int k = 0; k < rank; k++) {
+    r.d[k] = d[perm[k]];
+    r.s[k] = s[perm[k]];
+  }
+  return r;
+}
+
+Tensor Tensor::slice0(int64_t i) const {
+  Tensor r;
+  r.p = p + i * s[0];
+  r.rank = rank - 1;
+  for (int k = 1; k < rank; k++) {
+    r.d[k - 1] = d[k];
+    r.s[k - 1] = s[k];
+  }
+  return r;
+}
+
+DeviceBuffer::DeviceBuffer(size_t count) : n(count) {
+  if (count) UCC_CUDA(cudaMalloc(&p, count * sizeof(double)));
+}
+DeviceBuffer::~DeviceBuffer() {
+  if (p) cudaFree(p);
+}
+
+Scratch::Scratch(Ctx& c, size_t bytes) : ctx(&c) {
+  if (bytes == 0) bytes = 16;
+  UCC_CUDA(cudaMallocAsync(&p, bytes, c.stream));
+}
+Scratch::~Scratch() {
+  if (p) cudaFreeAsync(p, ctx->stream);
+}
+
+Timer::Timer(cudaStream_t s) : st(s) {
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+}
+Timer::~Timer() {
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+}
+void Timer::start() { cudaEventRecord(a, st); }
+double Timer::stop_ms() {
+  cudaEventRecord(b, st);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+Tensor Ctx::get(const std::string& name) const {
+  auto it = store.find(name);
+  UCC_REQUIRE(it != store.end(), UCC_BAD_STATE, "array not available: " + name);
+  return make_view(it->second->p, shapes.at(name));
+}
+
+Tensor Ctx::alloc(const std::string& name, const std::vector<int64_t>& dims, bool zero) {
+  size_t n = 1;
+  for (auto x : dims) n *= (size_t)x;
+  auto it = store.find(name);
+  if (it == store.end() || it->second->n != n) {
+    store[name].reset();
+    store[name] = std::make_unique<DeviceBuffer>(n);
+  }
+  shapes[name] = dims;
+  if (zero && n) UCC_CUDA(cudaMemsetAsync(store[name]->p, 0, n * sizeof(double), stream));
+  return make_view(store[name]->p, dims);
+}
+
+void Ctx::drop(const std::string& name) {
+  store.erase(name);
+  shapes.erase(name);
+}
+
+Temp::Temp(Ctx& c, const std::vector<int64_t>& dims, bool zero) : buf(c, [&] {
+  size_t n = 1;
+  for (auto x : dims) n *= (size_t)x;
+  return n * sizeof(double);
+}()) {
+  t = make_view(buf.d(), dims);
+  if (zero) UCC_CUDA(cudaMemsetAsync(buf.p, 0, t.size() * sizeof(double), c.stream));
+}
+
+// ---------------------------------------------------------------------------------------
+namespace {
+
+struct Parsed {
+  std::string a, b, c;
+};
+
+Parsed parse(const std::string& spec) {
+  Parsed p;
+  auto arrow = spec.find("->");
+  UCC_REQUIRE(arrow != std::string::npos, UCC_BAD_ARGS, "spec needs ->: " + spec);
+  std::string lhs = spec.substr(0, arrow);
+  p.c = spec.substr(arrow + 2);
+  auto comma = lhs.find(',');
+  if (comma == std::string::npos) {
+    p.a = lhs;
+  } else {
+    p.a = lhs.substr(0, comma);
+    p.b = lhs.substr(comma + 1);
+  }
+  return p;
+}
+
+int pos(const std::string& s, char ch) {
+  auto k = s.find(ch);
+  return k == std::string::npos ? -1 : (int)k;
+}
+
+// A group of labels, in order, addressed with one stride in tensor T (labels str)?
+// Returns the innermost stride (0 = group empty / extent 1, any stride works).
+bool fusable(const Tensor& T, const std::string& str, const std::string& grp, int64_t& inner) {
+  inner = 0;
+  int64_t expect = -1;
+  for (int k = (int)grp.size() - 1; k >= 0; k--) {
+    const int ax = pos(str, grp[k]);
+    const int64_t d = T.d[ax], s = T.s[ax];
+    if (d == 1) continue;
+    if (expect < 0) {
+      inner = s;
+    } else if (s != expect) {
+      return false;
+    }
+    expect = s * d;
+  }
+  return true;
+}
+
+int64_t extent(const Tensor& T, const std::string& str, const std::string& grp) {
+  int64_t e = 1;
+  for (char ch : grp) e *= T.d[pos(str, ch)];
+  return e;
+}
+
+std::string ordered(const std::string& src, const std::string& set) {
+  std::string r;
+  for (char ch : src)
+    if (set.find(ch) != std::string::npos) r += ch;
+  return r;
+}
+
+// dense copy of T relabelled into the order `target`
+Tensor gather(Ctx& c, const Tensor& T, const std::string& str, const std::string& target,
+              std::unique_ptr<Scratch>& holder) {
+  std::vector<int> perm;
+  std::vector<int64_t> dims;
+  for (char ch : target) {
+    perm.push_back(pos(str, ch));
+    dims.push_back(T.d[pos(str, ch)]);
+  }
+  size_t n = 1;
+  for (auto x : dims) n *= (size_t)x;
+  holder = std::make_unique<Scratch>(c, n * sizeof(double));
+  Tensor out = make_view(holder->d(), dims);
+  Tensor src = T.permute(perm);
+  permute_add(c, src, 1.0, 0.0, out);
+  return out;
+}
+
+}  // namespace
+
+Tensor view(const Tensor& T, const std::string& spec) {
+  Parsed p = parse(spec);
+  UCC_REQUIRE((int)p.a.size() == T.rank && p.a.size() == p.c.size(), UCC_BAD_ARGS, "view: bad spec " + spec);
+  std::vector<int> perm;
+  for (char ch : p.c) {
+    int k = pos(p.a, ch);
+    UCC_REQUIRE(k >= 0, UCC_BAD_ARGS, "view: bad spec " + spec);
+    perm.push_back(k);
+  }
+  return T.permute(perm);
+}
+
+void transpose_add(Ctx& c, const std::string& spec, double alpha, const Tensor& A, double beta, const Tensor& C) {
+  Tensor v = view(A, spec);
+  permute_add(c, v, alpha, beta, C);
+}
+
+double dot_all(Ctx& c, const Tensor& A, const Tensor& B) {
+  UCC_REQUIRE(A.rank == B.rank, UCC_BAD_ARGS, "dot_all: rank mismatch");
+  for (int k = 0; k < A.rank; k++) UCC_REQUIRE(A.d[k] == B.d[k], UCC_BAD_ARGS, "dot_all: dim mismatch");
+  std::unique_ptr<Scratch> ha, hb;
+  const double* pa = A.p;
+  const double* pb = B.p;
+  std::string lab = std::string("abcdef").substr(0, A.rank);
+  if (!A.dense()) pa = gather(c, A, lab, lab, ha).p;
+  if (!B.dense()) pb = gather(c, B, lab, lab, hb).p;
+  return dot(c, A.size(), pa, pb);
+}
+
+void contract(Ctx& c, const std::string& spec, double alpha, const Tensor& A, const Tensor& B, double beta,
+              const Tensor& C) {
+  Parsed p = parse(spec);
+  UCC_REQUIRE((int)p.a.size() == A.rank && (int)p.b.size() == B.rank && (int)p.c.size() == C.rank, UCC_BAD_ARGS,
+              "contract: rank/spec mismatch " + spec);
+  std::string Ms, Ns, Ks;
+  for (char ch : p.c) {
+    const bool ia = pos(p.a, ch) >= 0, ib = pos(p.b, ch) >= 0;
+    UCC_REQUIRE(ia != ib, UCC_UNSUPPORTED, "contract: batch/free label unsupported in " + spec);
+    (ia ? Ms : Ns) += ch;
+  }
+  for (char ch : p.a) {
+    if (pos(p.c, ch) >= 0) continue;
+    UCC_REQUIRE(pos(p.b, ch) >= 0, UCC_UNSUPPORTED, "contract: trace label unsupported in " + spec);
+    Ks += ch;
+  }
+  for (char ch : p.b)
+    if (pos(p.c, ch) < 0) UCC_REQUIRE(pos(p.a, ch) >= 0, UCC_UNSUPPORTED, "contract: trace label in " + spec);
+  // dimension checks
+  for (char ch : p.c) {
+    const Tensor& S = pos(p.a, ch) >= 0 ? A : B;
+    const std::string& ss = pos(p.a, ch) >= 0 ? p.a : p.b;
+    UCC_REQUIRE(S.d[pos(ss, ch)] == C.d[pos(p.c, ch)], UCC_BAD_ARGS, "contract: extent mismatch in " + spec);
+  }
+  for (char ch : Ks)
+    UCC_REQUIRE(A.d[pos(p.a, ch)] == B.d[pos(p.b, ch)], UCC_BAD_ARGS, "contract: extent mismatch in " + spec);
+
+  const int64_t M = extent(C, p.c, Ms), N = extent(C, p.c, Ns), K = extent(A, p.a, Ks);
+  if (M == 0 || N == 0) return;
+
+  // choose group orders minimising gathered bytes
+  const std::string Mcand[2] = {ordered(p.c, Ms), ordered(p.a, Ms)};
+  const std::string Ncand[2] = {ordered(p.c, Ns), ordered(p.b, Ns)};
+  const std::string Kcand[2] = {ordered(p.a, Ks), ordered(p.b, Ks)};
+  double best = 1e300;
+  std::string bm, bn, bk;
+  for (const auto& mo : Mcand)
+    for (const auto& no_ : Ncand)
+      for (const auto& ko : Kcand) {
+        int64_t s1, s2;
+        double cost = 0;
+        if (!(fusable(A, p.a, mo, s1) && fusable(A, p.a, ko, s2))) cost += (double)A.size();
+        if (!(fusable(B, p.b, ko, s1) && fusable(B, p.b, no_, s2))) cost += (double)B.size();
+        if (!(fusable(C, p.c, mo, s1) && fusable(C, p.c, no_, s2))) cost += 3.0 * (double)C.size();
+        if (cost < best) {
+          best = cost;
+          bm = mo;
+          bn = no_;
+          bk = ko;
+        }
+      }
+
+  std::unique_ptr<Scratch> hA, hB, hC;
+  Tensor a = A, b = B;
+  std::string sa = p.a, sb = p.b;
+  int64_t sAm, sAk, sBk, sBn, sCm, sCn;
+  if (!(fusable(a, sa, bm, sAm) && fusable(a, sa, bk, sAk))) {
+    a = gather(c, A, p.a, bm + bk, hA);
+    sa = bm + bk;
+    fusable(a, sa, bm, sAm);
+    fusable(a, sa, bk, sAk);
+  }
+  if (!(fusable(b, sb, bk, sBk) && fusable(b, sb, bn, sBn))) {
+    b = gather(c, B, p.b, bk + bn, hB);
+    sb = bk + bn;
+    fusable(b, sb, bk, sBk);
+    fusable(b, sb, bn, sBn);
+  }
+  const bool cdirect = fusable(C, p.c, bm, sCm) && fusable(C, p.c, bn, sCn);
+  Tensor ct = C;
+  if (!cdirect) {
+    std::vector<int64_t> dims;
+    for (char ch : bm + bn) dims.push_back(C.d[pos(p.c, ch)]);
+    size_t n = 1;
+    for (auto x : dims) n *= (size_t)x;
+    hC = std::make_unique<Scratch>(c, n * sizeof(double));
+    ct = make_view(hC->d(), dims);
+    sCm = N;
+    sCn = 1;
+  }
+  // empty groups: any stride works
+  if (sAm == 0) sAm = 1;
+  if (sAk == 0) sAk = 1;
+  if (sBk == 0) sBk = 1;
+  if (sBn == 0) sBn = 1;
+  if (sCm == 0) sCm = 1;
+  if (sCn == 0) sCn = 1;
+  const double ga = cdirect ? alpha : 1.0, gb = cdirect ? beta : 0.0;
+  bool done = false;
+  if (M == 1) {  // row vector times matrix
+    dgemv_strided(c, N, K, ga, a.p, sAk, b.p, sBk, sBn, gb, ct.p, sCn);
+    done = true;
+  } else if (N == 1) {  // matrix times column vector
+    dgemv_strided(c, M, K, ga, b.p, sBk, a.p, sAk, sAm, gb, ct.p, sCm);
+    done = true;
+  }
+  if (!done && c.opt.precision == UCC_MIXED && !c.force_fp64)
+    done = mixed_gemm(c, M, N, K, ga, a.p, sAm, sAk, b.p, sBk, sBn, gb, ct.p, sCm, sCn);
+  if (!done) {
+    GemmEpilogue epi;
+    epi.msplit = 0;
+    epi.s_mhi = sCm;
+    epi.s_n = sCn;
+    dgemm_strided(c, M, N, K, ga, a.p, sAm, sAk, b.p, sBk, sBn, gb, ct.p, epi, 1, 0, 0, 0, nullptr);
+  }
+  if (!cdirect) {
+    // ct is laid out (bm, bn); view it with C's label order and accumulate
+    std::string tl = bm + bn;
+    std::vector<int> perm;
+    for (char ch : p.c) perm.push_back(pos(tl, ch));
+    Tensor v = ct.permute(perm);
+    permute_add(c, v, alpha, beta, C);
+  }
+}
+
+}  // namespace ucc

@@ -1,0 +1,587 @@
+// FP64 kernels for the plain form of the RHF-CC solver (sm_103a).
+//
+//  * dgemm_kernel      -- register-blocked DFMA GEMM over arbitrarily strided operands,
+//                         with a permuting epilogue so that a contraction result lands
+//                         directly in its tensor layout (no separate transpose pass)
+//  * permute_kernel_*  -- tensor transposition with alpha/beta through a 32x33 shared tile
+//  * reductions        -- compensated (Neumaier) FP64 sums in two deterministic passes
+//  * amplitude kernels -- tau/ttau, Jacobi update with on-the-fly denominators, DIIS
+//                         linear combination
+//  * triples_energy    -- the (T) energy of ccwfn.cc:795-852 for a batch of i>=j>=k
+//                         tuples, reading W3 produced by the tuple GEMMs
+#include <atomic>
+#include <cstdio>
+
+#include "core.h"
+
+namespace ucc {
+
+static std::atomic<int64_t> g_launches{0};
+int64_t launches() { return g_launches.load(); }
+static inline void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+static void check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw Error(UCC_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// ------------------------------------------------------------------------------------
+// GEMM
+// ------------------------------------------------------------------------------------
+namespace {
+constexpr int BM = 64, BN = 64, BK = 16, GT = 256;
+
+struct GemmArgs {
+  int64_t M, N, K;
+  double alpha, beta;
+  const double* A;
+  int64_t sAm, sAk, bA;
+  const double* B;
+  int64_t sBk, sBn, bB;
+  double* C;
+  int64_t bC;
+  GemmEpilogue epi;
+  const GemmPtrs* ptrs;
+};
+
+template <bool AK, bool BN_>
+__global__ void __launch_bounds__(GT) dgemm_kernel(GemmArgs g) {
+  __shared__ double As[BK][BM + 1];
+  __shared__ double Bs[BK][BN + 1];
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
+  const double* A;
+  const double* B;
+  double* C;
+  if (g.ptrs) {
+    A = g.ptrs[blockIdx.z].A;
+    B = g.ptrs[blockIdx.z].B;
+    C = g.ptrs[blockIdx.z].C;
+  } else {
+    A = g.A + (int64_t)blockIdx.z * g.bA;
+    B = g.B + (int64_t)blockIdx.z * g.bB;
+    C = g.C + (int64_t)blockIdx.z * g.bC;
+  }
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[i][j] = 0.0;
+
+  for (int64_t k0 = 0; k0 < g.K; k0 += BK) {
+#pragma unroll
+    for (int r = 0; r < (BM * BK) / GT; r++) {
+      const int e = tid + r * GT;
+      int mm, kk;
+      if (AK) { mm = e / BK; kk = e % BK; } else { kk = e / BM; mm = e % BM; }
+      const int64_t m = m0 + mm, k = k0 + kk;
+      As[kk][mm] = (m < g.M && k < g.K) ? A[m * g.sAm + k * g.sAk] : 0.0;
+    }
+#pragma unroll
+    for (int r = 0; r < (BN * BK) / GT; r++) {
+      const int e = tid + r * GT;
+      int nn, kk;
+      if (BN_) { kk = e / BN; nn = e % BN; } else { nn = e / BK; kk = e % BK; }
+      const int64_t n = n0 + nn, k = k0 + kk;
+      Bs[kk][nn] = (n < g.N && k < g.K) ? B[k * g.sBk + n * g.sBn] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; kk++) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  const GemmEpilogue ep = g.epi;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int64_t m = m0 + ty + 16 * i;
+    if (m >= g.M) continue;
+    const int64_t mo = ep.msplit ? (m / ep.msplit) * ep.s_mhi + (m % ep.msplit) * ep.s_mlo : m * ep.s_mhi;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int64_t n = n0 + tx + 16 * j;
+      if (n >= g.N) continue;
+      double* cp = C + mo + n * ep.s_n;
+      const double v = g.alpha * acc[i][j];
+      *cp = (g.beta == 0.0) ? v : fma(g.beta, *cp, v);
+    }
+  }
+}
+}  // namespace
+
+void dgemm_strided(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                   const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi,
+                   int batch, int64_t bA, int64_t bB, int64_t bC, const GemmPtrs* ptrs) {
+  if (M <= 0 || N <= 0 || batch <= 0) return;
+  UCC_REQUIRE(batch <= 65535, UCC_BAD_ARGS, "dgemm: batch too large");
+  GemmArgs g{M, N, K, alpha, beta, A, sAm, sAk, bA, B, sBk, sBn, bB, C, bC, epi, ptrs};
+  dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM), (unsigned)batch);
+  UCC_REQUIRE(grid.y <= 65535, UCC_BAD_ARGS, "dgemm: M too large");
+  const bool ak = (sAk == 1) || (sAm != 1 && sAk < sAm);
+  const bool bn = (sBn == 1) || (sBk != 1 && sBn < sBk);
+  if (ak && bn)
+    dgemm_kernel<true, true><<<grid, GT, 0, c.stream>>>(g);
+  else if (ak)
+    dgemm_kernel<true, false><<<grid, GT, 0, c.stream>>>(g);
+  else if (bn)
+    dgemm_kernel<false, true><<<grid, GT, 0, c.stream>>>(g);
+  else
+    dgemm_kernel<false, false><<<grid, GT, 0, c.stream>>>(g);
+  count_launch();
+  check_launch("dgemm");
+}
+
+void dgemm(Ctx& c, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+           const double* B, int64_t ldb, double beta, double* C, const GemmEpilogue& epi, int batch, int64_t sA,
+           int64_t sB, int64_t sC, const GemmPtrs* ptrs) {
+  const int64_t sAm = ta ? 1 : lda, sAk = ta ? lda : 1;
+  const int64_t sBk = tb ? 1 : ldb, sBn = tb ? ldb : 1;
+  dgemm_strided(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, batch, sA, sB, sC, ptrs);
+}
+
+// ------------------------------------------------------------------------------------
+// Permutation: out (dense, dims od) = alpha * in(strides is, in out's axis order) + beta * out
+// ------------------------------------------------------------------------------------
+namespace {
+struct PermArgs {
+  int rank;
+  int64_t od[kMaxRank];
+  int64_t is[kMaxRank];
+  int64_t os[kMaxRank];
+  double alpha, beta;
+  const double* in;
+  double* out;
+  int64_t total;
+};
+
+__global__ void permute_kernel_elem(PermArgs a) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < a.total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rem = idx, off = 0, oo = 0;
+    for (int k = a.rank - 1; k >= 0; k--) {
+      const int64_t x = rem % a.od[k];
+      rem /= a.od[k];
+      off += x * a.is[k];
+      oo += x * a.os[k];
+    }
+    const double v = a.alpha * a.in[off];
+    a.out[oo] = (a.beta == 0.0) ? v : fma(a.beta, a.out[oo], v);
+  }
+}
+
+// Tile over output axis q (contiguous in the input) and the last output axis.
+struct TileArgs {
+  PermArgs p;
+  int q;
+  int nrest;
+  int64_t rd[kMaxRank];   // dims of the remaining axes
+  int64_t ris[kMaxRank];  // their input strides
+  int64_t ros[kMaxRank];  // their output strides
+  int64_t rest_total;
+  int64_t tiles_last;
+};
+
+__global__ void permute_kernel_tile(TileArgs t) {
+  __shared__ double tile[32][33];
+  const int r = t.p.rank;
+  const int64_t dl = t.p.od[r - 1], dq = t.p.od[t.q];
+  const int64_t tl = (blockIdx.x % t.tiles_last) * 32, tq = (blockIdx.x / t.tiles_last) * 32;
+  const int64_t isl = t.p.is[r - 1], osq = t.p.os[t.q];
+  for (int64_t rest = blockIdx.y; rest < t.rest_total; rest += gridDim.y) {
+    int64_t rem = rest, bi = 0, bo = 0;
+    for (int k = t.nrest - 1; k >= 0; k--) {
+      const int64_t x = rem % t.rd[k];
+      rem /= t.rd[k];
+      bi += x * t.ris[k];
+      bo += x * t.ros[k];
+    }
+    for (int jj = threadIdx.y; jj < 32; jj += blockDim.y) {
+      const int64_t xl = tl + jj, xq = tq + threadIdx.x;
+      if (xl < dl && xq < dq) tile[jj][threadIdx.x] = t.p.in[bi + xl * isl + xq];
+    }
+    __syncthreads();
+    for (int jj = threadIdx.y; jj < 32; jj += blockDim.y) {
+      const int64_t xq = tq + jj, xl = tl + threadIdx.x;
+      if (xl < dl && xq < dq) {
+        double* o = t.p.out + bo + xq * osq + xl * t.p.os[r - 1];
+        const double v = t.p.alpha * tile[threadIdx.x][jj];
+        *o = (t.p.beta == 0.0) ? v : fma(t.p.beta, *o, v);
+      }
+    }
+    __syncthreads();
+  }
+}
+}  // namespace
+
+void permute_add(Ctx& c, const Tensor& in, double alpha, double beta, const Tensor& out) {
+  UCC_REQUIRE(in.rank == out.rank, UCC_BAD_ARGS, "permute_add: rank mismatch");
+  PermArgs a{};
+  a.rank = out.rank;
+  a.total = out.size();
+  if (a.total == 0) return;
+  for (int k = 0; k < out.rank; k++) {
+    UCC_REQUIRE(in.d[k] == out.d[k], UCC_BAD_ARGS, "permute_add: dim mismatch");
+    a.od[k] = out.d[k];
+    a.is[k] = in.s[k];
+  }
+  for (int k = 0; k < out.rank; k++) a.os[k] = out.s[k];
+  a.alpha = alpha;
+  a.beta = beta;
+  a.in = in.p;
+  a.out = out.p;
+  const int r = out.rank;
+  int q = -1;
+  if (r >= 2 && in.s[r - 1] != 1 && out.s[r - 1] == 1 && out.d[r - 1] >= 8) {
+    for (int k = 0; k < r - 1; k++)
+      if (in.s[k] == 1 && out.d[k] >= 8) q = k;
+  }
+  if (q < 0) {
+    const int threads = 256;
+    const int64_t blocks = std::min<int64_t>((a.total + threads - 1) / threads, 152 * 64);
+    permute_kernel_elem<<<(unsigned)blocks, threads, 0, c.stream>>>(a);
+  } else {
+    TileArgs t{};
+    t.p = a;
+    t.q = q;
+    t.nrest = 0;
+    t.rest_total = 1;
+    for (int k = 0; k < r - 1; k++) {
+      if (k == q) continue;
+      t.rd[t.nrest] = a.od[k];
+      t.ris[t.nrest] = a.is[k];
+      t.ros[t.nrest] = a.os[k];
+      t.rest_total *= a.od[k];
+      t.nrest++;
+    }
+    t.tiles_last = (a.od[r - 1] + 31) / 32;
+    const int64_t tiles_q = (a.od[q] + 31) / 32;
+    dim3 grid((unsigned)(t.tiles_last * tiles_q), (unsigned)std::min<int64_t>(t.rest_total, 65535));
+    permute_kernel_tile<<<grid, dim3(32, 8), 0, c.stream>>>(t);
+  }
+  count_launch();
+  check_launch("permute");
+}
+
+// ------------------------------------------------------------------------------------
+// Elementwise
+// ------------------------------------------------------------------------------------
+namespace {
+__global__ void axpby_kernel(int64_t n, double alpha, const double* x, double beta, double* y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = alpha * x[i];
+    y[i] = (beta == 0.0) ? v : fma(beta, y[i], v);
+  }
+}
+__global__ void fill_kernel(int64_t n, double v, double* y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = v;
+}
+unsigned grid_for(int64_t n, int threads = 256) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, 152 * 32));
+}
+}  // namespace
+
+void axpby(Ctx& c, int64_t n, double alpha, const double* x, double beta, double* y) {
+  if (n <= 0) return;
+  axpby_kernel<<<grid_for(n), 256, 0, c.stream>>>(n, alpha, x, beta, y);
+  count_launch();
+  check_launch("axpby");
+}
+
+void fill(Ctx& c, int64_t n, double v, double* y) {
+  if (n <= 0) return;
+  fill_kernel<<<grid_for(n), 256, 0, c.stream>>>(n, v, y);
+  count_launch();
+  check_launch("fill");
+}
+
+// ------------------------------------------------------------------------------------
+// Compensated reductions.  Pass 1: each block writes (sum, compensation) of its
+// grid-stride share; pass 2: one block folds the partials.  Fixed grid => deterministic.
+// ------------------------------------------------------------------------------------
+namespace {
+constexpr int RED_BLOCKS = 512, RED_THREADS = 256;
+
+__device__ inline void neumaier(double& s, double& c, double x) {
+  const double t = s + x;
+  if (fabs(s) >= fabs(x))
+    c += (s - t) + x;
+  else
+    c += (x - t) + s;
+  s = t;
+}
+
+__device__ double block_sum(double v) {
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) / 32;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+  if (w == 0)
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// partial[(vec * gridDim.x + block)] ; x may be indexed per vector via xs
+__global__ void dot_pass1(int64_t n, const double* const* xs, const double* x0, const double* y, double* partial) {
+  const double* x = xs ? xs[blockIdx.y] : x0;
+  double s = 0.0, cc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    neumaier(s, cc, y ? x[i] * y[i] : x[i]);
+  const double tot = block_sum(s + cc);
+  if (threadIdx.x == 0) partial[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = tot;
+}
+
+__global__ void sum_pass2(int nparts, const double* partial, double* out) {
+  // one block per output
+  const double* p = partial + (int64_t)blockIdx.x * nparts;
+  double s = 0.0, cc = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) neumaier(s, cc, p[i]);
+  const double tot = block_sum(s + cc);
+  if (threadIdx.x == 0) out[blockIdx.x] = tot;
+}
+}  // namespace
+
+void dot_async(Ctx& c, int64_t n, const double* x, const double* y, double* d_out) {
+  Scratch part(c, sizeof(double) * RED_BLOCKS);
+  dot_pass1<<<dim3(RED_BLOCKS, 1), RED_THREADS, 0, c.stream>>>(n, nullptr, x, y, part.d());
+  sum_pass2<<<1, RED_THREADS, 0, c.stream>>>(RED_BLOCKS, part.d(), d_out);
+  count_launch();
+  count_launch();
+  check_launch("dot");
+}
+
+double dot(Ctx& c, int64_t n, const double* x, const double* y) {
+  Scratch out(c, sizeof(double));
+  dot_async(c, n, x, y, out.d());
+  double h = 0.0;
+  UCC_CUDA(cudaMemcpyAsync(&h, out.d(), sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  UCC_CUDA(cudaStreamSynchronize(c.stream));
+  return h;
+}
+
+void multidot_async(Ctx& c, int nvec, const double* const* d_xs, const double* y, int64_t n, double* d_out) {
+  if (nvec <= 0) return;
+  Scratch part(c, sizeof(double) * RED_BLOCKS * nvec);
+  dot_pass1<<<dim3(RED_BLOCKS, nvec), RED_THREADS, 0, c.stream>>>(n, d_xs, nullptr, y, part.d());
+  sum_pass2<<<nvec, RED_THREADS, 0, c.stream>>>(RED_BLOCKS, part.d(), d_out);
+  count_launch();
+  count_launch();
+  check_launch("multidot");
+}
+
+// ------------------------------------------------------------------------------------
+// Amplitude kernels
+// ------------------------------------------------------------------------------------
+namespace {
+__global__ void tau_kernel(int no, int nv, const double* t1, const double* t2, double f1, double* tau, double f2,
+                           double* ttau) {
+  const int64_t n = (int64_t)no * no * nv * nv;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(x % nv);
+    int64_t r = x / nv;
+    const int a = (int)(r % nv);
+    r /= nv;
+    const int j = (int)(r % no);
+    const int i = (int)(r / no);
+    const double tt = t1[(int64_t)i * nv + a] * t1[(int64_t)j * nv + b];
+    const double v = t2[x];
+    tau[x] = v + f1 * tt;
+    if (ttau) ttau[x] = v + f2 * tt;
+  }
+}
+
+// sum of squares of the residuals goes to partial[block]
+__global__ void jacobi_kernel(int no, int nv, const double* d_do, const double* d_dv, double shift, const double* R1,
+                              const double* R2, const double* t1o, const double* t2o, double* t1n, double* t2n,
+                              double* partial) {
+  const int64_t n1 = (int64_t)no * nv, n2 = (int64_t)no * no * nv * nv;
+  double s = 0.0, cc = 0.0;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n1 + n2;
+       x += (int64_t)gridDim.x * blockDim.x) {
+    if (x < n1) {
+      const int a = (int)(x % nv), i = (int)(x / nv);
+      const double r = R1[x];
+      neumaier(s, cc, r * r);
+      t1n[x] = t1o[x] + r / ((d_do[i] - d_dv[a]) + shift);
+    } else {
+      const int64_t y = x - n1;
+      const int b = (int)(y % nv);
+      int64_t q = y / nv;
+      const int a = (int)(q % nv);
+      q /= nv;
+      const int j = (int)(q % no);
+      const int i = (int)(q / no);
+      const double r = R2[y];
+      neumaier(s, cc, r * r);
+      const double D = ((d_do[i] + d_do[j]) - d_dv[a]) - d_dv[b];
+      t2n[y] = t2o[y] + r / (D + shift);
+    }
+  }
+  const double tot = block_sum(s + cc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+}
+
+__global__ void lincomb_kernel(int nvec, const double* const* vecs, const double* coef, int64_t n, double* out) {
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int p = 0; p < nvec; p++) s += coef[p] * vecs[p][x];
+    out[x] = s;
+  }
+}
+}  // namespace
+
+void build_tau(Ctx& c, int no, int nv, const double* t1, const double* t2, double f1, double* tau, double f2,
+               double* ttau) {
+  const int64_t n = (int64_t)no * no * nv * nv;
+  tau_kernel<<<grid_for(n), 256, 0, c.stream>>>(no, nv, t1, t2, f1, tau, f2, ttau);
+  count_launch();
+  check_launch("tau");
+}
+
+void jacobi_update(Ctx& c, int no, int nv, const double* d_do, const double* d_dv, double shift, const double* R1,
+                   const double* R2, const double* t1old, const double* t2old, double* t1new, double* t2new,
+                   double* d_sumsq) {
+  Scratch part(c, sizeof(double) * RED_BLOCKS);
+  jacobi_kernel<<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(no, nv, d_do, d_dv, shift, R1, R2, t1old, t2old, t1new,
+                                                          t2new, part.d());
+  sum_pass2<<<1, RED_THREADS, 0, c.stream>>>(RED_BLOCKS, part.d(), d_sumsq);
+  count_launch();
+  count_launch();
+  check_launch("jacobi");
+}
+
+void lincomb(Ctx& c, int nvec, const double* const* d_vecs, const double* coef, int64_t n, double* out) {
+  Scratch dc(c, sizeof(double) * nvec);
+  UCC_CUDA(cudaMemcpyAsync(dc.p, coef, sizeof(double) * nvec, cudaMemcpyHostToDevice, c.stream));
+  lincomb_kernel<<<grid_for(n), 256, 0, c.stream>>>(nvec, d_vecs, dc.d(), n, out);
+  count_launch();
+  check_launch("lincomb");
+  // the host coefficient array may go out of scope once the copy has been consumed
+  UCC_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+// ------------------------------------------------------------------------------------
+// (T) energy, ccwfn.cc:795-852.  One block per (tuple, a); threads over (b, c) with
+// a >= b >= c.  W3 holds nv^3 per tuple as W[a][b][c].
+// ------------------------------------------------------------------------------------
+namespace {
+__global__ void triples_energy_kernel(int no, int nv, const int* tuples, const double* W3, const double* t1,
+                                      const double* Voovv, const double* eps, double* partial) {
+  const int t = blockIdx.y;
+  const int a = blockIdx.x;
+  const int i = tuples[3 * t], j = tuples[3 * t + 1], k = tuples[3 * t + 2];
+  const int64_t nv2 = (int64_t)nv * nv;
+  const double* W = W3 + (int64_t)t * nv2 * nv;
+  const double* Vij = Voovv + ((int64_t)i * no + j) * nv2;
+  const double* Vik = Voovv + ((int64_t)i * no + k) * nv2;
+  const double* Vjk = Voovv + ((int64_t)j * no + k) * nv2;
+  const double* t1i = t1 + (int64_t)i * nv;
+  const double* t1j = t1 + (int64_t)j * nv;
+  const double* t1k = t1 + (int64_t)k * nv;
+  const double eijk = eps[i] + eps[j] + eps[k];
+  const double fac = 2.0 - (double)((i == j) + (i == k) + (j == k));
+  double s = 0.0, cc = 0.0;
+  const int npair = (a + 1) * (a + 1);
+  for (int q = threadIdx.x; q < npair; q += blockDim.x) {
+    const int b = q / (a + 1), c = q % (a + 1);
+    if (c > b) continue;
+    auto Wv = [&](int x, int y, int z) { return W[(int64_t)x * nv2 + (int64_t)y * nv + z]; };
+    auto Vv = [&](int x, int y, int z) {
+      const double num = Wv(x, y, z) + Vij[(int64_t)x * nv + y] * t1k[z] + Vik[(int64_t)x * nv + z] * t1j[y] +
+                         Vjk[(int64_t)y * nv + z] * t1i[x];
+      return num / (1.0 + (double)((x == y) + (x == z) + (y == z)));
+    };
+    const double wabc = Wv(a, b, c), wacb = Wv(a, c, b), wbac = Wv(b, a, c);
+    const double wbca = Wv(b, c, a), wcab = Wv(c, a, b), wcba = Wv(c, b, a);
+    const double vabc = Vv(a, b, c), vacb = Vv(a, c, b), vbac = Vv(b, a, c);
+    const double vbca = Vv(b, c, a), vcab = Vv(c, a, b), vcba = Vv(c, b, a);
+    const double X3 = wabc * vabc + wacb * vacb + wbac * vbac + wbca * vbca + wcab * vcab + wcba * vcba;
+    const double Y3 = vabc + vbca + vcab;
+    const double Z3 = vacb + vbac + vcba;
+    const double denom = eijk - (eps[no + a] + eps[no + b] + eps[no + c]);
+    const double e = ((Y3 - 2.0 * Z3) * (wabc + wbca + wcab) + (Z3 - 2.0 * Y3) * (wacb + wbac + wcba) + 3.0 * X3) *
+                     fac / denom;
+    neumaier(s, cc, e);
+  }
+  const double tot = block_sum(s + cc);
+  if (threadIdx.x == 0) partial[(int64_t)t * nv + a] = tot;
+}
+}  // namespace
+
+void triples_energy(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const double* W3, const double* t1,
+                    const double* Voovv, const double* eps, double* d_partial) {
+  UCC_REQUIRE(ntuple <= 65535, UCC_BAD_ARGS, "triples_energy: too many tuples per batch");
+  dim3 grid((unsigned)nv, (unsigned)ntuple);
+  triples_energy_kernel<<<grid, 256, 0, c.stream>>>(no, nv, d_tuples, W3, t1, Voovv, eps, d_partial);
+  count_launch();
+  check_launch("triples_energy");
+}
+
+
+// ------------------------------------------------------------------------------------
+// GEMV: y[n] = alpha * sum_k x[k] * A[k*sk + n*sn] + beta * y[n*sy]  (contractions whose
+// free side is a single vector; a 64x64 GEMM tile would waste 63/64 of its work)
+// ------------------------------------------------------------------------------------
+namespace {
+__global__ void gemv_ncontig(int64_t N, int64_t K, double alpha, const double* x, int64_t sx, const double* A,
+                             int64_t sk, int64_t sn, double beta, double* y, int64_t sy) {
+  // blockDim = (32, 8): threadIdx.x over n (coalesced when sn == 1), threadIdx.y over k
+  __shared__ double red[8][33];
+  const int64_t n = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  double s = 0.0;
+  if (n < N)
+    for (int64_t k = threadIdx.y; k < K; k += 8) s = fma(x[k * sx], A[k * sk + n * sn], s);
+  red[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && n < N) {
+    double t = 0.0;
+    for (int r = 0; r < 8; r++) t += red[r][threadIdx.x];
+    double* o = y + n * sy;
+    *o = (beta == 0.0) ? alpha * t : fma(beta, *o, alpha * t);
+  }
+}
+__global__ void gemv_kcontig(int64_t N, int64_t K, double alpha, const double* x, int64_t sx, const double* A,
+                             int64_t sk, int64_t sn, double beta, double* y, int64_t sy) {
+  // one warp per n, lanes over k (coalesced when sk == 1)
+  const int64_t n = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x % 32;
+  if (n >= N) return;
+  double s = 0.0;
+  for (int64_t k = lane; k < K; k += 32) s = fma(x[k * sx], A[k * sk + n * sn], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    double* op = y + n * sy;
+    *op = (beta == 0.0) ? alpha * s : fma(beta, *op, alpha * s);
+  }
+}
+}  // namespace
+
+void dgemv_strided(Ctx& c, int64_t N, int64_t K, double alpha, const double* x, int64_t sx, const double* A,
+                   int64_t sk, int64_t sn, double beta, double* y, int64_t sy) {
+  if (N <= 0) return;
+  if (sk == 1 && sn != 1) {
+    const int wpb = 8;
+    gemv_kcontig<<<(unsigned)((N + wpb - 1) / wpb), 32 * wpb, 0, c.stream>>>(N, K, alpha, x, sx, A, sk, sn, beta, y,
+                                                                            sy);
+  } else {
+    gemv_ncontig<<<(unsigned)((N + 31) / 32), dim3(32, 8), 0, c.stream>>>(N, K, alpha, x, sx, A, sk, sn, beta, y, sy);
+  }
+  count_launch();
+  check_launch("gemv");
+}
+
+}  // namespace ucc

@@ -1,0 +1,121 @@
+// (T) correction: the i>=j>=k W/V algorithm of ccwfn.cc:795-852 with W3_ijk (:1388-1418).
+//
+// W3[a,b,c] for a tuple (i,j,k) is a sum of six "e" terms (<xe|..> t2, K = nv) and six
+// "m" terms (<..|mc> t2, K = no).  They pair up by output permutation, so with
+//   A_x[k'][ab] = [ <xe|ab> for e ; -t2[x][m][a][b] for m ]           (nv+no) x nv^2
+//   B_yz[k'][c] = [ t2[y][z][c][e] for e ; <zy|mc> for m ]           (nv+no) x nv
+// every pair is one GEMM  G = A_x^T B_yz  (M = nv^2, N = nv, K = nv+no) whose epilogue
+// writes G[(u,v), w] straight into W3 at the permuted position:
+//   x=i (y,z)=(k,j) -> W[a][b][c]    x=i (j,k) -> W[a][c][b]    x=k (j,i) -> W[c][a][b]
+//   x=k (i,j)       -> W[c][b][a]    x=j (i,k) -> W[b][c][a]    x=j (k,i) -> W[b][a][c]
+// Tuples are processed in batches (one batched launch per term), then the energy kernel
+// forms V3, X3, Y3, Z3 and the a>=b>=c weighted sum per tuple.
+#include <algorithm>
+#include <cmath>
+
+#include "cc.h"
+
+namespace ucc {
+
+double flops_triples(double no, double nv) { return 2.0 * no * (no + 1) * (no + 2) * nv * nv * nv * (nv + no); }
+
+// mixed-precision tuple GEMMs (tc_gemm.cu); false if not available for this shape
+bool mixed_triples_batch(Ctx& c, int nbatch, const int* h_tuples, double* W3);
+bool mixed_triples_prepare(Ctx& c);
+
+double run_triples(Ctx& c) {
+  UCC_REQUIRE(c.have_ccsd, UCC_BAD_STATE, "(T) needs converged CCSD amplitudes");
+  const int no = c.no, nv = c.nv;
+  const int64_t nv2 = (int64_t)nv * nv, nv3 = nv2 * nv, Kp = nv + no;
+  double* T = c.get("T").p;
+  Tensor t1 = amp1(c, T), t2 = amp2(c, T);
+
+  // concatenated operands
+  Tensor Acat = c.alloc("T3_A", {no, Kp, nv2}, false);
+  {
+    Tensor Ae = narrow(Acat, 1, 0, nv), Am = narrow(Acat, 1, nv, no);
+    Tensor Vovvv = c.get("Vovvv");
+    Tensor src = make_view(Vovvv.p, {no, nv, nv2});
+    permute_add(c, src, 1.0, 0.0, Ae);
+    Tensor t2v = make_view(t2.p, {no, no, nv2});
+    permute_add(c, t2v, -1.0, 0.0, Am);
+  }
+  Tensor Bcat = c.alloc("T3_B", {no, no, Kp, nv}, false);
+  {
+    Tensor Be = narrow(Bcat, 2, 0, nv), Bm = narrow(Bcat, 2, nv, no);
+    permute_add(c, view(t2, "yzce->yzec"), 1.0, 0.0, Be);
+    permute_add(c, view(c.get("Vooov"), "zymc->yzmc"), 1.0, 0.0, Bm);
+  }
+
+  std::vector<int> tuples;
+  for (int i = 0; i < no; i++)
+    for (int j = 0; j <= i; j++)
+      for (int k = 0; k <= j; k++) {
+        tuples.push_back(i);
+        tuples.push_back(j);
+        tuples.push_back(k);
+      }
+  const int ntup = (int)tuples.size() / 3;
+  size_t free_b = 0, total_b = 0;
+  UCC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const double budget = std::min<double>(8.0e9, 0.25 * (double)free_b);
+  const int batch = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)(budget / (8.0 * nv3)), 4096, ntup}));
+
+  Scratch dtup(c, sizeof(int) * tuples.size());
+  UCC_CUDA(cudaMemcpyAsync(dtup.p, tuples.data(), sizeof(int) * tuples.size(), cudaMemcpyHostToDevice, c.stream));
+  Scratch W3(c, sizeof(double) * nv3 * batch);
+  Scratch partial(c, sizeof(double) * (size_t)ntup * nv);
+
+  const bool mixed = c.opt.precision == UCC_MIXED && !c.force_fp64 && mixed_triples_prepare(c);
+  // term table: x, y, z selectors into (i,j,k) and the W3 strides of (u, v, w)
+  struct Term {
+    int x, y, z;
+    int64_t su, sv, sw;
+  };
+  const Term terms[6] = {{0, 2, 1, nv2, nv, 1}, {0, 1, 2, nv2, 1, nv}, {2, 1, 0, 1, nv2, nv},
+                         {2, 0, 1, 1, nv, nv2}, {1, 0, 2, nv, 1, nv2}, {1, 2, 0, nv, nv2, 1}};
+  std::vector<GemmPtrs> hp((size_t)batch);
+  Scratch dptr(c, sizeof(GemmPtrs) * batch * 6);
+  GemmPtrs* dp = static_cast<GemmPtrs*>(dptr.p);
+  for (int t0 = 0; t0 < ntup; t0 += batch) {
+    const int nb = std::min(batch, ntup - t0);
+    if (mixed) {
+      mixed_triples_batch(c, nb, tuples.data() + 3 * t0, W3.d());
+    } else {
+      std::vector<GemmPtrs> all((size_t)nb * 6);
+      for (int q = 0; q < 6; q++)
+        for (int b = 0; b < nb; b++) {
+          const int* ijk = &tuples[3 * (t0 + b)];
+          const Term& tm = terms[q];
+          all[(size_t)q * nb + b] = {Acat.p + (int64_t)ijk[tm.x] * Kp * nv2,
+                                     Bcat.p + ((int64_t)ijk[tm.y] * no + ijk[tm.z]) * Kp * nv,
+                                     W3.d() + (int64_t)b * nv3};
+        }
+      UCC_CUDA(cudaMemcpyAsync(dp, all.data(), sizeof(GemmPtrs) * all.size(), cudaMemcpyHostToDevice, c.stream));
+      for (int q = 0; q < 6; q++) {
+        GemmEpilogue epi;
+        epi.msplit = nv;
+        epi.s_mhi = terms[q].su;
+        epi.s_mlo = terms[q].sv;
+        epi.s_n = terms[q].sw;
+        dgemm_strided(c, nv2, nv, Kp, 1.0, nullptr, 1, nv2, nullptr, nv, 1, q == 0 ? 0.0 : 1.0, nullptr, epi, nb, 0,
+                      0, 0, dp + (size_t)q * nb);
+      }
+      // the pointer array is reused by the next batch: keep the copy ordered after use
+      UCC_CUDA(cudaStreamSynchronize(c.stream));
+    }
+    triples_energy(c, no, nv, nb, static_cast<int*>(dtup.p) + 3 * t0, W3.d(), t1.p, c.get("Voovv").p,
+                   c.get("eps").p, partial.d() + (int64_t)t0 * nv);
+  }
+  Scratch et(c, sizeof(double));
+  dot_async(c, (int64_t)ntup * nv, partial.d(), nullptr, et.d());
+  double e = 0.0;
+  UCC_CUDA(cudaMemcpyAsync(&e, et.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  UCC_CUDA(cudaStreamSynchronize(c.stream));
+  c.drop("T3_A");
+  c.drop("T3_B");
+  UCC_REQUIRE(std::isfinite(e), UCC_NAN_DETECTED, "(T) energy is not finite");
+  return e;
+}
+
+}  // namespace ucc
