@@ -13,6 +13,8 @@ struct ucc_ctx {
 
 namespace ucc {
 Ctx::~Ctx() {
+  if (stream) cudaStreamSynchronize(stream);
+  tc_cache.reset();
   perts.clear();
   store.clear();
   if (stream) cudaStreamDestroy(stream);
@@ -40,6 +42,8 @@ ucc_status guard(ucc_ctx* ctx, F&& f) {
 }
 
 void reset_state(Ctx& c) {
+  cudaStreamSynchronize(c.stream);
+  c.tc_cache.reset();
   c.perts.clear();
   c.store.clear();
   c.shapes.clear();

@@ -118,6 +118,10 @@ struct Ctx {
   void drop(const std::string& name);
 
   bool force_fp64 = false;  // integral construction and refinement sweeps stay FP64
+  // state of the tensor-core path (split operand cache, error flag), dropped on reload
+  std::shared_ptr<void> tc_cache;
+  // true if p lies in a block that never changes once built (integrals, L, HBAR)
+  bool is_constant(const double* p) const;
   std::vector<std::unique_ptr<Perturbation>> perts;
   ucc_stats stats{};
 

@@ -97,6 +97,16 @@ Tensor Ctx::alloc(const std::string& name, const std::vector<int64_t>& dims, boo
   return make_view(store[name]->p, dims);
 }
 
+bool Ctx::is_constant(const double* p) const {
+  for (const auto& kv : store) {
+    const std::string& n = kv.first;
+    const bool block = n[0] == 'V' || (n[0] == 'H' && n != "Hdiag") || n == "Loovv" || n == "Looov" ||
+                       n == "Lovvv" || n == "Lovvo";
+    if (block && p >= kv.second->p && p < kv.second->p + kv.second->n) return true;
+  }
+  return false;
+}
+
 void Ctx::drop(const std::string& name) {
   store.erase(name);
   shapes.erase(name);

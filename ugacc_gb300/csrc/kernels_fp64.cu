@@ -19,6 +19,7 @@ namespace ucc {
 static std::atomic<int64_t> g_launches{0};
 int64_t launches() { return g_launches.load(); }
 static inline void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_kernel_launch() { count_launch(); }
 
 static void check_launch(const char* what) {
   cudaError_t e = cudaGetLastError();
