@@ -88,6 +88,21 @@ ucc_status ucc_pert_solve(ucc_ctx* ctx, int handle, int hand, double* pseudoresp
 /* Replaces: CCResp::linresp(X, Y) (ccresp.cc:28-124). */
 ucc_status ucc_linresp(ucc_ctx* ctx, int handle_x, int handle_y, double* value);
 
+/* (T) correction computed without allocating any device memory.  No counterpart in the
+ * reference: it serves host programs that cannot let a library call cudaMalloc (all
+ * device memory belongs to their own arena, or must not be allocated on this path).
+ * Inputs are caller-owned device arrays: t1 [no][nv], t2 [no][no][nv][nv], eps [no+nv]
+ * (orbital energies), ovvv [no][nv][nv][nv] = <ie|ab>, ooov [no][no][no][nv] = <jk|mc>,
+ * oovv [no][no][nv][nv] = <ij|ab>; e_t is host memory.  Working memory is one static
+ * 32 MiB device array per GPU: nv^3 + nv * no(no+1)(no+2)/6 doubles must fit, otherwise
+ * UCC_BAD_ARGS with a message in errbuf.  Calls share that array: do not let two calls
+ * overlap on the GPU.  The first call on a device looks up the array's address; make it
+ * before any stream capture.  stream may be NULL; the call returns after the result is
+ * on the host. */
+ucc_status ucc_triples_noalloc(int no, int nv, const double* t1, const double* t2, const double* eps,
+                               const double* ovvv, const double* ooov, const double* oovv, double* e_t,
+                               void* stream, char* errbuf, size_t errlen);
+
 /* Copy-out of named arrays: "t1" "t2" "tau" "l1" "l2" "Doo" "Dvv" "Dov" "Dvo" and the
  * HBAR blocks "Hov" "Hoo" "Hvv" "Hoooo" "Hvvvv" "Hvovv" "Hooov" "Hovvo" "Hovov" "Hvvvo"
  * "Hovoo"; per perturbation "X1:<h>" "X2:<h>" "Y1:<h>" "Y2:<h>".  count = elements. */

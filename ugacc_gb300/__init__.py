@@ -96,6 +96,7 @@ def load_library(path: str | None = None):
         "ucc_reset_stats": (i, [vp]),
         "ucc_last_error": (cp, [vp]),
         "ucc_status_string": (cp, [i]),
+        "ucc_triples_noalloc": (i, [i, i, vp, vp, vp, vp, vp, vp, dp, vp, cp, ctypes.c_size_t]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
