@@ -88,6 +88,14 @@ ucc_status ucc_pert_solve(ucc_ctx* ctx, int handle, int hand, double* pseudoresp
 /* Replaces: CCResp::linresp(X, Y) (ccresp.cc:28-124). */
 ucc_status ucc_linresp(ucc_ctx* ctx, int handle_x, int handle_y, double* value);
 
+/* C = alpha * op(A) op(B) + beta * C on host row-major float64 buffers, computed by the
+ * library's FP64 GEMM (precision UCC_FP64) or its tensor-core BF16 hi+lo split GEMM
+ * (UCC_MIXED, FP32 accumulation).  No counterpart in the reference (its contractions are
+ * inline loops); this is the building block every contraction above runs on.
+ * op(A) is M x K (transa: A stored K x M), op(B) is K x N (transb: B stored N x K). */
+ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t M, int64_t N, int64_t K,
+                    double alpha, const double* A, const double* B, double beta, double* C);
+
 /* (T) correction computed without allocating any device memory.  No counterpart in the
  * reference: it serves host programs that cannot let a library call cudaMalloc (all
  * device memory belongs to their own arena, or must not be allocated on this path).
@@ -120,6 +128,8 @@ typedef struct ucc_stats {
   double ladder_bytes;       /* its algorithmic operand bytes, summed */
   double ladder_flops;       /* its algorithmic FLOPs, summed */
   int64_t ladder_launches;
+  int fp64_iterations;       /* CCSD iterations whose residual was built in FP64 */
+  int64_t tc_gemm_launches;  /* tensor-core (BF16 split) GEMM launches */
 } ucc_stats;
 ucc_status ucc_get_stats(ucc_ctx* ctx, ucc_stats* out);
 ucc_status ucc_reset_stats(ucc_ctx* ctx);

@@ -1,0 +1,53 @@
+"""Tensor-core (tcgen05, BF16 hi+lo split, FP32 accumulate) path against FP64."""
+import numpy as np
+import pytest
+
+import ugacc_gb300 as U
+from ugacc_gb300.generator import make_hamiltonian
+
+pytestmark = pytest.mark.gpu
+
+# Two-term split products keep ~16 significant bits per operand: relative error of a
+# GEMM element is bounded by ~2^-16 of the sum of |products|.
+SPLIT_RTOL = 4e-5
+
+
+@pytest.mark.parametrize("M,N,K,ta,tb", [(128, 256, 64, 0, 0), (300, 520, 777, 0, 1), (257, 129, 1000, 1, 0),
+                                          (1000, 300, 96, 1, 1)])
+def test_tc_gemm_against_fp64(M, N, K, ta, tb):
+    rng = np.random.default_rng(M + N + K)
+    A = rng.standard_normal((K, M) if ta else (M, K))
+    B = rng.standard_normal((N, K) if tb else (K, N))
+    C0 = rng.standard_normal((M, N))
+    ctx = U.Context()
+    ref = 0.7 * (A.T if ta else A) @ (B.T if tb else B) - 0.3 * C0
+    got = ctx.gemm(A, B, C0, alpha=0.7, beta=-0.3, transa=ta, transb=tb, precision=U.MIXED)
+    scale = 0.7 * np.abs(A.T if ta else A) @ np.abs(B.T if tb else B)
+    assert np.all(np.abs(got - ref) <= SPLIT_RTOL * scale + 1e-12)
+    f64 = ctx.gemm(A, B, C0, alpha=0.7, beta=-0.3, transa=ta, transb=tb, precision=U.FP64)
+    np.testing.assert_allclose(f64, ref, rtol=1e-12, atol=1e-10)
+
+
+def test_mixed_refined_ccsd_matches_fp64():
+    h = make_hamiltonian(12, 64, 9)
+    H = U.Hamiltonian.from_synthetic(h)
+    cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10})
+    e64 = cc.compute_energy()
+    t2 = cc.t2
+    H.ctx.reset_stats()
+    mx = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": "MIXED", "REFINE_SWEEPS": 2})
+    emx = mx.compute_energy()
+    st = H.ctx.stats()
+    assert st["tc_gemm_launches"] > 0 and st["fp64_iterations"] >= 2
+    assert abs(emx - e64) < 1e-9
+    np.testing.assert_allclose(mx.t2, t2, atol=1e-9, rtol=0)
+
+
+def test_mixed_unrefined_within_one_microhartree():
+    h = make_hamiltonian(12, 64, 9)
+    H = U.Hamiltonian.from_synthetic(h)
+    e64 = U.CCWfn(H, {"R_CONVERGENCE": 1e-8}).compute_energy()
+    mx = U.CCWfn(H, {"R_CONVERGENCE": 1e-5, "PRECISION": "MIXED", "REFINE_SWEEPS": 0})
+    emx = mx.compute_energy()
+    assert H.ctx.stats()["fp64_iterations"] == 0
+    assert abs(emx - e64) < 1e-6

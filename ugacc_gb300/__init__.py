@@ -49,7 +49,8 @@ class Stats(ctypes.Structure):
                 ("ccsd_iterations", ctypes.c_int), ("lambda_iterations", ctypes.c_int),
                 ("kernel_launches", ctypes.c_int64), ("ladder_ms", ctypes.c_double),
                 ("ladder_bytes", ctypes.c_double), ("ladder_flops", ctypes.c_double),
-                ("ladder_launches", ctypes.c_int64)]
+                ("ladder_launches", ctypes.c_int64), ("fp64_iterations", ctypes.c_int),
+                ("tc_gemm_launches", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -97,6 +98,7 @@ def load_library(path: str | None = None):
         "ucc_last_error": (cp, [vp]),
         "ucc_status_string": (cp, [i]),
         "ucc_triples_noalloc": (i, [i, i, vp, vp, vp, vp, vp, vp, dp, vp, cp, ctypes.c_size_t]),
+        "ucc_gemm": (i, [vp, i, i, i, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, d, dp, dp, d, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -141,6 +143,17 @@ class Context:
     def set(self, name: str, arr: np.ndarray):
         a = np.ascontiguousarray(arr, dtype=np.float64)
         self.check(self.lib.ucc_set_tensor(self.h, name.encode(), _ptr(a), a.size))
+
+    def gemm(self, A, B, C=None, alpha=1.0, beta=0.0, transa=False, transb=False, precision=FP64):
+        """C = alpha op(A) op(B) + beta C on the GPU (ucc_gemm)."""
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        M, K = (A.shape[1], A.shape[0]) if transa else A.shape
+        N = B.shape[0] if transb else B.shape[1]
+        C = np.zeros((M, N)) if C is None else np.array(C, dtype=np.float64, order="C")
+        self.check(self.lib.ucc_gemm(self.h, precision, int(transa), int(transb), M, N, K, alpha, _ptr(A), _ptr(B),
+                                     beta, _ptr(C)))
+        return C
 
     def stats(self) -> dict:
         s = Stats()

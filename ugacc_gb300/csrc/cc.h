@@ -64,6 +64,23 @@ inline int64_t npacked(const Ctx& c) {
   return (int64_t)c.no * c.nv + (int64_t)c.no * c.no * c.nv * c.nv;
 }
 
+// The six W3 terms of a (T) tuple (i,j,k): A operand of occupied index x, B operand of
+// the ordered pair (y,z) (selectors into (i,j,k)), and the W3[a][b][c] strides of the GEMM
+// output G[(u,v), w] (see triples.cpp).
+struct TriplesTerm {
+  int x, y, z;
+  int64_t su, sv, sw;
+};
+inline void triples_terms(int64_t nv, TriplesTerm t[6]) {
+  const int64_t nv2 = nv * nv;
+  t[0] = {0, 2, 1, nv2, nv, 1};
+  t[1] = {0, 1, 2, nv2, 1, nv};
+  t[2] = {2, 1, 0, 1, nv2, nv};
+  t[3] = {2, 0, 1, 1, nv, nv2};
+  t[4] = {1, 0, 2, nv, 1, nv2};
+  t[5] = {1, 2, 0, nv, nv2, 1};
+}
+
 // algorithmic FLOP counts (2 per multiply-add, no symmetry credit)
 double flops_ccsd_iter(double no, double nv);
 double flops_triples(double no, double nv);

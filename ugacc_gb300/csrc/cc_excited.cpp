@@ -17,6 +17,7 @@ using V4 = std::vector<int64_t>;
 
 void run_hbar(Ctx& c) {
   UCC_REQUIRE(c.have_ccsd, UCC_BAD_STATE, "HBAR needs converged CCSD amplitudes");
+  Fp64Scope fp64(c);  // HBAR, Lambda, densities and response run in FP64
   const int no = c.no, nv = c.nv;
   double* T = c.get("T").p;
   Tensor t1 = amp1(c, T), t2 = amp2(c, T), tau = c.get("tau");
@@ -200,6 +201,7 @@ void lambda_l2(Ctx& c, const Tensor& l1, const Tensor& l2, const Tensor& Goo, co
 
 CCSDResult run_lambda(Ctx& c) {  // :93-129
   UCC_REQUIRE(c.have_hbar, UCC_BAD_STATE, "Lambda needs HBAR");
+  Fp64Scope fp64(c);
   const int no = c.no, nv = c.nv;
   const int64_t np = npacked(c), n1 = (int64_t)no * nv;
   Tensor Lam = c.alloc("Lam", {np}, false);
@@ -262,6 +264,7 @@ CCSDResult run_lambda(Ctx& c) {  // :93-129
 // ---------------------------------------------------------------------------------------
 void run_density(Ctx& c, double* e1, double* e2) {
   UCC_REQUIRE(c.have_lambda, UCC_BAD_STATE, "densities need converged Lambda amplitudes");
+  Fp64Scope fp64(c);
   const int no = c.no, nv = c.nv;
   double* T = c.get("T").p;
   double* Lp = c.get("Lam").p;

@@ -384,6 +384,9 @@ double energy(Ctx& c, const Tensor& t1, const Tensor& tau) {
 
 }  // namespace
 
+// residual norm below which BF16 hi+lo split products stop resolving the update
+constexpr double kMixedFloor = 1e-6;
+
 CCSDResult run_ccsd(Ctx& c) {
   UCC_REQUIRE(c.loaded, UCC_BAD_STATE, "no Hamiltonian loaded");
   const int no = c.no, nv = c.nv;
@@ -428,7 +431,13 @@ CCSDResult run_ccsd(Ctx& c) {
   }
   Diis diis(c, np, 8);
   std::vector<cudaEvent_t> ev;
-  double rms = INFINITY, eccsd = NAN;
+  double rms = INFINITY, rms_prev = INFINITY, eccsd = NAN;
+  // Mixed precision: residuals from BF16 hi+lo split GEMMs until the residual norm
+  // reaches the split-product noise floor (or stops falling), then FP64 sweeps until
+  // ||R|| < r_convergence; at least refine_sweeps FP64 iterations close the solve.
+  const bool mixed = c.opt.precision == UCC_MIXED;
+  bool fp64_phase = !mixed;
+  int fp64_iters = 0;
   int iter = 0;
   for (iter = 1; iter <= c.opt.maxiter; iter++) {
     c.store["T"].swap(c.store["Told"]);  // amp_save, ccwfn.cc:300-309
@@ -436,10 +445,13 @@ CCSDResult run_ccsd(Ctx& c) {
     double* tn = c.get("T").p;
     double* r = c.get("R").p;
     Tensor t1 = amp1(c, to), t2 = amp2(c, to);
-    build_F(c, t1, c.get("ttau"));
-    build_W(c, t1, t2, c.get("tau"));
-    build_t1(c, t1, t2, amp1(c, r));
-    build_t2(c, t1, t2, c.get("tau"), amp2(c, r), &ev);
+    {
+      Fp64Scope scope(c, fp64_phase);
+      build_F(c, t1, c.get("ttau"));
+      build_W(c, t1, t2, c.get("tau"));
+      build_t1(c, t1, t2, amp1(c, r));
+      build_t2(c, t1, t2, c.get("tau"), amp2(c, r), &ev);
+    }
     jacobi_update(c, no, nv, d_do, d_dv, 0.0, r, r + (int64_t)no * nv, to, to + (int64_t)no * nv, tn,
                   tn + (int64_t)no * nv, sumsq.d());
     double ss = 0.0;
@@ -447,7 +459,13 @@ CCSDResult run_ccsd(Ctx& c) {
     UCC_CUDA(cudaStreamSynchronize(c.stream));
     rms = std::sqrt(ss);
     UCC_REQUIRE(std::isfinite(rms), UCC_NAN_DETECTED, "CCSD residual is not finite");
-    if (rms < c.opt.r_convergence) break;
+    if (fp64_phase) fp64_iters++;
+    const bool refined = !mixed || c.opt.refine_sweeps == 0 || (fp64_phase && fp64_iters >= c.opt.refine_sweeps);
+    if (rms < c.opt.r_convergence && refined) break;
+    if (mixed && !fp64_phase && c.opt.refine_sweeps > 0 &&
+        (rms < std::max(c.opt.r_convergence, kMixedFloor) || (iter > 2 && rms > 0.5 * rms_prev)))
+      fp64_phase = true;
+    rms_prev = rms;
     if (c.opt.diis) {
       diis.add(tn, to);
       if (diis.size() > 2) diis.extrapolate(tn);
@@ -475,6 +493,7 @@ CCSDResult run_ccsd(Ctx& c) {
   res.iterations = std::min(iter, c.opt.maxiter);
   res.e_ccsd = eccsd;
   res.converged = rms < c.opt.r_convergence;
+  c.stats.fp64_iterations = fp64_iters;
   c.have_ccsd = res.converged;
   return res;
 }

@@ -367,6 +367,7 @@ double pseudoresponse(Ctx& c, Perturbation& p, double* amps) {  // ccpert.cc:233
 
 int pert_create(Ctx& c, const double* pert, double omega) {
   UCC_REQUIRE(c.have_lambda, UCC_BAD_STATE, "perturbed wavefunctions need HBAR and Lambda");
+  Fp64Scope fp64(c);
   const int no = c.no, nv = c.nv, n = no + nv;
   auto pp = std::make_unique<Perturbation>();
   pp->id = (int)c.perts.size();
@@ -411,6 +412,7 @@ int pert_create(Ctx& c, const double* pert, double omega) {
 
 CCSDResult pert_solve(Ctx& c, int h, bool right) {  // ccpert.cc:177-229
   Perturbation& p = get_pert(c, h);
+  Fp64Scope fp64(c);
   UCC_REQUIRE(right || p.right_done, UCC_BAD_STATE, "left-hand solve needs the right-hand solution");
   const int no = c.no, nv = c.nv;
   const int64_t np = npacked(c), n1 = (int64_t)no * nv;
@@ -457,6 +459,7 @@ CCSDResult pert_solve(Ctx& c, int h, bool right) {  // ccpert.cc:177-229
 
 double linresp(Ctx& c, int hx, int hy) {  // ccresp.cc:28-124
   Perturbation& X = get_pert(c, hx);
+  Fp64Scope fp64(c);
   Perturbation& Y = get_pert(c, hy);
   const int no = c.no, nv = c.nv;
   double* Lp = c.get("Lam").p;

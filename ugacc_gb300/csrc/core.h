@@ -97,6 +97,15 @@ struct Timer {  // CUDA events on the context stream
 };
 
 struct Perturbation;  // cc_pert.cpp
+struct Ctx;
+
+// Scoped switch that keeps every contraction in FP64 (Hamiltonian build, refinement).
+struct Fp64Scope {
+  Ctx& c;
+  bool saved;
+  explicit Fp64Scope(Ctx& ctx, bool on = true);
+  ~Fp64Scope();
+};
 
 struct Ctx {
   int device = 0;

@@ -97,6 +97,11 @@ Tensor Ctx::alloc(const std::string& name, const std::vector<int64_t>& dims, boo
   return make_view(store[name]->p, dims);
 }
 
+Fp64Scope::Fp64Scope(Ctx& ctx, bool on) : c(ctx), saved(ctx.force_fp64) {
+  if (on) c.force_fp64 = true;
+}
+Fp64Scope::~Fp64Scope() { c.force_fp64 = saved; }
+
 bool Ctx::is_constant(const double* p) const {
   for (const auto& kv : store) {
     const std::string& n = kv.first;

@@ -9,8 +9,10 @@
 //                         linear combination
 //  * triples_energy    -- the (T) energy of ccwfn.cc:795-852 for a batch of i>=j>=k
 //                         tuples, reading W3 produced by the tuple GEMMs
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
+#include <memory>
 
 #include "core.h"
 
@@ -34,6 +36,8 @@ constexpr int BM = 64, BN = 64, BK = 16, GT = 256;
 
 struct GemmArgs {
   int64_t M, N, K;
+  int64_t kchunk;  // > 0: split-K, blockIdx.z selects K range [z*kchunk, min(K,(z+1)*kchunk)) and the
+                   // tile goes to C + z*M*N as a plain row-major partial (alpha = 1, beta = 0)
   double alpha, beta;
   const double* A;
   int64_t sAm, sAk, bA;
@@ -55,10 +59,17 @@ __global__ void __launch_bounds__(GT) dgemm_kernel(GemmArgs g) {
   const double* A;
   const double* B;
   double* C;
+  int64_t kbeg = 0, kend = g.K;
   if (g.ptrs) {
     A = g.ptrs[blockIdx.z].A;
     B = g.ptrs[blockIdx.z].B;
     C = g.ptrs[blockIdx.z].C;
+  } else if (g.kchunk > 0) {
+    A = g.A;
+    B = g.B;
+    C = g.C + (int64_t)blockIdx.z * g.M * g.N;
+    kbeg = (int64_t)blockIdx.z * g.kchunk;
+    kend = min(g.K, kbeg + g.kchunk);
   } else {
     A = g.A + (int64_t)blockIdx.z * g.bA;
     B = g.B + (int64_t)blockIdx.z * g.bB;
@@ -70,14 +81,14 @@ __global__ void __launch_bounds__(GT) dgemm_kernel(GemmArgs g) {
 #pragma unroll
     for (int j = 0; j < 4; j++) acc[i][j] = 0.0;
 
-  for (int64_t k0 = 0; k0 < g.K; k0 += BK) {
+  for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
 #pragma unroll
     for (int r = 0; r < (BM * BK) / GT; r++) {
       const int e = tid + r * GT;
       int mm, kk;
       if (AK) { mm = e / BK; kk = e % BK; } else { kk = e / BM; mm = e % BM; }
       const int64_t m = m0 + mm, k = k0 + kk;
-      As[kk][mm] = (m < g.M && k < g.K) ? A[m * g.sAm + k * g.sAk] : 0.0;
+      As[kk][mm] = (m < g.M && k < kend) ? A[m * g.sAm + k * g.sAk] : 0.0;
     }
 #pragma unroll
     for (int r = 0; r < (BN * BK) / GT; r++) {
@@ -85,7 +96,7 @@ __global__ void __launch_bounds__(GT) dgemm_kernel(GemmArgs g) {
       int nn, kk;
       if (BN_) { kk = e / BN; nn = e % BN; } else { nn = e / BK; kk = e % BK; }
       const int64_t n = n0 + nn, k = k0 + kk;
-      Bs[kk][nn] = (n < g.N && k < g.K) ? B[k * g.sBk + n * g.sBn] : 0.0;
+      Bs[kk][nn] = (n < g.N && k < kend) ? B[k * g.sBk + n * g.sBn] : 0.0;
     }
     __syncthreads();
 #pragma unroll
@@ -102,7 +113,15 @@ __global__ void __launch_bounds__(GT) dgemm_kernel(GemmArgs g) {
     }
     __syncthreads();
   }
-  const GemmEpilogue ep = g.epi;
+  GemmEpilogue ep = g.epi;
+  double alpha = g.alpha, beta = g.beta;
+  if (g.kchunk > 0) {
+    ep.msplit = 0;
+    ep.s_mhi = g.N;
+    ep.s_n = 1;
+    alpha = 1.0;
+    beta = 0.0;
+  }
 #pragma unroll
   for (int i = 0; i < 4; i++) {
     const int64_t m = m0 + ty + 16 * i;
@@ -113,9 +132,24 @@ __global__ void __launch_bounds__(GT) dgemm_kernel(GemmArgs g) {
       const int64_t n = n0 + tx + 16 * j;
       if (n >= g.N) continue;
       double* cp = C + mo + n * ep.s_n;
-      const double v = g.alpha * acc[i][j];
-      *cp = (g.beta == 0.0) ? v : fma(g.beta, *cp, v);
+      const double v = alpha * acc[i][j];
+      *cp = (beta == 0.0) ? v : fma(beta, *cp, v);
     }
+  }
+}
+
+// C(epi) = alpha * sum_z P[z][m][n] + beta * C(epi), the fixed-order split-K reduction
+__global__ void splitk_reduce_kernel(int64_t M, int64_t N, int nsplit, const double* P, double alpha, double beta,
+                                     double* C, GemmEpilogue ep) {
+  const int64_t MN = M * N;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < MN; x += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int z = 0; z < nsplit; z++) s += P[(int64_t)z * MN + x];
+    const int64_t m = x / N, n = x - m * N;
+    const int64_t mo = ep.msplit ? (m / ep.msplit) * ep.s_mhi + (m % ep.msplit) * ep.s_mlo : m * ep.s_mhi;
+    double* cp = C + mo + n * ep.s_n;
+    const double v = alpha * s;
+    *cp = (beta == 0.0) ? v : fma(beta, *cp, v);
   }
 }
 }  // namespace
@@ -125,9 +159,25 @@ void dgemm_strided(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const 
                    int batch, int64_t bA, int64_t bB, int64_t bC, const GemmPtrs* ptrs) {
   if (M <= 0 || N <= 0 || batch <= 0) return;
   UCC_REQUIRE(batch <= 65535, UCC_BAD_ARGS, "dgemm: batch too large");
-  GemmArgs g{M, N, K, alpha, beta, A, sAm, sAk, bA, B, sBk, sBn, bB, C, bC, epi, ptrs};
+  GemmArgs g{M, N, K, 0, alpha, beta, A, sAm, sAk, bA, B, sBk, sBn, bB, C, bC, epi, ptrs};
   dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM), (unsigned)batch);
   UCC_REQUIRE(grid.y <= 65535, UCC_BAD_ARGS, "dgemm: M too large");
+  // Too few output tiles to fill the GPU and a long K: split K over blockIdx.z into
+  // partial tiles, then reduce them in a fixed order (deterministic).
+  const int64_t tiles = (int64_t)grid.x * grid.y;
+  std::unique_ptr<Scratch> part;
+  int nsplit = 1;
+  if (batch == 1 && !ptrs && tiles < 2 * 152 && K >= 4 * 64) {
+    nsplit = (int)std::min<int64_t>({(2 * 152 + tiles - 1) / tiles, K / 64, 512});
+    const int64_t kchunk = ((K + nsplit - 1) / nsplit + BK - 1) / BK * BK;
+    nsplit = (int)((K + kchunk - 1) / kchunk);
+    if (nsplit > 1) {
+      part = std::make_unique<Scratch>(c, sizeof(double) * M * N * nsplit);
+      g.kchunk = kchunk;
+      g.C = part->d();
+      grid.z = (unsigned)nsplit;
+    }
+  }
   const bool ak = (sAk == 1) || (sAm != 1 && sAk < sAm);
   const bool bn = (sBn == 1) || (sBk != 1 && sBn < sBk);
   if (ak && bn)
@@ -140,6 +190,13 @@ void dgemm_strided(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const 
     dgemm_kernel<false, false><<<grid, GT, 0, c.stream>>>(g);
   count_launch();
   check_launch("dgemm");
+  if (part) {
+    const int64_t MN = M * N;
+    const unsigned blocks = (unsigned)std::min<int64_t>((MN + 255) / 256, 152 * 16);
+    splitk_reduce_kernel<<<blocks, 256, 0, c.stream>>>(M, N, nsplit, part->d(), alpha, beta, C, epi);
+    count_launch();
+    check_launch("dgemm split-K reduce");
+  }
 }
 
 void dgemm(Ctx& c, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,

@@ -23,6 +23,7 @@
 #include <map>
 #include <tuple>
 
+#include "cc.h"
 #include "core.h"
 
 namespace ucc {
@@ -46,6 +47,12 @@ struct Params {
   double* C;
   GemmEpilogue epi;
   int* err;
+  // batched problems of one shape (0 = a single problem): problem p reads A rows from
+  // a_row0[p] and B rows from b_row0[p] of the tensor maps and writes C + c_off[p]
+  int nprob;
+  const int* a_row0;
+  const int* b_row0;
+  const int64_t* c_off;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -164,7 +171,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   fence_after();
   const uint32_t tmem = *tslot;
   const int KB = 3 * p.kblocks;
-  const int ntile = p.mtiles * p.ntiles;
+  const int tiles_per = p.mtiles * p.ntiles;
+  const int ntile = tiles_per * (p.nprob ? p.nprob : 1);
 
   if (warp == 0) {
     if (lane == 0) {
@@ -173,7 +181,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       int64_t issued = 0;
       bool ok = true;
       for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
-        const int mt = tile % p.mtiles, nt = tile / p.mtiles;
+        const int pb = tile / tiles_per, tl = tile - pb * tiles_per;
+        const int mt = tl % p.mtiles, nt = tl / p.mtiles;
+        const int ar = (p.nprob ? p.a_row0[pb] : 0) + mt * BM, br = (p.nprob ? p.b_row0[pb] : 0) + nt * BN;
         for (int kb = 0; kb < KB; kb++) {
           if (!mbar_wait(&empty[stage], phase ^ 1u, p.err)) {
             ok = false;
@@ -181,8 +191,8 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
           const int part = kb / p.kblocks, kk = (kb - part * p.kblocks) * BK;
           mbar_expect_tx(&full[stage], A_BYTES + B_BYTES);
-          tma_load(sA + stage * A_BYTES, part < 2 ? &mAhi : &mAlo, &full[stage], kk, mt * BM);
-          tma_load(sB + stage * B_BYTES, part == 1 ? &mBlo : &mBhi, &full[stage], kk, nt * BN);
+          tma_load(sA + stage * A_BYTES, part < 2 ? &mAhi : &mAlo, &full[stage], kk, ar);
+          tma_load(sB + stage * B_BYTES, part == 1 ? &mBlo : &mBhi, &full[stage], kk, br);
           ++issued;
           if (++stage == STAGES) {
             stage = 0;
@@ -233,7 +243,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     uint32_t aphase = 0;
     const GemmEpilogue ep = p.epi;
     for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
-      const int mt = tile % p.mtiles, nt = tile / p.mtiles;
+      const int pb = tile / tiles_per, tl = tile - pb * tiles_per;
+      const int mt = tl % p.mtiles, nt = tl / p.mtiles;
+      double* Cb = p.C + (p.nprob ? p.c_off[pb] : 0);
       if (!mbar_wait(&tfull[acc], aphase, p.err)) break;
       fence_after();
       const int64_t m = (int64_t)mt * BM + q * 32 + lane;
@@ -247,7 +259,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           for (int j = 0; j < 32; j++) {
             const int64_t n = n0 + j;
             if (n < p.N) {
-              double* cp = p.C + mo + n * ep.s_n;
+              double* cp = Cb + mo + n * ep.s_n;
               const double v = p.alpha * (double)__uint_as_float(r[j]);
               *cp = (p.beta == 0.0) ? v : fma(p.beta, *cp, v);
             }
@@ -298,8 +310,10 @@ struct Split {
 };
 
 using Key = std::tuple<const double*, int64_t, int64_t, int64_t, int64_t, int>;
+struct Triples;
 struct Cache {
   std::map<Key, std::unique_ptr<Split>> ops;
+  std::shared_ptr<Triples> triples;
   int* err = nullptr;
   int sms = 0;
   bool attr_set = false;
@@ -396,10 +410,14 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
   p.C = C;
   p.epi = epi;
   p.err = k.err;
+  p.nprob = 0;
+  p.a_row0 = p.b_row0 = nullptr;
+  p.c_off = nullptr;
   const int tiles = p.mtiles * p.ntiles;
   const int grid = std::min(tiles, k.sms);
   gemm_kernel<<<grid, THREADS, SMEM_BYTES, c.stream>>>(a->mhi, a->mlo, b->mhi, b->mlo, p);
   count_kernel_launch();
+  c.stats.tc_gemm_launches++;
   UCC_CUDA(cudaGetLastError());
   int herr = 0;
   UCC_CUDA(cudaMemcpyAsync(&herr, k.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
@@ -422,7 +440,159 @@ bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const dou
   return true;
 }
 
-bool mixed_triples_prepare(Ctx&) { return false; }
-bool mixed_triples_batch(Ctx&, int, const int*, double*) { return false; }
+// ------------------------------------------------------------------------------------
+// (T) on the tensor cores: A_x^T = [<xe|ab> ; -t2[x][m][a][b]] stacked over x as
+// [no*nv^2][K'] and B_yz^T = [t2[y][z][c][e] ; <zy|mc>] stacked over (y,z) as [no^2*nv][K']
+// (K' = nv + no padded to 64), split once per (T) call; each of the six terms of a tuple
+// batch is one batched launch whose problems are the tuples of the batch.
+// ------------------------------------------------------------------------------------
+namespace tc {
+// dst[(row0 + r) * ld + col0 + k] (hi/lo) = scale * src[r*sr + k*sk], r < rows, k < cols;
+// 32x32 tiles through shared memory so that the destination rows are written coalesced
+__global__ void split_into_kernel(int64_t rows, int64_t cols, const double* src, int64_t sr, int64_t sk, double scale,
+                                  __nv_bfloat16* hi, __nv_bfloat16* lo, int64_t ld, int64_t row0, int64_t col0) {
+  __shared__ double t[32][33];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
+  for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+    const int64_t r = r0 + threadIdx.x, k = k0 + yy;
+    t[yy][threadIdx.x] = (r < rows && k < cols) ? scale * src[r * sr + k * sk] : 0.0;
+  }
+  __syncthreads();
+  for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+    const int64_t r = r0 + yy, k = k0 + threadIdx.x;
+    if (r < rows && k < cols) {
+      const double v = t[threadIdx.x][yy];
+      const __nv_bfloat16 h = __double2bfloat16(v);
+      const int64_t o = (row0 + r) * ld + col0 + k;
+      hi[o] = h;
+      lo[o] = __double2bfloat16(v - (double)__bfloat162float(h));
+    }
+  }
+}
+
+struct Triples {
+  Split A, B;
+  int* d_arow = nullptr;
+  int* d_brow = nullptr;
+  int64_t* d_coff = nullptr;
+  ~Triples() {
+    if (d_arow) cudaFree(d_arow);
+    if (d_brow) cudaFree(d_brow);
+    if (d_coff) cudaFree(d_coff);
+  }
+};
+
+static void split_into(Ctx& c, int64_t rows, int64_t cols, const double* src, int64_t sr, int64_t sk, double scale,
+                       Split& dst, int64_t row0, int64_t col0) {
+  dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+  UCC_REQUIRE(grid.y <= 65535, UCC_BAD_ARGS, "split_into: too many rows");
+  split_into_kernel<<<grid, dim3(32, 8), 0, c.stream>>>(rows, cols, src, sr, sk, scale, dst.hi, dst.lo, dst.kp, row0,
+                                                        col0);
+  count_kernel_launch();
+  UCC_CUDA(cudaGetLastError());
+}
+
+static void alloc_split(Split& s, int64_t rows, int64_t kp, cudaStream_t st) {
+  s.rows = rows;
+  s.kp = kp;
+  UCC_CUDA(cudaMalloc(&s.hi, sizeof(__nv_bfloat16) * rows * kp));
+  UCC_CUDA(cudaMalloc(&s.lo, sizeof(__nv_bfloat16) * rows * kp));
+  UCC_CUDA(cudaMemsetAsync(s.hi, 0, sizeof(__nv_bfloat16) * rows * kp, st));
+  UCC_CUDA(cudaMemsetAsync(s.lo, 0, sizeof(__nv_bfloat16) * rows * kp, st));
+}
+}  // namespace tc
+
+bool mixed_triples_prepare(Ctx& c, int max_batch) {
+  using namespace tc;
+  const int64_t no = c.no, nv = c.nv, nv2 = nv * nv, kp = (nv + no + BK - 1) / BK * BK;
+  if (nv < 64) return false;  // small virtual spaces stay on the FP64 path
+  Cache& k = cache(c);
+  auto T = std::make_shared<Triples>();
+  alloc_split(T->A, no * nv2, kp, c.stream);
+  alloc_split(T->B, no * no * nv, kp, c.stream);
+  const double* t2 = c.get("T").p + no * nv;
+  const double* Vovvv = c.get("Vovvv").p;
+  const double* Vooov = c.get("Vooov").p;
+  for (int64_t x = 0; x < no; x++) {
+    split_into(c, nv2, nv, Vovvv + x * nv * nv2, 1, nv2, 1.0, T->A, x * nv2, 0);   // <xe|ab>
+    split_into(c, nv2, no, t2 + x * no * nv2, 1, nv2, -1.0, T->A, x * nv2, nv);   // -t2[x][m][a][b]
+  }
+  split_into(c, no * no * nv, nv, t2, nv, 1, 1.0, T->B, 0, 0);  // t2[y][z][c][e]
+  for (int64_t y = 0; y < no; y++)
+    for (int64_t z = 0; z < no; z++)  // <zy|mc>
+      split_into(c, nv, no, Vooov + (z * no + y) * no * nv, 1, nv, 1.0, T->B, (y * no + z) * nv, nv);
+  make_map(&T->A.mhi, T->A.hi, T->A.rows, kp, BM);
+  make_map(&T->A.mlo, T->A.lo, T->A.rows, kp, BM);
+  make_map(&T->B.mhi, T->B.hi, T->B.rows, kp, BN);
+  make_map(&T->B.mlo, T->B.lo, T->B.rows, kp, BN);
+  UCC_CUDA(cudaMalloc(&T->d_arow, sizeof(int) * max_batch));
+  UCC_CUDA(cudaMalloc(&T->d_brow, sizeof(int) * max_batch));
+  UCC_CUDA(cudaMalloc(&T->d_coff, sizeof(int64_t) * max_batch));
+  k.triples = T;
+  if (!k.attr_set) {
+    UCC_CUDA(cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+    k.attr_set = true;
+  }
+  return true;
+}
+
+void mixed_triples_release(Ctx& c) {
+  UCC_CUDA(cudaStreamSynchronize(c.stream));
+  tc::cache(c).triples.reset();
+}
+
+bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, double* W3) {
+  using namespace tc;
+  Cache& k = cache(c);
+  Triples& T = *k.triples;
+  const int64_t no = c.no, nv = c.nv, nv2 = nv * nv, nv3 = nv2 * nv;
+  TriplesTerm terms[6];
+  triples_terms(nv, terms);
+  std::vector<int> arow(nb), brow(nb);
+  std::vector<int64_t> coff(nb);
+  for (int b = 0; b < nb; b++) coff[b] = b * nv3;
+  UCC_CUDA(cudaMemcpyAsync(T.d_coff, coff.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice, c.stream));
+  for (int q = 0; q < 6; q++) {
+    for (int b = 0; b < nb; b++) {
+      const int* ijk = tuples + 3 * b;
+      arow[b] = (int)(ijk[terms[q].x] * nv2);
+      brow[b] = (int)((ijk[terms[q].y] * no + ijk[terms[q].z]) * nv);
+    }
+    UCC_CUDA(cudaMemcpyAsync(T.d_arow, arow.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c.stream));
+    UCC_CUDA(cudaMemcpyAsync(T.d_brow, brow.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c.stream));
+    Params p;
+    p.M = (int)nv2;
+    p.N = (int)nv;
+    p.kblocks = (int)(T.A.kp / BK);
+    p.mtiles = (int)((nv2 + BM - 1) / BM);
+    p.ntiles = (int)((nv + BN - 1) / BN);
+    p.alpha = 1.0;
+    p.beta = q == 0 ? 0.0 : 1.0;
+    p.C = W3;
+    p.epi.msplit = nv;
+    p.epi.s_mhi = terms[q].su;
+    p.epi.s_mlo = terms[q].sv;
+    p.epi.s_n = terms[q].sw;
+    p.err = k.err;
+    p.nprob = nb;
+    p.a_row0 = T.d_arow;
+    p.b_row0 = T.d_brow;
+    p.c_off = T.d_coff;
+    const int tiles = p.mtiles * p.ntiles * nb;
+    gemm_kernel<<<std::min(tiles, k.sms), THREADS, SMEM_BYTES, c.stream>>>(T.A.mhi, T.A.mlo, T.B.mhi, T.B.mlo, p);
+    count_kernel_launch();
+    c.stats.tc_gemm_launches++;
+    UCC_CUDA(cudaGetLastError());
+    // the row tables are rewritten for the next term: keep the copies ordered after use
+    UCC_CUDA(cudaStreamSynchronize(c.stream));
+  }
+  int herr = 0;
+  UCC_CUDA(cudaMemcpy(&herr, k.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) {
+    cudaMemset(k.err, 0, sizeof(int));
+    throw Error(UCC_DEVICE_TIMEOUT, "tensor-core (T) GEMM: a pipeline wait timed out");
+  }
+  return true;
+}
 
 }  // namespace ucc

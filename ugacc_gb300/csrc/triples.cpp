@@ -21,7 +21,8 @@ double flops_triples(double no, double nv) { return 2.0 * no * (no + 1) * (no + 
 
 // mixed-precision tuple GEMMs (tc_gemm.cu); false if not available for this shape
 bool mixed_triples_batch(Ctx& c, int nbatch, const int* h_tuples, double* W3);
-bool mixed_triples_prepare(Ctx& c);
+bool mixed_triples_prepare(Ctx& c, int max_batch);
+void mixed_triples_release(Ctx& c);
 
 double run_triples(Ctx& c) {
   UCC_REQUIRE(c.have_ccsd, UCC_BAD_STATE, "(T) needs converged CCSD amplitudes");
@@ -66,15 +67,9 @@ double run_triples(Ctx& c) {
   Scratch W3(c, sizeof(double) * nv3 * batch);
   Scratch partial(c, sizeof(double) * (size_t)ntup * nv);
 
-  const bool mixed = c.opt.precision == UCC_MIXED && !c.force_fp64 && mixed_triples_prepare(c);
-  // term table: x, y, z selectors into (i,j,k) and the W3 strides of (u, v, w)
-  struct Term {
-    int x, y, z;
-    int64_t su, sv, sw;
-  };
-  const Term terms[6] = {{0, 2, 1, nv2, nv, 1}, {0, 1, 2, nv2, 1, nv}, {2, 1, 0, 1, nv2, nv},
-                         {2, 0, 1, 1, nv, nv2}, {1, 0, 2, nv, 1, nv2}, {1, 2, 0, nv, nv2, 1}};
-  std::vector<GemmPtrs> hp((size_t)batch);
+  const bool mixed = c.opt.precision == UCC_MIXED && !c.force_fp64 && mixed_triples_prepare(c, batch);
+  TriplesTerm terms[6];
+  triples_terms(nv, terms);
   Scratch dptr(c, sizeof(GemmPtrs) * batch * 6);
   GemmPtrs* dp = static_cast<GemmPtrs*>(dptr.p);
   for (int t0 = 0; t0 < ntup; t0 += batch) {
@@ -86,7 +81,7 @@ double run_triples(Ctx& c) {
       for (int q = 0; q < 6; q++)
         for (int b = 0; b < nb; b++) {
           const int* ijk = &tuples[3 * (t0 + b)];
-          const Term& tm = terms[q];
+          const TriplesTerm& tm = terms[q];
           all[(size_t)q * nb + b] = {Acat.p + (int64_t)ijk[tm.x] * Kp * nv2,
                                      Bcat.p + ((int64_t)ijk[tm.y] * no + ijk[tm.z]) * Kp * nv,
                                      W3.d() + (int64_t)b * nv3};
@@ -114,6 +109,7 @@ double run_triples(Ctx& c) {
   UCC_CUDA(cudaStreamSynchronize(c.stream));
   c.drop("T3_A");
   c.drop("T3_B");
+  if (mixed) mixed_triples_release(c);
   UCC_REQUIRE(std::isfinite(e), UCC_NAN_DETECTED, "(T) energy is not finite");
   return e;
 }

@@ -1,0 +1,61 @@
+"""Run a bounded slice of the solver for profiling (ncu launch lists, kernel captures).
+
+    python -m ugacc_gb300.profile_step --no 16 --nv 160 --seed 1 --iters 2 [--triples]
+                                       [--precision fp64|mixed] [--gemm M N K]
+
+--iters n runs n CCSD iterations from the MP2 guess (MAXITER=n; the not-converged
+status is expected and ignored); --triples then adds (T) on converged amplitudes;
+--gemm runs one tensor-core GEMM of that shape through ucc_gemm instead.
+Prints the library's per-stage CUDA-event timings.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+
+import numpy as np
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--no", type=int, default=16)
+    ap.add_argument("--nv", type=int, default=160)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--iters", type=int, default=1)
+    ap.add_argument("--triples", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--gemm", type=int, nargs=3, metavar=("M", "N", "K"))
+    a = ap.parse_args(argv)
+
+    import ugacc_gb300 as U
+    from ugacc_gb300.generator import make_hamiltonian
+
+    if a.gemm:
+        M, N, K = a.gemm
+        rng = np.random.default_rng(0)
+        ctx = U.Context()
+        A, B = rng.standard_normal((M, K)), rng.standard_normal((K, N))
+        ctx.gemm(A, B, precision=U.MIXED if a.precision == "mixed" else U.FP64)
+        print(json.dumps({"gemm": [M, N, K], "precision": a.precision}))
+        return 0
+    h = make_hamiltonian(a.no, a.nv, a.seed)
+    H = U.Hamiltonian.from_synthetic(h)
+    prec = a.precision.upper()
+    if a.iters > 0:
+        cc = U.CCWfn(H, {"MAXITER": a.iters, "R_CONVERGENCE": 1e-10, "PRECISION": prec})
+        try:
+            cc.compute_energy()
+        except U.ConvergenceError:
+            pass
+    if a.triples:
+        cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": prec})
+        cc.compute_energy()
+        H.ctx.reset_stats()
+        cc.triples()
+    print(json.dumps(H.ctx.stats()))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
