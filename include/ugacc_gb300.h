@@ -130,6 +130,7 @@ typedef struct ucc_stats {
   int64_t ladder_launches;
   int fp64_iterations;       /* CCSD iterations whose residual was built in FP64 */
   int64_t tc_gemm_launches;  /* tensor-core (BF16 split) GEMM launches */
+  int mixed_iterations;      /* CCSD iterations with split-product residuals */
 } ucc_stats;
 ucc_status ucc_get_stats(ucc_ctx* ctx, ucc_stats* out);
 ucc_status ucc_reset_stats(ucc_ctx* ctx);

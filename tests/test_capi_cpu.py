@@ -48,3 +48,17 @@ def test_no_cpu_fallback_when_library_missing(tmp_path):
             U.load_library(str(tmp_path / "missing.so"))
         finally:
             U._lib = None
+
+
+def test_cpp_driver_usage_and_bad_input(tmp_path):
+    import subprocess
+
+    from ugacc_gb300.build import DRIVER, build
+
+    build()
+    r = subprocess.run([DRIVER], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(b"NOPE" + b"\0" * 64)
+    r = subprocess.run([DRIVER, str(bad)], capture_output=True, text=True)
+    assert r.returncode == 1 and "not a synthetic Hamiltonian file" in r.stderr

@@ -51,3 +51,18 @@ def test_mixed_unrefined_within_one_microhartree():
     emx = mx.compute_energy()
     assert H.ctx.stats()["fp64_iterations"] == 0
     assert abs(emx - e64) < 1e-6
+
+
+def test_mixed_triples_matches_fp64():
+    h = make_hamiltonian(6, 80, 13)
+    H = U.Hamiltonian.from_synthetic(h)
+    cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10})
+    cc.compute_energy()
+    e64 = cc.triples()
+    mx = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": "MIXED"})
+    mx.compute_energy()
+    H.ctx.reset_stats()
+    emx = mx.triples()
+    assert H.ctx.stats()["tc_gemm_launches"] == 6  # one batched launch per W3 term
+    # split products carry ~2^-16 relative error into W3; E(T) is a weighted sum of W3*V3
+    assert abs(emx - e64) < 1e-8 + 1e-4 * abs(e64)

@@ -50,7 +50,7 @@ class Stats(ctypes.Structure):
                 ("kernel_launches", ctypes.c_int64), ("ladder_ms", ctypes.c_double),
                 ("ladder_bytes", ctypes.c_double), ("ladder_flops", ctypes.c_double),
                 ("ladder_launches", ctypes.c_int64), ("fp64_iterations", ctypes.c_int),
-                ("tc_gemm_launches", ctypes.c_int64)]
+                ("tc_gemm_launches", ctypes.c_int64), ("mixed_iterations", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -45,6 +45,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
     headers = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith(".h")]
     headers.append(os.path.join(os.path.dirname(HERE), "include", "ugacc_gb300.h"))
+    headers.append(os.path.join(os.path.dirname(HERE), "include", "ugacc_gb300.hpp"))
+    headers.append(os.path.join(HERE, "driver", "ugacc_driver.cpp"))
     srcs = [os.path.join(SRC, f) for f in sources()]
     key = _digest(sorted(headers) + srcs)
     stamp = os.path.join(OBJ, "stamp")
@@ -70,9 +72,25 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver()
     with open(stamp, "w") as f:
         f.write(key)
     return LIB
+
+
+DRIVER = os.path.join(OUT, "ugacc_driver")
+
+
+def build_driver() -> str:
+    """The C++ command-line driver (driver/ugacc_driver.cpp) linked against the library."""
+    src = os.path.join(HERE, "driver", "ugacc_driver.cpp")
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(os.path.dirname(HERE), "include"), src, "-L", OUT,
+           "-lugacc_gb300", "-Wl,-rpath,$ORIGIN", "-o", DRIVER]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+    return DRIVER
 
 
 if __name__ == "__main__":

@@ -30,6 +30,7 @@ class Diis {
   void add(const double* vnew, const double* vold);
   int size() const { return count_; }
   void extrapolate(double* out);
+  void reset();
 
  private:
   Ctx& c_;

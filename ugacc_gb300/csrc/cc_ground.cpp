@@ -226,6 +226,12 @@ std::vector<double> diis_coefficients(const std::vector<double>& Bin, int n) {
   return c;
 }
 
+void Diis::reset() {
+  count_ = 0;
+  nadded_ = 0;
+  std::fill(B_.begin(), B_.end(), 0.0);
+}
+
 void Diis::extrapolate(double* out) {
   const int n = count_;
   std::vector<double> Bn((size_t)n * n);
@@ -462,10 +468,17 @@ CCSDResult run_ccsd(Ctx& c) {
     if (fp64_phase) fp64_iters++;
     const bool refined = !mixed || c.opt.refine_sweeps == 0 || (fp64_phase && fp64_iters >= c.opt.refine_sweeps);
     if (rms < c.opt.r_convergence && refined) break;
+    bool switched = false;
     if (mixed && !fp64_phase && c.opt.refine_sweeps > 0 &&
-        (rms < std::max(c.opt.r_convergence, kMixedFloor) || (iter > 2 && rms > 0.5 * rms_prev)))
+        (rms < std::max(c.opt.r_convergence, kMixedFloor) || (iter > 2 && rms > 0.5 * rms_prev))) {
       fp64_phase = true;
+      switched = true;
+      c.stats.mixed_iterations = iter;
+    }
     rms_prev = rms;
+    // error vectors of split-product residuals do not extrapolate FP64 ones: the refinement
+    // sweeps start a fresh DIIS subspace
+    if (switched) diis.reset();
     if (c.opt.diis) {
       diis.add(tn, to);
       if (diis.size() > 2) diis.extrapolate(tn);

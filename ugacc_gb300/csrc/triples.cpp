@@ -31,23 +31,6 @@ double run_triples(Ctx& c) {
   double* T = c.get("T").p;
   Tensor t1 = amp1(c, T), t2 = amp2(c, T);
 
-  // concatenated operands
-  Tensor Acat = c.alloc("T3_A", {no, Kp, nv2}, false);
-  {
-    Tensor Ae = narrow(Acat, 1, 0, nv), Am = narrow(Acat, 1, nv, no);
-    Tensor Vovvv = c.get("Vovvv");
-    Tensor src = make_view(Vovvv.p, {no, nv, nv2});
-    permute_add(c, src, 1.0, 0.0, Ae);
-    Tensor t2v = make_view(t2.p, {no, no, nv2});
-    permute_add(c, t2v, -1.0, 0.0, Am);
-  }
-  Tensor Bcat = c.alloc("T3_B", {no, no, Kp, nv}, false);
-  {
-    Tensor Be = narrow(Bcat, 2, 0, nv), Bm = narrow(Bcat, 2, nv, no);
-    permute_add(c, view(t2, "yzce->yzec"), 1.0, 0.0, Be);
-    permute_add(c, view(c.get("Vooov"), "zymc->yzmc"), 1.0, 0.0, Bm);
-  }
-
   std::vector<int> tuples;
   for (int i = 0; i < no; i++)
     for (int j = 0; j <= i; j++)
@@ -68,6 +51,18 @@ double run_triples(Ctx& c) {
   Scratch partial(c, sizeof(double) * (size_t)ntup * nv);
 
   const bool mixed = c.opt.precision == UCC_MIXED && !c.force_fp64 && mixed_triples_prepare(c, batch);
+  // FP64 path: concatenated operands A_x (no x (nv+no) x nv^2) and B_yz (no^2 x (nv+no) x nv)
+  Tensor Acat, Bcat;
+  if (!mixed) {
+    Acat = c.alloc("T3_A", {no, Kp, nv2}, false);
+    Tensor Ae = narrow(Acat, 1, 0, nv), Am = narrow(Acat, 1, nv, no);
+    permute_add(c, make_view(c.get("Vovvv").p, {no, nv, nv2}), 1.0, 0.0, Ae);
+    permute_add(c, make_view(t2.p, {no, no, nv2}), -1.0, 0.0, Am);
+    Bcat = c.alloc("T3_B", {no, no, Kp, nv}, false);
+    Tensor Be = narrow(Bcat, 2, 0, nv), Bm = narrow(Bcat, 2, nv, no);
+    permute_add(c, view(t2, "yzce->yzec"), 1.0, 0.0, Be);
+    permute_add(c, view(c.get("Vooov"), "zymc->yzmc"), 1.0, 0.0, Bm);
+  }
   TriplesTerm terms[6];
   triples_terms(nv, terms);
   Scratch dptr(c, sizeof(GemmPtrs) * batch * 6);
@@ -107,9 +102,12 @@ double run_triples(Ctx& c) {
   double e = 0.0;
   UCC_CUDA(cudaMemcpyAsync(&e, et.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
   UCC_CUDA(cudaStreamSynchronize(c.stream));
-  c.drop("T3_A");
-  c.drop("T3_B");
-  if (mixed) mixed_triples_release(c);
+  if (mixed) {
+    mixed_triples_release(c);
+  } else {
+    c.drop("T3_A");
+    c.drop("T3_B");
+  }
   UCC_REQUIRE(std::isfinite(e), UCC_NAN_DETECTED, "(T) energy is not finite");
   return e;
 }

@@ -1,0 +1,121 @@
+// Command-line driver: the reference plugin's pipeline (ugacc.cc:108-241) on the
+// C++ class surface of the GB300 library, for a Hamiltonian stored in the synthetic
+// input format of ugacc_gb300/generator.py (three-index factors are used).
+//
+// usage: ugacc_driver <input.bin> [WFN=CCSD|CCSD_T] [DERTYPE=NONE|FIRST|SECOND]
+//        [MAXITER=100] [R_CONVERGENCE=1e-7] [DIIS=1] [MY_OMEGA=0] [MYHAND=RIGHT|LEFT]
+//        [PRECISION=FP64|MIXED] [REFINE_SWEEPS=2] [PRINT=0]
+// Prints one JSON object with the energies (and polarizabilities for DERTYPE=SECOND).
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/ugacc_gb300.hpp"
+
+using namespace ugacc_gb300;
+
+namespace {
+struct Input {
+  int no = 0, nv = 0, naux = 0, npert = 0;
+  std::vector<double> eps, B;
+  std::vector<std::vector<double>> perts;
+};
+
+Input read_input(const char* path) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) throw std::runtime_error(std::string("cannot open ") + path);
+  auto rd = [&](void* p, size_t n) {
+    if (n && std::fread(p, 1, n, f) != n) throw std::runtime_error("short read");
+  };
+  char magic[4];
+  rd(magic, 4);
+  if (std::string(magic, 4) != "UGAH") throw std::runtime_error("not a synthetic Hamiltonian file");
+  int32_t h[6];
+  rd(h, sizeof h);
+  Input in;
+  in.no = h[1];
+  in.nv = h[2];
+  in.naux = h[3];
+  in.npert = h[4];
+  const size_t n = (size_t)in.no + in.nv;
+  in.eps.resize(n);
+  rd(in.eps.data(), n * 8);
+  in.B.resize((size_t)in.naux * n * n);
+  rd(in.B.data(), in.B.size() * 8);
+  in.perts.assign(in.npert, std::vector<double>(n * n));
+  for (auto& p : in.perts) rd(p.data(), p.size() * 8);
+  std::fclose(f);
+  return in;
+}
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 2) {
+    std::fprintf(stderr, "usage: %s input.bin [KEY=VALUE ...]\n", argv[0]);
+    return 2;
+  }
+  std::map<std::string, std::string> kv;
+  for (int k = 2; k < argc; k++) {
+    std::string a = argv[k];
+    auto eq = a.find('=');
+    if (eq != std::string::npos) kv[a.substr(0, eq)] = a.substr(eq + 1);
+  }
+  auto get = [&](const char* k, const char* d) { return kv.count(k) ? kv[k] : std::string(d); };
+  try {
+    Input in = read_input(argv[1]);
+    const int n = in.no + in.nv;
+    std::vector<double> fock((size_t)n * n, 0.0);
+    for (int p = 0; p < n; p++) fock[(size_t)p * n + p] = in.eps[p];
+    Options o;
+    o.wfn = get("WFN", "CCSD");
+    o.dertype = get("DERTYPE", "NONE");
+    o.myhand = get("MYHAND", "RIGHT");
+    o.precision = get("PRECISION", "FP64");
+    o.maxiter = std::atoi(get("MAXITER", "100").c_str());
+    o.refine_sweeps = std::atoi(get("REFINE_SWEEPS", "2").c_str());
+    o.print = std::atoi(get("PRINT", "0").c_str());
+    o.r_convergence = std::atof(get("R_CONVERGENCE", "1e-7").c_str());
+    o.my_omega = std::atof(get("MY_OMEGA", "0").c_str());
+    o.diis = get("DIIS", "1") == "1";
+
+    auto H = std::make_shared<Hamiltonian>(in.no, in.nv, in.naux, fock.data(), in.B.data());
+    auto cc = std::make_shared<CCWfn>(H, o);
+    const double ecc = cc->compute_energy();
+    std::printf("{\"e_ccsd\": %.17g, \"e_t\": %.17g, \"e_cc\": %.17g", cc->eccsd(), cc->et(), ecc);
+    if (o.dertype != "NONE") {
+      auto hbar = std::make_shared<HBAR>(H, cc);
+      auto lam = std::make_shared<CCLambda>(cc, hbar);
+      lam->compute_lambda();
+      CCDensity dens(cc, lam);
+      const double e1 = dens.onepdm(), e2 = dens.twopdm();
+      std::printf(", \"pseudoenergy\": %.17g, \"e_onepdm\": %.17g, \"e_twopdm\": %.17g", lam->pseudoenergy(), e1, e2);
+      if (o.dertype == "SECOND" && in.npert >= 3) {
+        const char* cart = "XYZ";
+        std::vector<std::shared_ptr<CCPert>> mu(3);
+        for (int x = 0; x < 3; x++) {
+          mu[x] = std::make_shared<CCPert>(in.perts[x].data(), o.my_omega, cc, hbar, lam);
+          mu[x]->solve(right);
+          if (o.myhand != "RIGHT") mu[x]->solve(left);
+        }
+        for (int p = 0; p < 3; p++)
+          for (int q = 0; q <= p; q++) {
+            CCResp r(mu[p], mu[q]);
+            const double a = p == q ? r.linresp(mu[p], mu[q])
+                                    : 0.5 * r.linresp(mu[p], mu[q]) + 0.5 * r.linresp(mu[q], mu[p]);
+            std::printf(", \"alpha_%c%c\": %.17g", cart[p], cart[q], a);
+          }
+      }
+    }
+    std::printf("}\n");
+  } catch (const ConvergenceError& e) {
+    std::fprintf(stderr, "ugacc_driver: %s\n", e.what());
+    return 3;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "ugacc_driver: %s\n", e.what());
+    return 1;
+  }
+  return 0;
+}

@@ -3,7 +3,7 @@
     python -m ugacc_gb300.profile_step --no 16 --nv 160 --seed 1 --iters 2 [--triples]
                                        [--precision fp64|mixed] [--gemm M N K]
 
---iters n runs n CCSD iterations from the MP2 guess (MAXITER=n; the not-converged
+--print shows the iteration tables; --iters n runs n CCSD iterations from the MP2 guess (MAXITER=n; the not-converged
 status is expected and ignored); --triples then adds (T) on converged amplitudes;
 --gemm runs one tensor-core GEMM of that shape through ucc_gemm instead.
 Prints the library's per-stage CUDA-event timings.
@@ -26,6 +26,7 @@ def main(argv=None):
     ap.add_argument("--triples", action="store_true")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--gemm", type=int, nargs=3, metavar=("M", "N", "K"))
+    ap.add_argument("--print", action="store_true", help="print the iteration tables")
     a = ap.parse_args(argv)
 
     import ugacc_gb300 as U
@@ -43,13 +44,13 @@ def main(argv=None):
     H = U.Hamiltonian.from_synthetic(h)
     prec = a.precision.upper()
     if a.iters > 0:
-        cc = U.CCWfn(H, {"MAXITER": a.iters, "R_CONVERGENCE": 1e-10, "PRECISION": prec})
+        cc = U.CCWfn(H, {"MAXITER": a.iters, "R_CONVERGENCE": 1e-10, "PRECISION": prec, "PRINT": int(a.print)})
         try:
             cc.compute_energy()
         except U.ConvergenceError:
             pass
     if a.triples:
-        cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": prec})
+        cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": prec, "PRINT": int(a.print)})
         cc.compute_energy()
         H.ctx.reset_stats()
         cc.triples()
