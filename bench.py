@@ -2,14 +2,17 @@
 """Benchmark: CCSD(T) on the no=16 / nv=160 synthetic RHF Hamiltonian (seed 1).
 
 One step = one full CCSD(T) solve from the MP2 guess to ||R|| < 1e-10 followed by the
-(T) correction, on Hamiltonian blocks already resident in HBM.  value = algorithmic
+(T) correction, on Hamiltonian blocks already resident in HBM.  The default arm is the
+mixed form (BF16 hi+lo split tensor-core contractions, FP64-accurate refinement sweeps,
+tensor-core (T)); the plain FP64 form of the same step is timed alongside and the energy
+differences between the two are reported.  value = algorithmic
 TFLOP/s of the whole job (CCSD iterations x 2(no^2 nv^4 + 2 no^4 nv^2 + 10 no^3 nv^3 +
 8 no^2 nv^3) + (T) 2 no(no+1)(no+2) nv^3 (nv+no)), device time from CUDA events on the
 library's stream.  e2e repeats the step through the public API from pinned host
 buffers: Hamiltonian upload (DF factors) + block build + CCSD(T) + energies back.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--precision fp64|mixed]
+                    [--precision mixed|fp64] [--no-fp64-reference] [--no-cpu-baseline]
 Multi-GPU: replicas only (each rank solves its own copy; weak scaling).
 """
 from __future__ import annotations
@@ -20,7 +23,6 @@ import os
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -88,6 +90,18 @@ class ClockSampler:
             return None
         sm.sort()
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# DRAM traffic of the tensor-core GEMM per algorithmic FLOP is not measured live; set from
+# the committed ncu capture (profiles/) when available
+TC_TRAFFIC = None
+
+
+def measured_peak(key):
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))[key])
+    except Exception:
+        return None
 
 
 def fp64_gemm_peak_tflops():
@@ -158,8 +172,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-reference", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -200,8 +215,20 @@ def main():
                                          "no=16/nv=160 from the MP2 guess, %.1f s" % t[0]}
     fp64_peak = fp64_gemm_peak_tflops()
 
-    opts = {"R_CONVERGENCE": 1e-10, "MAXITER": 100, "WFN": "CCSD_T", "PRECISION": args.precision.upper()}
     H = U.Hamiltonian.from_synthetic(h, device=local)
+    # plain FP64 form of the same workload (the comparison the metric is quoted against)
+    fp64 = None
+    if args.precision == "mixed" and not args.no_fp64_reference:
+        c64 = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "MAXITER": 100, "WFN": "CCSD_T", "PRECISION": "FP64"})
+        c64.compute_energy()
+        H.ctx.reset_stats()
+        c64.compute_energy()
+        s64 = H.ctx.stats()
+        fp64 = {"ms_per_step": s64["ccsd_ms"] + s64["triples_ms"], "ccsd_ms": s64["ccsd_ms"],
+                "triples_ms": s64["triples_ms"], "ccsd_iterations": s64["ccsd_iterations"],
+                "e_ccsd": c64.eccsd, "e_t": c64.et}
+
+    opts = {"R_CONVERGENCE": 1e-10, "MAXITER": 100, "WFN": "CCSD_T", "PRECISION": args.precision.upper()}
     cc = U.CCWfn(H, opts)
     for _ in range(args.warmup):
         cc.compute_energy()
@@ -239,30 +266,51 @@ def main():
     e2e_ms = allmax(1e3 * (time.perf_counter() - t1) / e2e_steps)
     e2e_value = world * flops_step / (e2e_ms * 1e-3) / 1e12
 
+    roof = None
     ladder = None
     if st["ladder_launches"]:
         ach = st["ladder_flops"] / (st["ladder_ms"] * 1e-3) / 1e12
-        ladder = {"bound": "tensor", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
-                  "frac": (ach / fp64_peak) if fp64_peak else None, "traffic": None,
-                  "kernel": "particle ladder GEMM (ijef,abef->ijab), FP64",
-                  "peak_source": "measured cuBLAS DGEMM 8192^3 on this GPU (FP64 has no entry in the measured peaks)",
-                  "algorithmic_flops_per_launch": st["ladder_flops"] / st["ladder_launches"],
-                  "ms_per_launch": st["ladder_ms"] / st["ladder_launches"]}
+        ladder = {"achieved": ach, "unit": "TFLOP/s", "peak_fp64_dgemm": fp64_peak,
+                  "ms_per_launch": st["ladder_ms"] / st["ladder_launches"], "launches": st["ladder_launches"]}
+    bf16 = measured_peak("bf16_tflops")
+    if args.precision == "mixed" and st["tc_gemm_launches"]:
+        ach = st["tc_gemm_flops"] / (st["tc_gemm_ms"] * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+                "frac": (ach / bf16) if bf16 else None, "traffic": TC_TRAFFIC,
+                "kernel": "tcgen05 BF16 hi+lo split GEMM (ucc::tc::gemm_kernel), all launches of the step",
+                "flops": "algorithmic 2*M*N*K; the tensor pipe executes 3x that (hi.hi + hi.lo + lo.hi)",
+                "tensor_work_frac": (3 * ach / bf16) if bf16 else None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
+                "share_of_step": st["tc_gemm_ms"] / (ms_dev * args.steps),
+                "launches": st["tc_gemm_launches"], "ms_per_launch": st["tc_gemm_ms"] / st["tc_gemm_launches"]}
+    elif ladder:
+        roof = {"bound": "tensor", "achieved": ladder["achieved"], "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": (ladder["achieved"] / fp64_peak) if fp64_peak else None, "traffic": None,
+                "kernel": "particle ladder GEMM (ijef,abef->ijab), FP64 DFMA",
+                "peak_source": "measured cuBLAS DGEMM 8192^3 on this GPU (FP64 has no entry in the measured peaks)",
+                "ms_per_launch": ladder["ms_per_launch"]}
     if rank == 0:
+        cfg = {"workload": WORKLOAD, "no": NO, "nv": NV, "naux": h.naux, "seed": SEED,
+               "precision": args.precision, "ccsd_iterations": iters,
+               "mixed_iterations": st["mixed_iterations"] if args.precision == "mixed" else 0,
+               "r_convergence": 1e-10, "e_ccsd": e_ref[0], "e_t": e_ref[1], "wall_s_per_step": wall / args.steps,
+               "ccsd_ms_per_step": st["ccsd_ms"] / args.steps, "triples_ms_per_step": st["triples_ms"] / args.steps,
+               "l2": "inputs larger than L2 (vvvv block 5.2 GB)", "parallelism": f"replicas x{world}"}
+        if fp64:
+            cfg["fp64_gpu"] = fp64
+            cfg["speedup_vs_fp64_gpu"] = fp64["ms_per_step"] / ms_dev
+            cfg["abs_dE_ccsd_vs_fp64"] = abs(e_ref[0] - fp64["e_ccsd"])
+            cfg["abs_dE_t_vs_fp64"] = abs(e_ref[1] - fp64["e_t"])
+        if ladder:
+            cfg["ladder"] = ladder
         line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "bf16x3-split/f32-acc+f64",
-                "data": "synthetic",
-                "config": {"workload": WORKLOAD, "no": NO, "nv": NV, "naux": h.naux, "seed": SEED,
-                           "precision": args.precision, "ccsd_iterations": iters, "r_convergence": 1e-10,
-                           "e_ccsd": e_ref[0], "e_t": e_ref[1], "wall_s_per_step": wall / args.steps,
-                           "ccsd_ms_per_step": st["ccsd_ms"] / args.steps,
-                           "triples_ms_per_step": st["triples_ms"] / args.steps,
-                           "l2": "inputs larger than L2 (vvvv block 5.2 GB)", "parallelism": f"replicas x{world}"},
+                "data": "synthetic", "config": cfg,
                 "e2e": {"value": e2e_value, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
                         "h2d_bytes_per_step": int(Bp.numel() * 8 + Fp.numel() * 8), "d2h_bytes_per_step": 16},
                 "gpu_launches": int(st["kernel_launches"]),
-                "roofline": ladder, "cpu_baseline": cpu, "clocks": clk}
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -52,6 +52,7 @@ typedef struct ucc_options {
   int precision;          /* ucc_precision, default UCC_FP64 */
   int refine_sweeps;      /* FP64 sweeps after a MIXED solve, default 2 */
   int print;              /* 0 silent, 1 iteration table on stdout */
+  double mixed_switch;    /* MIXED: residual norm at which FP64 sweeps take over, default 1e-5 */
 } ucc_options;
 
 void ucc_options_default(ucc_options* opt);
@@ -118,7 +119,63 @@ ucc_status ucc_get_tensor(ucc_ctx* ctx, const char* name, double* host_out, size
 /* Copy-in (restart files, learned guesses): "t1" "t2" "l1" "l2". */
 ucc_status ucc_set_tensor(ucc_ctx* ctx, const char* name, const double* host_in, size_t count);
 
+/* ---- Learned T2 starting amplitudes (no counterpart in the reference; its guess is MP2,
+ * ccwfn.cc:75-87).  A small MLP (8 pair features -> 256 -> 256 -> 1, SiLU, FP16 weights,
+ * FP32 accumulation) predicts S*(t2_CCSD - t2_MP2) per doubles element, S = 100; the
+ * plain CCSD iteration started from its prediction decides the converged answer.
+ * Features of element (i,j,a,b), D = e_i+e_j-e_a-e_b: S<ij|ab>/D, S<ij|ba>/D, S<ij|ab>,
+ * -1/D, (e_i+e_j)/2, (e_a+e_b)/2, [i==j], [a==b].  Rows are [no][no][nv][nv] order. */
+typedef struct ucc_mlp ucc_mlp;
+ucc_status ucc_mlp_create(ucc_mlp** net, int device, uint64_t seed);
+ucc_status ucc_mlp_destroy(ucc_mlp* net);
+const char* ucc_mlp_last_error(ucc_mlp* net);
+int ucc_mlp_num_params(void);
+/* parameters (FP32 masters) in the order W1[8][256] b1[256] W2[256][256] b2[256] w3[256] b3 */
+ucc_status ucc_mlp_get_params(ucc_mlp* net, float* out, size_t count);
+ucc_status ucc_mlp_set_params(ucc_mlp* net, const float* in, size_t count);
+/* predictions y[rows] for features X[rows][8] (host buffers) */
+ucc_status ucc_mlp_predict(ucc_mlp* net, const float* X, int64_t rows, float* y);
+/* mean squared error and its gradient (count = ucc_mlp_num_params()) on one batch */
+ucc_status ucc_mlp_loss_grad(ucc_mlp* net, const float* X, const float* t, int64_t rows, float* loss, float* grad,
+                             size_t count);
+/* Adam, minibatches of `batch` rows shuffled per epoch; final_loss = last epoch's mean */
+ucc_status ucc_mlp_train(ucc_mlp* net, const float* X, const float* t, int64_t rows, int epochs, int batch, float lr,
+                         uint64_t seed, float* final_loss);
+/* features (and, after a converged ucc_ccsd, targets) of the loaded Hamiltonian */
+ucc_status ucc_mlp_features(ucc_ctx* ctx, float* X, size_t rows, int with_targets, float* targets);
+/* the next ucc_ccsd on ctx starts from t1 = f_ia/D1, t2 = t2_MP2 + prediction/S */
+ucc_status ucc_mlp_guess(ucc_ctx* ctx, ucc_mlp* net);
+
 /* Per-stage device timings (CUDA events on the library's stream) and FLOP counts. */
+/* ------------------------------------------------------------------------------------
+ * Batched CCSD: many small Hamiltonians of different sizes solved together, each sweep
+ * one CUDA-graph launch of grouped kernels (no counterpart in the reference, which
+ * solves one molecule per call).  FP64 form; each member converges exactly as the
+ * single-context solver would, and is masked out of later sweeps once it has.
+ * ------------------------------------------------------------------------------------ */
+typedef struct ucc_batch ucc_batch;
+typedef struct ucc_batch_info {
+  int members;
+  int sweeps;              /* graph launches of the last solve */
+  int grouped_ops;         /* recorded residual operations, each one grouped launch per sweep */
+  int graph_kernels;       /* kernel nodes in the sweep graph */
+  int shape_choice[4];     /* GEMM operations given tile 64x64, 32x32, 64x32, 32x64 by the autotuner */
+  double solve_ms;         /* device time of the last solve (CUDA events) */
+  double flops;            /* algorithmic CCSD FLOPs of the last solve, summed over members' iterations */
+  double arena_bytes;      /* recorded scratch held for the members */
+} ucc_batch_info;
+ucc_status ucc_batch_create(ucc_batch** out, int device);
+ucc_status ucc_batch_destroy(ucc_batch* b);
+const char* ucc_batch_last_error(ucc_batch* b);
+/* add a member from its Fock matrix [nact][nact] and factors B[naux][nact][nact] */
+ucc_status ucc_batch_add_df(ucc_batch* b, int no, int nv, int naux, const double* fock, const double* B, int* index);
+/* the next solve starts member `index` from the network's T2 (ucc_mlp_guess semantics) */
+ucc_status ucc_batch_guess_mlp(ucc_batch* b, int index, ucc_mlp* net);
+/* solve every member: e_ccsd, iterations and converged (0/1) are arrays of length members */
+ucc_status ucc_batch_ccsd(ucc_batch* b, const ucc_options* opt, double* e_ccsd, int* iterations, int* converged);
+ucc_status ucc_batch_get_info(ucc_batch* b, ucc_batch_info* out);
+ucc_status ucc_batch_get_t2(ucc_batch* b, int index, double* out, size_t count);
+
 typedef struct ucc_stats {
   double ccsd_ms, triples_ms, hbar_ms, lambda_ms, density_ms, pert_ms;
   double ccsd_flops, triples_flops;
@@ -131,6 +188,9 @@ typedef struct ucc_stats {
   int fp64_iterations;       /* CCSD iterations whose residual was built in FP64 */
   int64_t tc_gemm_launches;  /* tensor-core (BF16 split) GEMM launches */
   int mixed_iterations;      /* CCSD iterations with split-product residuals */
+  double tc_gemm_ms;         /* device time of the tensor-core GEMMs (CUDA events) */
+  double tc_gemm_flops;      /* their algorithmic FLOPs, 2*M*N*K per GEMM */
+  int anchored_iterations;   /* refinement iterations built as FP64 anchor + tensor-core corrections */
 } ucc_stats;
 ucc_status ucc_get_stats(ucc_ctx* ctx, ucc_stats* out);
 ucc_status ucc_reset_stats(ucc_ctx* ctx);

@@ -39,7 +39,7 @@ inline void check(ucc_ctx* ctx, ucc_status s) {
 struct Options {
   std::string wfn = "CCSD", dertype = "NONE", myhand = "RIGHT", precision = "FP64";
   int maxiter = 100, refine_sweeps = 2, print = 0;
-  double r_convergence = 1e-7, my_omega = 0.0;
+  double r_convergence = 1e-7, my_omega = 0.0, mixed_switch = 1e-5;
   bool diis = true;
 };
 
@@ -78,6 +78,7 @@ class CCWfn {
     u.precision = o.precision == "MIXED" ? UCC_MIXED : UCC_FP64;
     u.refine_sweeps = o.refine_sweeps;
     u.print = o.print;
+    u.mixed_switch = o.mixed_switch;
     check(H_->ctx(), ucc_set_options(H_->ctx(), &u));
   }
   // ccwfn.cc:188-258: CCSD correlation energy, plus (T) for WFN == CCSD_T

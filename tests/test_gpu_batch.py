@@ -1,0 +1,60 @@
+"""Batched CCSD: every member must end where the one-context solver ends.
+
+Members of one smooth family with uneven sizes are solved together (one graph launch
+per sweep); each member's energy, iteration count and amplitudes are compared with a
+separate single-context solve of the same Hamiltonian.
+"""
+import numpy as np
+import pytest
+
+import ugacc_gb300 as U
+from ugacc_gb300.generator import make_family
+
+pytestmark = pytest.mark.gpu
+
+
+def _single(h, opts):
+    H = U.Hamiltonian.from_synthetic(h)
+    cc = U.CCWfn(H, opts)
+    e = cc.compute_energy()
+    return e, cc.iterations, cc.t2
+
+
+@pytest.mark.parametrize("diis", [True, False])
+def test_batch_matches_single_solves(diis):
+    fam = make_family(9, seed=21, no_range=(4, 7), nv_range=(20, 40))
+    opts = {"R_CONVERGENCE": 1e-9, "DIIS": diis, "MAXITER": 60}
+    bt = U.Batch()
+    for h in fam:
+        bt.add(h)
+    e, it, cv = bt.ccsd(opts)
+    assert cv.all()
+    for k, h in enumerate(fam):
+        e1, it1, t2 = _single(h, opts)
+        assert abs(e[k] - e1) < 1e-10, (k, e[k], e1)
+        assert abs(int(it[k]) - it1) <= 1, (k, it[k], it1)
+        np.testing.assert_allclose(bt.t2(k), t2, atol=1e-7, rtol=0)
+    info = bt.info()
+    assert info["members"] == len(fam) and info["sweeps"] == it.max()
+    assert info["grouped_ops"] > 10 and sum(info["shape_choice"]) > 0 and info["graph_kernels"] > info["grouped_ops"]
+    # a second solve starts again from MP2 and repeats the first exactly
+    e2, it2, _ = bt.ccsd(opts)
+    np.testing.assert_array_equal(it2, it)
+    np.testing.assert_allclose(e2, e, rtol=0, atol=1e-13)
+
+
+def test_batch_iteration_limit():
+    fam = make_family(3, seed=5, no_range=(4, 5), nv_range=(20, 24))
+    bt = U.Batch()
+    for h in fam:
+        bt.add(h)
+    e, it, cv = bt.ccsd({"R_CONVERGENCE": 1e-12, "MAXITER": 3})
+    assert not cv.any() and (it == 3).all()
+
+
+def test_batch_rejects_mixed_precision():
+    fam = make_family(1, seed=5, no_range=(4, 4), nv_range=(20, 20))
+    bt = U.Batch()
+    bt.add(fam[0])
+    with pytest.raises(U.UccError):
+        bt.ccsd({"PRECISION": "MIXED"})

@@ -39,7 +39,8 @@ class ConvergenceError(UccError):
 
 class _Options(ctypes.Structure):
     _fields_ = [("maxiter", ctypes.c_int), ("r_convergence", ctypes.c_double), ("diis", ctypes.c_int),
-                ("precision", ctypes.c_int), ("refine_sweeps", ctypes.c_int), ("print", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("refine_sweeps", ctypes.c_int), ("print", ctypes.c_int),
+                ("mixed_switch", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -50,10 +51,23 @@ class Stats(ctypes.Structure):
                 ("kernel_launches", ctypes.c_int64), ("ladder_ms", ctypes.c_double),
                 ("ladder_bytes", ctypes.c_double), ("ladder_flops", ctypes.c_double),
                 ("ladder_launches", ctypes.c_int64), ("fp64_iterations", ctypes.c_int),
-                ("tc_gemm_launches", ctypes.c_int64), ("mixed_iterations", ctypes.c_int)]
+                ("tc_gemm_launches", ctypes.c_int64), ("mixed_iterations", ctypes.c_int),
+                ("tc_gemm_ms", ctypes.c_double), ("tc_gemm_flops", ctypes.c_double),
+                ("anchored_iterations", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("members", ctypes.c_int), ("sweeps", ctypes.c_int), ("grouped_ops", ctypes.c_int),
+                ("graph_kernels", ctypes.c_int), ("shape_choice", ctypes.c_int * 4), ("solve_ms", ctypes.c_double),
+                ("flops", ctypes.c_double), ("arena_bytes", ctypes.c_double)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["shape_choice"] = list(self.shape_choice)
+        return d
 
 
 _lib = None
@@ -76,6 +90,7 @@ def load_library(path: str | None = None):
     P = ctypes.POINTER
     d, i, vp, cp = ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_char_p
     dp = P(d)
+    fp = P(ctypes.c_float)
     sig = {
         "ucc_options_default": (None, [P(_Options)]),
         "ucc_ctx_create": (i, [P(vp), i]),
@@ -99,6 +114,25 @@ def load_library(path: str | None = None):
         "ucc_status_string": (cp, [i]),
         "ucc_triples_noalloc": (i, [i, i, vp, vp, vp, vp, vp, vp, dp, vp, cp, ctypes.c_size_t]),
         "ucc_gemm": (i, [vp, i, i, i, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, d, dp, dp, d, dp]),
+        "ucc_mlp_create": (i, [P(vp), i, ctypes.c_uint64]),
+        "ucc_mlp_destroy": (i, [vp]),
+        "ucc_mlp_last_error": (cp, [vp]),
+        "ucc_mlp_num_params": (i, []),
+        "ucc_mlp_get_params": (i, [vp, fp, ctypes.c_size_t]),
+        "ucc_mlp_set_params": (i, [vp, fp, ctypes.c_size_t]),
+        "ucc_mlp_predict": (i, [vp, fp, ctypes.c_int64, fp]),
+        "ucc_mlp_loss_grad": (i, [vp, fp, fp, ctypes.c_int64, fp, fp, ctypes.c_size_t]),
+        "ucc_mlp_train": (i, [vp, fp, fp, ctypes.c_int64, i, i, ctypes.c_float, ctypes.c_uint64, fp]),
+        "ucc_mlp_features": (i, [vp, fp, ctypes.c_size_t, i, fp]),
+        "ucc_mlp_guess": (i, [vp, vp]),
+        "ucc_batch_create": (i, [P(vp), i]),
+        "ucc_batch_destroy": (i, [vp]),
+        "ucc_batch_last_error": (cp, [vp]),
+        "ucc_batch_add_df": (i, [vp, i, i, i, dp, dp, P(i)]),
+        "ucc_batch_guess_mlp": (i, [vp, i, vp]),
+        "ucc_batch_ccsd": (i, [vp, P(_Options), dp, P(i), P(i)]),
+        "ucc_batch_get_info": (i, [vp, P(BatchInfo)]),
+        "ucc_batch_get_t2": (i, [vp, i, dp, ctypes.c_size_t]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -131,8 +165,9 @@ class Context:
             raise ConvergenceError(st, msg or "Computation has not converged.")
         raise UccError(st, msg)
 
-    def set_options(self, maxiter=100, r_convergence=1e-7, diis=True, precision=FP64, refine_sweeps=2, printing=0):
-        o = _Options(maxiter, r_convergence, int(diis), precision, refine_sweeps, printing)
+    def set_options(self, maxiter=100, r_convergence=1e-7, diis=True, precision=FP64, refine_sweeps=2, printing=0,
+                    mixed_switch=1e-5):
+        o = _Options(maxiter, r_convergence, int(diis), precision, refine_sweeps, printing, mixed_switch)
         self.check(self.lib.ucc_set_options(self.h, ctypes.byref(o)))
 
     def get(self, name: str, shape) -> np.ndarray:
@@ -179,7 +214,8 @@ class Context:
 # Mirror of the reference's classes
 # ------------------------------------------------------------------------------------
 DEFAULT_OPTIONS = {"WFN": "CCSD", "DERTYPE": "NONE", "MAXITER": 100, "R_CONVERGENCE": 1e-7, "DIIS": True,
-                   "MYHAND": "RIGHT", "MY_OMEGA": 0.0, "PRECISION": "FP64", "REFINE_SWEEPS": 2, "PRINT": 0}
+                   "MYHAND": "RIGHT", "MY_OMEGA": 0.0, "PRECISION": "FP64", "REFINE_SWEEPS": 2, "PRINT": 0,
+                   "MIXED_SWITCH": 1e-5}
 
 
 class Hamiltonian:
@@ -218,7 +254,8 @@ class CCWfn:
         o = self.options
         self.ctx.set_options(maxiter=int(o["MAXITER"]), r_convergence=float(o["R_CONVERGENCE"]), diis=bool(o["DIIS"]),
                              precision=MIXED if str(o["PRECISION"]).upper() == "MIXED" else FP64,
-                             refine_sweeps=int(o["REFINE_SWEEPS"]), printing=int(o["PRINT"]))
+                             refine_sweeps=int(o["REFINE_SWEEPS"]), printing=int(o["PRINT"]),
+                             mixed_switch=float(o["MIXED_SWITCH"]))
         self.no, self.nv = H.no, H.nv
         self.eccsd = self.et = None
         self.iterations = 0
@@ -385,3 +422,156 @@ def response(cc: CCWfn, hbar: HBAR, lam: CCLambda, perts, omega: float, hand: st
             r = CCResp(A, B)
             rot[axes[p] + axes[q]] = -(0.5 * r.linresp(A, B) - 0.5 * r.linresp(B, A))
     return alpha, rot, P
+
+
+# ------------------------------------------------------------------------------------
+# Learned T2 starting amplitudes
+# ------------------------------------------------------------------------------------
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class MLP:
+    """The guess network of mlp.cu: 8 pair features -> 256 -> 256 -> 1 (SiLU)."""
+
+    NFEAT = 8
+
+    def __init__(self, device: int = 0, seed: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        st = self.lib.ucc_mlp_create(ctypes.byref(h), device, seed)
+        if st != UCC_OK:
+            raise UccError(st, "cannot create the network")
+        self.h = h
+        self.nparam = self.lib.ucc_mlp_num_params()
+
+    def check(self, st):
+        if st != UCC_OK:
+            raise UccError(st, (self.lib.ucc_mlp_last_error(self.h) or b"").decode())
+
+    @property
+    def params(self) -> np.ndarray:
+        out = np.empty(self.nparam, dtype=np.float32)
+        self.check(self.lib.ucc_mlp_get_params(self.h, _fptr(out), out.size))
+        return out
+
+    @params.setter
+    def params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self.check(self.lib.ucc_mlp_set_params(self.h, _fptr(p), p.size))
+
+    def predict(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.empty(X.shape[0], dtype=np.float32)
+        self.check(self.lib.ucc_mlp_predict(self.h, _fptr(X), X.shape[0], _fptr(y)))
+        return y
+
+    def loss_grad(self, X, t):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        loss = ctypes.c_float()
+        g = np.empty(self.nparam, dtype=np.float32)
+        self.check(self.lib.ucc_mlp_loss_grad(self.h, _fptr(X), _fptr(t), X.shape[0], ctypes.byref(loss), _fptr(g),
+                                              g.size))
+        return loss.value, g
+
+    def train(self, X, t, epochs=5, batch=4096, lr=1e-3, seed=0) -> float:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        loss = ctypes.c_float()
+        self.check(self.lib.ucc_mlp_train(self.h, _fptr(X), _fptr(t), X.shape[0], epochs, batch, lr, seed,
+                                          ctypes.byref(loss)))
+        return loss.value
+
+    def guess(self, H: "Hamiltonian"):
+        """The next CCWfn.compute_energy() on H starts from the network's T2."""
+        H.ctx.check(self.lib.ucc_mlp_guess(H.ctx.h, self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ucc_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mlp_features(H: "Hamiltonian", with_targets: bool = False):
+    """Pair features (and targets after a converged CCSD) of every T2 element of H."""
+    n = H.no * H.no * H.nv * H.nv
+    X = np.empty((n, MLP.NFEAT), dtype=np.float32)
+    t = np.empty(n, dtype=np.float32) if with_targets else None
+    lib = H.ctx.lib
+    H.ctx.check(lib.ucc_mlp_features(H.ctx.h, _fptr(X), n, int(with_targets),
+                                     _fptr(t) if with_targets else None))
+    return (X, t) if with_targets else X
+
+
+# ------------------------------------------------------------------------------------
+# Batched CCSD over many Hamiltonians
+# ------------------------------------------------------------------------------------
+class Batch:
+    """Many small Hamiltonians solved together (ucc_batch_*): one graph launch per sweep."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        st = self.lib.ucc_batch_create(ctypes.byref(h), device)
+        if st != UCC_OK:
+            raise UccError(st, "cannot create a batch on CUDA device %d" % device)
+        self.h = h
+        self.sizes = []
+
+    def check(self, st):
+        if st != UCC_OK:
+            raise UccError(st, (self.lib.ucc_batch_last_error(self.h) or b"").decode())
+
+    def add(self, ham) -> int:
+        """Add a synthetic Hamiltonian (no, nv, naux, eps/fock, B)."""
+        fock = np.ascontiguousarray(ham.fock, dtype=np.float64)
+        B = np.ascontiguousarray(ham.B, dtype=np.float64)
+        idx = ctypes.c_int()
+        self.check(self.lib.ucc_batch_add_df(self.h, ham.no, ham.nv, ham.naux, _ptr(fock), _ptr(B), ctypes.byref(idx)))
+        self.sizes.append((ham.no, ham.nv))
+        return idx.value
+
+    def guess(self, index: int, net: "MLP"):
+        self.check(self.lib.ucc_batch_guess_mlp(self.h, index, net.h))
+
+    def ccsd(self, options: dict | None = None):
+        """Energies, iteration counts and convergence flags of every member."""
+        o = dict(DEFAULT_OPTIONS, **(options or {}))
+        prec = MIXED if str(o["PRECISION"]).upper() == "MIXED" else FP64
+        opts = _Options(int(o["MAXITER"]), float(o["R_CONVERGENCE"]), int(bool(o["DIIS"])), prec,
+                        int(o["REFINE_SWEEPS"]), int(o["PRINT"]), float(o["MIXED_SWITCH"]))
+        n = len(self.sizes)
+        e = np.zeros(n)
+        it = (ctypes.c_int * n)()
+        cv = (ctypes.c_int * n)()
+        self.check(self.lib.ucc_batch_ccsd(self.h, ctypes.byref(opts), _ptr(e), it, cv))
+        return e, np.array(list(it)), np.array(list(cv), dtype=bool)
+
+    def info(self) -> dict:
+        out = BatchInfo()
+        self.check(self.lib.ucc_batch_get_info(self.h, ctypes.byref(out)))
+        return out.as_dict()
+
+    def t2(self, index: int) -> np.ndarray:
+        no, nv = self.sizes[index]
+        out = np.empty((no, no, nv, nv))
+        self.check(self.lib.ucc_batch_get_t2(self.h, index, _ptr(out), out.size))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ucc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

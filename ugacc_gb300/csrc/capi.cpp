@@ -17,6 +17,8 @@ struct ucc_ctx {
 };
 
 namespace ucc {
+Ctx& ctx_of(ucc_ctx* h) { return h->c; }
+
 Ctx::~Ctx() {
   if (stream) cudaStreamSynchronize(stream);
   tc_cache.reset();
@@ -66,6 +68,7 @@ void ucc_options_default(ucc_options* o) {
   o->precision = UCC_FP64;
   o->refine_sweeps = 2;
   o->print = 0;
+  o->mixed_switch = 1e-5;
 }
 
 const char* ucc_status_string(ucc_status s) {
@@ -125,6 +128,7 @@ ucc_status ucc_set_options(ucc_ctx* ctx, const ucc_options* o) {
     UCC_REQUIRE(o->r_convergence > 0, UCC_BAD_ARGS, "r_convergence must be > 0");
     UCC_REQUIRE(o->precision == UCC_FP64 || o->precision == UCC_MIXED, UCC_BAD_ARGS, "bad precision");
     UCC_REQUIRE(o->refine_sweeps >= 0, UCC_BAD_ARGS, "refine_sweeps must be >= 0");
+    UCC_REQUIRE(o->mixed_switch > 0, UCC_BAD_ARGS, "mixed_switch must be > 0");
     c.opt = *o;
   });
 }

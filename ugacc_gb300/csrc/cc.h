@@ -53,6 +53,9 @@ struct CCSDResult {
   bool converged = false;
 };
 CCSDResult run_ccsd(Ctx& c);
+void ccsd_alloc(Ctx& c);                                         // CCSD work arrays
+void ccsd_residual(Ctx& c, const double* t_old, double* r);      // R(t_old), tau/ttau current
+double ccsd_energy(Ctx& c, const double* t);                     // E from t and the stored tau
 double run_triples(Ctx& c);
 void run_hbar(Ctx& c);
 CCSDResult run_lambda(Ctx& c);

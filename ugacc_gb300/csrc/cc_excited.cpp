@@ -215,8 +215,10 @@ CCSDResult run_lambda(Ctx& c) {  // :93-129
     Tensor l2 = amp2(c, Lam.p);
     transpose_add(c, "ijab->ijba", -2.0, t2, 0.0, l2);
     axpby(c, l2.size(), 4.0, t2.p, 1.0, l2.p);
-  } else {
+  } else {  // a supplied guess applies to this solve only
     UCC_CUDA(cudaMemcpyAsync(Lam.p, c.get("Lam_guess").p, sizeof(double) * np, cudaMemcpyDeviceToDevice, c.stream));
+    UCC_CUDA(cudaStreamSynchronize(c.stream));
+    c.drop("Lam_guess");
   }
   Tensor eps = c.get("eps");
   Scratch sumsq(c, sizeof(double));

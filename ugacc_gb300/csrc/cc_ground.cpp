@@ -310,72 +310,68 @@ void build_t1(Ctx& c, const Tensor& t1, const Tensor& t2, Tensor R1) {
   contract(c, "mnae,nmei->ia", -1.0, t2, L(c, "oovo"), 1.0, R1);
 }
 
-// build_t2, ccwfn.cc:471-539 (unscaled residual)
+// build_t2, ccwfn.cc:471-539 (unscaled residual).
+//
+// The residual is symmetric under the simultaneous swap (i<->j, a<->b): the reference
+// computes each term and its swapped partner explicitly.  Here one member of each pair
+// goes into a half residual Rh and R2 = <ij|ab> + Woooo.tau + ladder + Rh + Rh(ji,ba);
+// <ij|ab>, the hole ladder and the particle ladder are symmetric on their own.
+//
+void ladder(Ctx& c, const Tensor& tau, const Tensor& R2) {
+  contract(c, "ijef,abef->ijab", 1.0, tau, V(c, "vvvv"), 1.0, R2);
+}
+
 void build_t2(Ctx& c, const Tensor& t1, const Tensor& t2, const Tensor& tau, Tensor R2, std::vector<cudaEvent_t>* ev) {
   const int no = c.no, nv = c.nv;
   Tensor Fvv = c.get("Fvv"), Foo = c.get("Foo"), Fov = c.get("Fov");
   Tensor Woooo = c.get("Woooo"), Wovov = c.get("Wovov"), Wovvo = c.get("Wovvo"), Zmbij = c.get("Zmbij");
   copy_into(c, V(c, "oovv"), R2);
-  contract(c, "ijae,be->ijab", 1.0, t2, Fvv, 1.0, R2);
-  contract(c, "jibe,ae->ijab", 1.0, t2, Fvv, 1.0, R2);
-  Temp tF(c, {nv, nv});
-  contract(c, "mb,me->be", 1.0, t1, Fov, 0.0, tF);
-  contract(c, "ijae,be->ijab", -0.5, t2, tF, 1.0, R2);
-  contract(c, "ijeb,ae->ijab", -0.5, t2, tF, 1.0, R2);
-  contract(c, "imab,mj->ijab", -1.0, t2, Foo, 1.0, R2);
-  contract(c, "mjab,mi->ijab", -1.0, t2, Foo, 1.0, R2);
-  Temp tF2(c, {no, no});
-  contract(c, "je,me->mj", 1.0, t1, Fov, 0.0, tF2);
-  contract(c, "imab,mj->ijab", -0.5, t2, tF2, 1.0, R2);
-  contract(c, "mjab,mi->ijab", -0.5, t2, tF2, 1.0, R2);
   contract(c, "mnab,mnij->ijab", 1.0, tau, Woooo, 1.0, R2);
-  // particle ladder (Wabef = <ab|ef> tau), the dominant term
   if (ev) {
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     cudaEventRecord(a, c.stream);
-    contract(c, "ijef,abef->ijab", 1.0, tau, V(c, "vvvv"), 1.0, R2);
+    ladder(c, tau, R2);
     cudaEventRecord(b, c.stream);
     ev->push_back(a);
     ev->push_back(b);
   } else {
-    contract(c, "ijef,abef->ijab", 1.0, tau, V(c, "vvvv"), 1.0, R2);
+    ladder(c, tau, R2);
   }
-  contract(c, "ie,abej->ijab", 1.0, t1, V(c, "vvvo"), 1.0, R2);
-  contract(c, "je,baei->ijab", 1.0, t1, V(c, "vvvo"), 1.0, R2);
-  contract(c, "ma,mbij->ijab", -1.0, t1, V(c, "ovoo"), 1.0, R2);
-  contract(c, "mb,maji->ijab", -1.0, t1, V(c, "ovoo"), 1.0, R2);
+  Temp Rh(c, {no, no, nv, nv});
+  contract(c, "ijae,be->ijab", 1.0, t2, Fvv, 0.0, Rh);
   {
-    Temp t2a(c, {no, no, nv, nv});
-    transpose_add(c, "ijab->ijba", -1.0, t2, 0.0, t2a);
-    axpby(c, t2a->size(), 1.0, t2.p, 1.0, t2a->p);
-    contract(c, "imae,mbej->ijab", 1.0, t2a, Wovvo, 1.0, R2);
-    contract(c, "jmbe,maei->ijab", 1.0, t2a, Wovvo, 1.0, R2);
+    Temp tF(c, {nv, nv});
+    contract(c, "mb,me->be", 1.0, t1, Fov, 0.0, tF);
+    contract(c, "ijae,be->ijab", -0.5, t2, tF, 1.0, Rh);
+    Temp tF2(c, {no, no});
+    contract(c, "je,me->mj", 1.0, t1, Fov, 0.0, tF2);
+    axpby(c, tF2->size(), 0.5, tF2->p, 0.0, tF2->p);
+    axpby(c, Foo.size(), 1.0, Foo.p, 1.0, tF2->p);  // Foo + tF2 / 2
+    contract(c, "imab,mj->ijab", -1.0, t2, tF2, 1.0, Rh);
   }
+  contract(c, "ie,abej->ijab", 1.0, t1, V(c, "vvvo"), 1.0, Rh);
+  contract(c, "ma,mbij->ijab", -1.0, t1, V(c, "ovoo"), 1.0, Rh);
   {
-    Temp WW(c, {no, nv, nv, no});
-    transpose_add(c, "mbje->mbej", 1.0, Wovov, 0.0, WW);
-    axpby(c, WW->size(), 1.0, Wovvo.p, 1.0, WW->p);
-    contract(c, "imae,mbej->ijab", 1.0, t2, WW, 1.0, R2);
-    contract(c, "jmbe,maei->ijab", 1.0, t2, WW, 1.0, R2);
+    // (t2 - t2(ba)) Wovvo + t2 (Wovvo + Wovov(..je->..ej)) = (2 t2 - t2(ba)) Wovvo + t2 Wovov^T
+    Temp t2x(c, {no, no, nv, nv});
+    transpose_add(c, "ijab->ijba", -1.0, t2, 0.0, t2x);
+    axpby(c, t2x->size(), 2.0, t2.p, 1.0, t2x->p);
+    contract(c, "imae,mbej->ijab", 1.0, t2x, Wovvo, 1.0, Rh);
+    contract(c, "imae,mbje->ijab", 1.0, t2, Wovov, 1.0, Rh);
   }
-  contract(c, "mjae,mbie->ijab", 1.0, t2, Wovov, 1.0, R2);
-  contract(c, "imeb,maje->ijab", 1.0, t2, Wovov, 1.0, R2);
+  contract(c, "mjae,mbie->ijab", 1.0, t2, Wovov, 1.0, Rh);
   {
-    // t1 t1 <..|..> terms and the Zmbij terms share the t1[m,a] / t1[m,b] contraction:
-    //   Za[m,b,i,j] = Zmbij + t1[i,e] <mb|ej> + t1[j,e] <mb|ie>   -> - t1[m,a] Za[m,b,i,j]
-    //   Zb[m,a,i,j] = Zmbij[m,a,j,i] + t1[i,e] <ma|je> + t1[j,e] <ma|ei> -> - t1[m,b] Zb
-    Temp Za(c, {no, nv, no, no}), Zb(c, {no, nv, no, no});
+    // Za[m,b,i,j] = Zmbij + t1[i,e] <mb|ej> + t1[j,e] <mb|ie>  ->  - t1[m,a] Za[m,b,i,j]
+    Temp Za(c, {no, nv, no, no});
     copy_into(c, Zmbij, Za);
     contract(c, "ie,mbej->mbij", 1.0, t1, V(c, "ovvo"), 1.0, Za);
     contract(c, "je,mbie->mbij", 1.0, t1, V(c, "ovov"), 1.0, Za);
-    transpose_add(c, "maji->maij", 1.0, Zmbij, 0.0, Zb);
-    contract(c, "ie,maje->maij", 1.0, t1, V(c, "ovov"), 1.0, Zb);
-    contract(c, "je,maei->maij", 1.0, t1, V(c, "ovvo"), 1.0, Zb);
-    contract(c, "ma,mbij->ijab", -1.0, t1, Za, 1.0, R2);
-    contract(c, "mb,maij->ijab", -1.0, t1, Zb, 1.0, R2);
+    contract(c, "ma,mbij->ijab", -1.0, t1, Za, 1.0, Rh);
   }
+  axpby(c, Rh->size(), 1.0, Rh->p, 1.0, R2.p);
+  transpose_add(c, "jiba->ijab", 1.0, Rh, 1.0, R2);
 }
 
 double energy(Ctx& c, const Tensor& t1, const Tensor& tau) {
@@ -390,14 +386,13 @@ double energy(Ctx& c, const Tensor& t1, const Tensor& tau) {
 
 }  // namespace
 
-// residual norm below which BF16 hi+lo split products stop resolving the update
-constexpr double kMixedFloor = 1e-6;
-
-CCSDResult run_ccsd(Ctx& c) {
-  UCC_REQUIRE(c.loaded, UCC_BAD_STATE, "no Hamiltonian loaded");
+// CCSD work arrays of one context (amplitudes packed as [t1 | t2])
+void ccsd_alloc(Ctx& c) {
   const int no = c.no, nv = c.nv;
   const int64_t np = npacked(c);
-  Tensor T = c.alloc("T", {np}, false), Told = c.alloc("Told", {np}, true), R = c.alloc("R", {np}, false);
+  c.alloc("T", {np}, false);
+  c.alloc("Told", {np}, true);
+  c.alloc("R", {np}, false);
   c.alloc("tau", {no, no, nv, nv}, false);
   c.alloc("ttau", {no, no, nv, nv}, false);
   c.alloc("Fvv", {nv, nv}, false);
@@ -407,6 +402,29 @@ CCSDResult run_ccsd(Ctx& c) {
   c.alloc("Wovov", {no, nv, no, nv}, false);
   c.alloc("Wovvo", {no, nv, nv, no}, false);
   c.alloc("Zmbij", {no, nv, no, no}, false);
+}
+
+// the unscaled residual R(t_old) into r, given tau/ttau of t_old (ccwfn.cc:311-539)
+void ccsd_residual(Ctx& c, const double* t_old, double* r) {
+  Tensor t1 = amp1(c, const_cast<double*>(t_old)), t2 = amp2(c, const_cast<double*>(t_old));
+  build_F(c, t1, c.get("ttau"));
+  build_W(c, t1, t2, c.get("tau"));
+  build_t1(c, t1, t2, amp1(c, r));
+  build_t2(c, t1, t2, c.get("tau"), amp2(c, r), nullptr);
+}
+
+double ccsd_energy(Ctx& c, const double* t) { return energy(c, amp1(c, const_cast<double*>(t)), c.get("tau")); }
+
+// residual norm near which BF16 hi+lo split products with FP32 accumulation stop
+// resolving the update (measured ~1.5e-6 at no=16/nv=160)
+constexpr double kMixedFloor = 2e-6;
+
+CCSDResult run_ccsd(Ctx& c) {
+  UCC_REQUIRE(c.loaded, UCC_BAD_STATE, "no Hamiltonian loaded");
+  const int no = c.no, nv = c.nv;
+  const int64_t np = npacked(c);
+  ccsd_alloc(c);
+  Tensor T = c.get("T"), Told = c.get("Told");
   Tensor eps = c.get("eps");
   const double* d_do = eps.p;
   const double* d_dv = eps.p + no;
@@ -419,8 +437,10 @@ CCSDResult run_ccsd(Ctx& c) {
     copy_into(c, V(c, "oovv"), amp2(c, R0->p));
     jacobi_update(c, no, nv, d_do, d_dv, 0.0, R0->p, R0->p + (int64_t)no * nv, Told.p, Told.p + (int64_t)no * nv, T.p,
                   T.p + (int64_t)no * nv, sumsq.d());
-  } else {
+  } else {  // a supplied guess (restart file, learned guess) applies to this solve only
     UCC_CUDA(cudaMemcpyAsync(T.p, c.get("T_guess").p, sizeof(double) * np, cudaMemcpyDeviceToDevice, c.stream));
+    UCC_CUDA(cudaStreamSynchronize(c.stream));
+    c.drop("T_guess");
   }
   auto tau_of = [&](double* buf) {
     build_tau(c, no, nv, buf, buf + (int64_t)no * nv, 1.0, c.get("tau").p, 0.5, c.get("ttau").p);
@@ -438,25 +458,61 @@ CCSDResult run_ccsd(Ctx& c) {
   Diis diis(c, np, 8);
   std::vector<cudaEvent_t> ev;
   double rms = INFINITY, rms_prev = INFINITY, eccsd = NAN;
-  // Mixed precision: residuals from BF16 hi+lo split GEMMs until the residual norm
-  // reaches the split-product noise floor (or stops falling), then FP64 sweeps until
-  // ||R|| < r_convergence; at least refine_sweeps FP64 iterations close the solve.
+  // Mixed precision (three kinds of sweep):
+  //  split  - residual from BF16 hi+lo split GEMMs, until the residual norm reaches the
+  //           split-product noise floor (or stops falling);
+  //  record - FP64 residual that also records every heavy GEMM as an anchor;
+  //  delta  - FP64 residual whose heavy GEMMs are anchor + tensor-core corrections.
+  // The solve ends only on a record sweep with ||R|| < r_convergence (and at least
+  // refine_sweeps record sweeps); a delta sweep that gets there, or stalls, asks for one.
+  enum Sweep { kFp64, kSplit, kRecord, kDelta };
   const bool mixed = c.opt.precision == UCC_MIXED;
-  bool fp64_phase = !mixed;
-  int fp64_iters = 0;
+  const bool refine = mixed && c.opt.refine_sweeps > 0;
+  bool split_phase = mixed, record_next = true;
+  int stalls = 0, record_sweeps = 0, delta_sweeps = 0, split_sweeps = 0;
   int iter = 0;
+  c.anchors.clear();
   for (iter = 1; iter <= c.opt.maxiter; iter++) {
     c.store["T"].swap(c.store["Told"]);  // amp_save, ccwfn.cc:300-309
     double* to = c.get("Told").p;
     double* tn = c.get("T").p;
     double* r = c.get("R").p;
     Tensor t1 = amp1(c, to), t2 = amp2(c, to);
+    const Sweep kind = !mixed ? kFp64 : split_phase ? kSplit : record_next ? kRecord : kDelta;
     {
-      Fp64Scope scope(c, fp64_phase);
+      Fp64Scope scope(c, kind != kSplit);
+      if (kind == kRecord) c.anchors.begin(1);
+      if (kind == kDelta) c.anchors.begin(2);
       build_F(c, t1, c.get("ttau"));
       build_W(c, t1, t2, c.get("tau"));
       build_t1(c, t1, t2, amp1(c, r));
       build_t2(c, t1, t2, c.get("tau"), amp2(c, r), &ev);
+      c.anchors.mode = 0;
+    }
+    double noise = -1.0, drift = -1.0;
+    if (c.opt.print >= 2 && mixed) {
+      // diagnostics: distance of this residual from the FP64 one at the same amplitudes,
+      // and of the amplitudes from the last anchor
+      if (kind == kRecord) {
+        c.alloc("T_anchor", {np}, false);
+        UCC_CUDA(cudaMemcpyAsync(c.get("T_anchor").p, to, sizeof(double) * np, cudaMemcpyDeviceToDevice, c.stream));
+      } else {
+        Temp Rx(c, {np});
+        {
+          Fp64Scope f(c);
+          const int saved = c.anchors.mode;
+          c.anchors.mode = 0;
+          ccsd_residual(c, to, Rx->p);
+          c.anchors.mode = saved;
+        }
+        axpby(c, np, -1.0, r, 1.0, Rx->p);
+        noise = std::sqrt(dot(c, np, Rx->p, Rx->p));
+        if (kind == kDelta) {
+          axpby(c, np, 1.0, to, 0.0, Rx->p);
+          axpby(c, np, -1.0, c.get("T_anchor").p, 1.0, Rx->p);
+          drift = std::sqrt(dot(c, np, Rx->p, Rx->p));
+        }
+      }
     }
     jacobi_update(c, no, nv, d_do, d_dv, 0.0, r, r + (int64_t)no * nv, to, to + (int64_t)no * nv, tn,
                   tn + (int64_t)no * nv, sumsq.d());
@@ -465,21 +521,37 @@ CCSDResult run_ccsd(Ctx& c) {
     UCC_CUDA(cudaStreamSynchronize(c.stream));
     rms = std::sqrt(ss);
     UCC_REQUIRE(std::isfinite(rms), UCC_NAN_DETECTED, "CCSD residual is not finite");
-    if (fp64_phase) fp64_iters++;
-    const bool refined = !mixed || c.opt.refine_sweeps == 0 || (fp64_phase && fp64_iters >= c.opt.refine_sweeps);
-    if (rms < c.opt.r_convergence && refined) break;
-    bool switched = false;
-    if (mixed && !fp64_phase && c.opt.refine_sweeps > 0 &&
-        (rms < std::max(c.opt.r_convergence, kMixedFloor) || (iter > 2 && rms > 0.5 * rms_prev))) {
-      fp64_phase = true;
-      switched = true;
-      c.stats.mixed_iterations = iter;
+    bool keep_history = true;
+    if (kind == kFp64) {
+      if (rms < c.opt.r_convergence) break;
+    } else if (kind == kSplit) {
+      split_sweeps++;
+      if (!refine && rms < c.opt.r_convergence) break;
+      // hand over near the split-product noise floor or when the residual stops falling
+      if (refine && (rms < std::max(c.opt.r_convergence, std::max(c.opt.mixed_switch, kMixedFloor)) ||
+                     (iter > 2 && rms > 0.5 * rms_prev))) {
+        split_phase = false;
+        record_next = true;
+        diis.reset();  // the split-sweep history extrapolates a different map
+        keep_history = false;
+      }
+    } else if (kind == kRecord) {
+      record_sweeps++;
+      record_next = false;
+      stalls = 0;
+      if (rms < c.opt.r_convergence && record_sweeps >= c.opt.refine_sweeps) break;
+    } else {
+      delta_sweeps++;
+      if (rms < c.opt.r_convergence) {
+        record_next = true;  // confirm with an FP64 residual
+      } else if (rms > 0.7 * rms_prev) {
+        if (++stalls >= 2) record_next = true;  // corrections no longer resolved: re-anchor
+      } else {
+        stalls = 0;
+      }
     }
     rms_prev = rms;
-    // error vectors of split-product residuals do not extrapolate FP64 ones: the refinement
-    // sweeps start a fresh DIIS subspace
-    if (switched) diis.reset();
-    if (c.opt.diis) {
+    if (c.opt.diis && keep_history) {
       diis.add(tn, to);
       if (diis.size() > 2) diis.extrapolate(tn);
     }
@@ -487,9 +559,18 @@ CCSDResult run_ccsd(Ctx& c) {
     eccsd = energy(c, amp1(c, tn), c.get("tau"));
     if (c.opt.print) {
       double t1n = std::sqrt(dot(c, (int64_t)no * nv, tn, tn) / (2 * no));
-      std::printf("\t  %3d  %20.15f  %8.6f  %8.6e\n", iter, eccsd, t1n, rms);
+      static const char* tag[] = {"", " split", " record", " delta"};
+      std::printf("\t  %3d  %20.15f  %8.6f  %8.6e%s", iter, eccsd, t1n, rms, tag[kind]);
+      if (noise >= 0.0) std::printf("  |R-R64| %.3e", noise);
+      if (drift >= 0.0) std::printf("  |T-T0| %.3e", drift);
+      std::printf("\n");
     }
   }
+  c.anchors.clear();
+  if (c.has("T_anchor")) c.drop("T_anchor");
+  c.stats.mixed_iterations = split_sweeps;
+  c.stats.anchored_iterations = delta_sweeps;
+  const int fp64_iters = mixed ? record_sweeps : std::min(iter, c.opt.maxiter);
   tau_of(c.get("T").p);
   UCC_CUDA(cudaStreamSynchronize(c.stream));
   for (size_t k = 0; k + 1 < ev.size(); k += 2) {

@@ -77,9 +77,11 @@ struct DeviceBuffer {
 struct Ctx;
 
 // Stream-ordered scratch allocation (CUDA's async pool on the context stream).
+struct Recorder;
 struct Scratch {
   Ctx* ctx = nullptr;
   void* p = nullptr;
+  Recorder* rec = nullptr;  // allocated from a recorder's arena
   Scratch(Ctx& c, size_t bytes);
   ~Scratch();
   double* d() const { return static_cast<double*>(p); }
@@ -106,6 +108,14 @@ struct Fp64Scope {
   explicit Fp64Scope(Ctx& ctx, bool on = true);
   ~Fp64Scope();
 };
+// Scoped setting of the FP64 switch to a given value (false re-enables split products
+// inside an FP64 scope when the context precision is MIXED).
+struct PrecisionScope {
+  Ctx& c;
+  bool saved;
+  PrecisionScope(Ctx& ctx, bool force_fp64);
+  ~PrecisionScope();
+};
 
 struct Ctx {
   int device = 0;
@@ -127,6 +137,32 @@ struct Ctx {
   void drop(const std::string& name);
 
   bool force_fp64 = false;  // integral construction and refinement sweeps stay FP64
+
+  // Anchored refinement of a mixed-precision solve.  In a record sweep (mode 1) every
+  // heavy GEMM runs in FP64 and keeps its operands A0, B0 and product P0 = A0 B0; in a
+  // delta sweep (mode 2) the same GEMM, found by its position in the sweep, is evaluated
+  // as P0 + (A - A0) B + A0 (B - B0) with the two correction products on the tensor
+  // cores, so that their rounding error scales with the distance from the anchor.
+  struct AnchorTerm {
+    int64_t M = 0, N = 0, K = 0;
+    bool a_const = false, b_const = false;
+    std::unique_ptr<DeviceBuffer> a0, b0, p0;  // dense [M][K], [K][N], [M][N]
+  };
+  struct Anchors {
+    int mode = 0;  // 0 off, 1 record, 2 delta
+    size_t next = 0;
+    std::vector<AnchorTerm> terms;
+    void begin(int m) {
+      mode = m;
+      next = 0;
+      if (m == 1) terms.clear();
+    }
+    void clear() {
+      mode = 0;
+      next = 0;
+      terms.clear();
+    }
+  } anchors;
   // state of the tensor-core path (split operand cache, error flag), dropped on reload
   std::shared_ptr<void> tc_cache;
   // true if p lies in a block that never changes once built (integrals, L, HBAR)
@@ -136,6 +172,46 @@ struct Ctx {
 
   ~Ctx();
 };
+
+// ----------------------------------------------------------------------------------
+// Operation recording for grouped replay (batched solver).  While a Recorder is
+// installed on the calling thread, the GEMM / GEMV / permute / axpby / fill launchers
+// append a description of their work instead of launching, Scratch allocations come
+// from the recorder's arena (a stack: scoped scratch is released in reverse order), and
+// contract() takes its index-group orders from a tape shared by all recorded problems,
+// so that every problem yields the same operation sequence.
+// ----------------------------------------------------------------------------------
+struct RecordedOp {
+  enum Kind { kGemm = 0, kPermute = 1, kFill = 2 } kind = kGemm;
+  // GEMM: C[m*sCm + n*sCn] = alpha * sum_k A[m*sAm + k*sAk] B[k*sBk + n*sBn] + beta * C
+  int64_t M = 0, N = 0, K = 0, sAm = 0, sAk = 0, sBk = 0, sBn = 0, sCm = 0, sCn = 0;
+  const double* A = nullptr;
+  const double* B = nullptr;
+  double* C = nullptr;
+  double alpha = 0.0, beta = 0.0;
+  // permute: out = alpha * in + beta * out over out's dims; fill: out = alpha
+  int rank = 0;
+  int64_t d[kMaxRank] = {}, si[kMaxRank] = {}, so[kMaxRank] = {};
+  const double* in = nullptr;
+  double* out = nullptr;
+};
+
+struct Recorder {
+  std::vector<RecordedOp> ops;
+  char* arena = nullptr;  // null: sizing pass, the addresses handed out are never used
+  size_t used = 0, peak = 0;
+  struct Block {
+    size_t off, bytes;
+    bool freed;
+  };
+  std::vector<Block> blocks;
+  std::vector<std::string> tape;
+  size_t tape_pos = 0;
+  bool replay_tape = false;
+  void* alloc(size_t bytes);
+  void release(void* p);
+};
+Recorder*& recorder();  // the calling thread's recorder (null: launch normally)
 
 // ----------------------------------------------------------------------------------
 // Kernel launchers (kernels_fp64.cu).  All are asynchronous on ctx.stream.

@@ -9,6 +9,10 @@ namespace ucc {
 // mixed-precision GEMM path (tc_gemm.cu); returns false if it declines the problem
 bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn);
+bool tc_eligible(int64_t M, int64_t N, int64_t K);
+void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
+                      int64_t sAk, const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm,
+                      int64_t sCn);
 
 // ---------------------------------------------------------------------------------------
 Tensor make_view(double* p, const std::vector<int64_t>& dims) {
@@ -55,10 +59,44 @@ DeviceBuffer::~DeviceBuffer() {
 
 Scratch::Scratch(Ctx& c, size_t bytes) : ctx(&c) {
   if (bytes == 0) bytes = 16;
+  if ((rec = recorder()) != nullptr) {
+    p = rec->alloc(bytes);
+    return;
+  }
   UCC_CUDA(cudaMallocAsync(&p, bytes, c.stream));
 }
 Scratch::~Scratch() {
-  if (p) cudaFreeAsync(p, ctx->stream);
+  if (rec)
+    rec->release(p);
+  else if (p)
+    cudaFreeAsync(p, ctx->stream);
+}
+
+Recorder*& recorder() {
+  static thread_local Recorder* r = nullptr;
+  return r;
+}
+
+void* Recorder::alloc(size_t bytes) {
+  bytes = (bytes + 255) / 256 * 256;
+  // sizing pass: offsets from a fixed non-null base; nothing is launched while recording
+  char* base = arena ? arena : reinterpret_cast<char*>(uintptr_t(1) << 44);
+  blocks.push_back({used, bytes, false});
+  void* p = base + used;
+  used += bytes;
+  peak = std::max(peak, used);
+  return p;
+}
+
+void Recorder::release(void* p) {
+  char* base = arena ? arena : reinterpret_cast<char*>(uintptr_t(1) << 44);
+  const size_t off = (size_t)(static_cast<char*>(p) - base);
+  for (auto& b : blocks)
+    if (b.off == off && !b.freed) b.freed = true;
+  while (!blocks.empty() && blocks.back().freed) {
+    used = blocks.back().off;
+    blocks.pop_back();
+  }
 }
 
 Timer::Timer(cudaStream_t s) : st(s) {
@@ -101,6 +139,8 @@ Fp64Scope::Fp64Scope(Ctx& ctx, bool on) : c(ctx), saved(ctx.force_fp64) {
   if (on) c.force_fp64 = true;
 }
 Fp64Scope::~Fp64Scope() { c.force_fp64 = saved; }
+PrecisionScope::PrecisionScope(Ctx& ctx, bool f) : c(ctx), saved(ctx.force_fp64) { c.force_fp64 = f; }
+PrecisionScope::~PrecisionScope() { c.force_fp64 = saved; }
 
 bool Ctx::is_constant(const double* p) const {
   for (const auto& kv : store) {
@@ -123,11 +163,87 @@ Temp::Temp(Ctx& c, const std::vector<int64_t>& dims, bool zero) : buf(c, [&] {
   return n * sizeof(double);
 }()) {
   t = make_view(buf.d(), dims);
-  if (zero) UCC_CUDA(cudaMemsetAsync(buf.p, 0, t.size() * sizeof(double), c.stream));
+  if (zero) {
+    if (buf.rec)
+      fill(c, t.size(), 0.0, buf.d());
+    else
+      UCC_CUDA(cudaMemsetAsync(buf.p, 0, t.size() * sizeof(double), c.stream));
+  }
 }
 
 // ---------------------------------------------------------------------------------------
 namespace {
+
+// GEMMs with at least this many multiply-adds are anchored during refinement; lighter
+// ones simply run in FP64 there
+constexpr double kAnchorMinWork = 5e8;
+
+Tensor matrix_view(const double* p, int64_t rows, int64_t cols, int64_t sr, int64_t sc) {
+  Tensor t;
+  t.p = const_cast<double*>(p);
+  t.rank = 2;
+  t.d[0] = rows;
+  t.d[1] = cols;
+  t.s[0] = sr;
+  t.s[1] = sc;
+  return t;
+}
+
+// C = alpha * A B + beta * C for one GEMM of an anchored refinement sweep
+void anchored_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                   bool a_const, const double* B, int64_t sBk, int64_t sBn, bool b_const, double beta, double* C,
+                   int64_t sCm, int64_t sCn) {
+  auto& an = c.anchors;
+  const Tensor av = matrix_view(A, M, K, sAm, sAk), bv = matrix_view(B, K, N, sBk, sBn);
+  const Tensor cv = matrix_view(C, M, N, sCm, sCn);
+  if (an.mode == 1) {
+    Ctx::AnchorTerm t;
+    t.M = M;
+    t.N = N;
+    t.K = K;
+    t.a_const = a_const;
+    t.b_const = b_const;
+    if (!a_const) {
+      t.a0 = std::make_unique<DeviceBuffer>((size_t)(M * K));
+      permute_add(c, av, 1.0, 0.0, make_view(t.a0->p, {M, K}));
+    }
+    if (!b_const) {
+      t.b0 = std::make_unique<DeviceBuffer>((size_t)(K * N));
+      permute_add(c, bv, 1.0, 0.0, make_view(t.b0->p, {K, N}));
+    }
+    t.p0 = std::make_unique<DeviceBuffer>((size_t)(M * N));
+    GemmEpilogue epi;
+    epi.s_mhi = N;
+    epi.s_n = 1;
+    dgemm_strided(c, M, N, K, 1.0, A, sAm, sAk, B, sBk, sBn, 0.0, t.p0->p, epi, 1, 0, 0, 0, nullptr);
+    permute_add(c, make_view(t.p0->p, {M, N}), alpha, beta, cv);
+    an.terms.push_back(std::move(t));
+    an.next++;
+    return;
+  }
+  UCC_REQUIRE(an.next < an.terms.size(), UCC_BAD_STATE, "anchored refinement: more heavy GEMMs than recorded");
+  const Ctx::AnchorTerm& t = an.terms[an.next++];
+  UCC_REQUIRE(t.M == M && t.N == N && t.K == K && t.a_const == a_const && t.b_const == b_const, UCC_BAD_STATE,
+              "anchored refinement: the GEMM sequence changed since the record sweep");
+  Temp P(c, {M, N});
+  UCC_CUDA(cudaMemcpyAsync(P->p, t.p0->p, sizeof(double) * M * N, cudaMemcpyDeviceToDevice, c.stream));
+  if (!a_const) {  // P += (A - A0) B
+    Temp dA(c, {M, K});
+    permute_add(c, av, 1.0, 0.0, dA);
+    axpby(c, M * K, -1.0, t.a0->p, 1.0, dA->p);
+    tc_gemm_oriented(c, M, N, K, 1.0, dA->p, K, 1, B, sBk, sBn, 1.0, P->p, N, 1);
+  }
+  if (!b_const) {  // P += A0 (B - B0)
+    Temp dB(c, {K, N});
+    permute_add(c, bv, 1.0, 0.0, dB);
+    axpby(c, K * N, -1.0, t.b0->p, 1.0, dB->p);
+    if (a_const)
+      tc_gemm_oriented(c, M, N, K, 1.0, A, sAm, sAk, dB->p, N, 1, 1.0, P->p, N, 1);
+    else
+      tc_gemm_oriented(c, M, N, K, 1.0, t.a0->p, K, 1, dB->p, N, 1, 1.0, P->p, N, 1);
+  }
+  permute_add(c, P, alpha, beta, cv);
+}
 
 struct Parsed {
   std::string a, b, c;
@@ -287,6 +403,20 @@ void contract(Ctx& c, const std::string& spec, double alpha, const Tensor& A, co
         }
       }
 
+  if (Recorder* r = recorder()) {  // every recorded problem follows the first one's choices
+    if (r->replay_tape) {
+      UCC_REQUIRE(r->tape_pos + 3 <= r->tape.size(), UCC_BAD_STATE, "recorded contraction sequence diverged");
+      bm = r->tape[r->tape_pos++];
+      bn = r->tape[r->tape_pos++];
+      bk = r->tape[r->tape_pos++];
+      UCC_REQUIRE(bm.size() == Ms.size() && bn.size() == Ns.size() && bk.size() == Ks.size(), UCC_BAD_STATE,
+                  "recorded contraction sequence diverged at " + spec);
+    } else {
+      r->tape.push_back(bm);
+      r->tape.push_back(bn);
+      r->tape.push_back(bk);
+    }
+  }
   std::unique_ptr<Scratch> hA, hB, hC;
   Tensor a = A, b = B;
   std::string sa = p.a, sb = p.b;
@@ -329,6 +459,12 @@ void contract(Ctx& c, const std::string& spec, double alpha, const Tensor& A, co
     done = true;
   } else if (N == 1) {  // matrix times column vector
     dgemv_strided(c, M, K, ga, b.p, sBk, a.p, sAk, sAm, gb, ct.p, sCm);
+    done = true;
+  }
+  if (!done && c.anchors.mode != 0 && c.opt.precision == UCC_MIXED && (double)M * N * K >= kAnchorMinWork &&
+      tc_eligible(M, N, K)) {
+    anchored_gemm(c, M, N, K, ga, a.p, sAm, sAk, c.is_constant(A.p), b.p, sBk, sBn, c.is_constant(B.p), gb, ct.p,
+                  sCm, sCn);
     done = true;
   }
   if (!done && c.opt.precision == UCC_MIXED && !c.force_fp64)

@@ -154,10 +154,22 @@ __global__ void splitk_reduce_kernel(int64_t M, int64_t N, int nsplit, const dou
 }
 }  // namespace
 
+void splitk_reduce(Ctx& c, int64_t M, int64_t N, int nsplit, const double* P, double alpha, double beta, double* C,
+                   const GemmEpilogue& epi);
+
 void dgemm_strided(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                    const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi,
                    int batch, int64_t bA, int64_t bB, int64_t bC, const GemmPtrs* ptrs) {
   if (M <= 0 || N <= 0 || batch <= 0) return;
+  if (Recorder* r = recorder()) {
+    UCC_REQUIRE(batch == 1 && !ptrs && epi.msplit == 0, UCC_UNSUPPORTED, "dgemm: form not recordable");
+    RecordedOp o;
+    o.kind = RecordedOp::kGemm;
+    o.M = M, o.N = N, o.K = K, o.sAm = sAm, o.sAk = sAk, o.sBk = sBk, o.sBn = sBn, o.sCm = epi.s_mhi, o.sCn = epi.s_n;
+    o.A = A, o.B = B, o.C = C, o.alpha = alpha, o.beta = beta;
+    r->ops.push_back(o);
+    return;
+  }
   UCC_REQUIRE(batch <= 65535, UCC_BAD_ARGS, "dgemm: batch too large");
   GemmArgs g{M, N, K, 0, alpha, beta, A, sAm, sAk, bA, B, sBk, sBn, bB, C, bC, epi, ptrs};
   dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM), (unsigned)batch);
@@ -190,13 +202,16 @@ void dgemm_strided(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const 
     dgemm_kernel<false, false><<<grid, GT, 0, c.stream>>>(g);
   count_launch();
   check_launch("dgemm");
-  if (part) {
-    const int64_t MN = M * N;
-    const unsigned blocks = (unsigned)std::min<int64_t>((MN + 255) / 256, 152 * 16);
-    splitk_reduce_kernel<<<blocks, 256, 0, c.stream>>>(M, N, nsplit, part->d(), alpha, beta, C, epi);
-    count_launch();
-    check_launch("dgemm split-K reduce");
-  }
+  if (part) splitk_reduce(c, M, N, nsplit, part->d(), alpha, beta, C, epi);
+}
+
+void splitk_reduce(Ctx& c, int64_t M, int64_t N, int nsplit, const double* P, double alpha, double beta, double* C,
+                   const GemmEpilogue& epi) {
+  const int64_t MN = M * N;
+  const unsigned blocks = (unsigned)std::min<int64_t>((MN + 255) / 256, 152 * 16);
+  splitk_reduce_kernel<<<blocks, 256, 0, c.stream>>>(M, N, nsplit, P, alpha, beta, C, epi);
+  count_launch();
+  check_launch("split-K reduce");
 }
 
 void dgemm(Ctx& c, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
@@ -283,6 +298,20 @@ __global__ void permute_kernel_tile(TileArgs t) {
 
 void permute_add(Ctx& c, const Tensor& in, double alpha, double beta, const Tensor& out) {
   UCC_REQUIRE(in.rank == out.rank, UCC_BAD_ARGS, "permute_add: rank mismatch");
+  if (Recorder* r = recorder()) {
+    RecordedOp o;
+    o.kind = RecordedOp::kPermute;
+    o.rank = out.rank;
+    for (int k = 0; k < out.rank; k++) {
+      UCC_REQUIRE(in.d[k] == out.d[k], UCC_BAD_ARGS, "permute_add: dim mismatch");
+      o.d[k] = out.d[k];
+      o.si[k] = in.s[k];
+      o.so[k] = out.s[k];
+    }
+    o.in = in.p, o.out = out.p, o.alpha = alpha, o.beta = beta;
+    if (out.size() > 0) r->ops.push_back(o);
+    return;
+  }
   PermArgs a{};
   a.rank = out.rank;
   a.total = out.size();
@@ -349,8 +378,21 @@ unsigned grid_for(int64_t n, int threads = 256) {
 }
 }  // namespace
 
+static void record_flat(Recorder* r, RecordedOp::Kind kind, int64_t n, double alpha, const double* x, double beta,
+                        double* y) {
+  RecordedOp o;
+  o.kind = kind;
+  o.rank = 1;
+  o.d[0] = n;
+  o.si[0] = 1;
+  o.so[0] = 1;
+  o.in = x, o.out = y, o.alpha = alpha, o.beta = beta;
+  r->ops.push_back(o);
+}
+
 void axpby(Ctx& c, int64_t n, double alpha, const double* x, double beta, double* y) {
   if (n <= 0) return;
+  if (Recorder* r = recorder()) return record_flat(r, RecordedOp::kPermute, n, alpha, x, beta, y);
   axpby_kernel<<<grid_for(n), 256, 0, c.stream>>>(n, alpha, x, beta, y);
   count_launch();
   check_launch("axpby");
@@ -358,6 +400,7 @@ void axpby(Ctx& c, int64_t n, double alpha, const double* x, double beta, double
 
 void fill(Ctx& c, int64_t n, double v, double* y) {
   if (n <= 0) return;
+  if (Recorder* r = recorder()) return record_flat(r, RecordedOp::kFill, n, v, nullptr, 0.0, y);
   fill_kernel<<<grid_for(n), 256, 0, c.stream>>>(n, v, y);
   count_launch();
   check_launch("fill");
@@ -414,6 +457,7 @@ __global__ void sum_pass2(int nparts, const double* partial, double* out) {
 }  // namespace
 
 void dot_async(Ctx& c, int64_t n, const double* x, const double* y, double* d_out) {
+  UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
   Scratch part(c, sizeof(double) * RED_BLOCKS);
   dot_pass1<<<dim3(RED_BLOCKS, 1), RED_THREADS, 0, c.stream>>>(n, nullptr, x, y, part.d());
   sum_pass2<<<1, RED_THREADS, 0, c.stream>>>(RED_BLOCKS, part.d(), d_out);
@@ -432,6 +476,7 @@ double dot(Ctx& c, int64_t n, const double* x, const double* y) {
 }
 
 void multidot_async(Ctx& c, int nvec, const double* const* d_xs, const double* y, int64_t n, double* d_out) {
+  UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
   if (nvec <= 0) return;
   Scratch part(c, sizeof(double) * RED_BLOCKS * nvec);
   dot_pass1<<<dim3(RED_BLOCKS, nvec), RED_THREADS, 0, c.stream>>>(n, d_xs, nullptr, y, part.d());
@@ -504,6 +549,7 @@ __global__ void lincomb_kernel(int nvec, const double* const* vecs, const double
 
 void build_tau(Ctx& c, int no, int nv, const double* t1, const double* t2, double f1, double* tau, double f2,
                double* ttau) {
+  UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
   const int64_t n = (int64_t)no * no * nv * nv;
   tau_kernel<<<grid_for(n), 256, 0, c.stream>>>(no, nv, t1, t2, f1, tau, f2, ttau);
   count_launch();
@@ -513,6 +559,7 @@ void build_tau(Ctx& c, int no, int nv, const double* t1, const double* t2, doubl
 void jacobi_update(Ctx& c, int no, int nv, const double* d_do, const double* d_dv, double shift, const double* R1,
                    const double* R2, const double* t1old, const double* t2old, double* t1new, double* t2new,
                    double* d_sumsq) {
+  UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
   Scratch part(c, sizeof(double) * RED_BLOCKS);
   jacobi_kernel<<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(no, nv, d_do, d_dv, shift, R1, R2, t1old, t2old, t1new,
                                                           t2new, part.d());
@@ -523,6 +570,7 @@ void jacobi_update(Ctx& c, int no, int nv, const double* d_do, const double* d_d
 }
 
 void lincomb(Ctx& c, int nvec, const double* const* d_vecs, const double* coef, int64_t n, double* out) {
+  UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
   Scratch dc(c, sizeof(double) * nvec);
   UCC_CUDA(cudaMemcpyAsync(dc.p, coef, sizeof(double) * nvec, cudaMemcpyHostToDevice, c.stream));
   lincomb_kernel<<<grid_for(n), 256, 0, c.stream>>>(nvec, d_vecs, dc.d(), n, out);
@@ -631,6 +679,14 @@ __global__ void gemv_kcontig(int64_t N, int64_t K, double alpha, const double* x
 void dgemv_strided(Ctx& c, int64_t N, int64_t K, double alpha, const double* x, int64_t sx, const double* A,
                    int64_t sk, int64_t sn, double beta, double* y, int64_t sy) {
   if (N <= 0) return;
+  if (Recorder* r = recorder()) {  // a GEMM with one row
+    RecordedOp o;
+    o.kind = RecordedOp::kGemm;
+    o.M = 1, o.N = N, o.K = K, o.sAm = 0, o.sAk = sx, o.sBk = sk, o.sBn = sn, o.sCm = 0, o.sCn = sy;
+    o.A = x, o.B = A, o.C = y, o.alpha = alpha, o.beta = beta;
+    r->ops.push_back(o);
+    return;
+  }
   if (sk == 1 && sn != 1) {
     const int wpb = 8;
     gemv_kcontig<<<(unsigned)((N + wpb - 1) / wpb), 32 * wpb, 0, c.stream>>>(N, K, alpha, x, sx, A, sk, sn, beta, y,

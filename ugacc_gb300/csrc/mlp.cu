@@ -1,0 +1,572 @@
+// Learned T2 starting amplitudes: a small MLP trained on converged amplitudes.
+//
+// For every doubles element (i,j,a,b) of a Hamiltonian the network maps MP2-level pair
+// features to the difference between the converged CCSD amplitude and the MP2 guess
+// (ccwfn.cc:75-87 gives the MP2 guess t2 = <ij|ab>/D).  The plain CCSD iteration then
+// starts from t2 = t2_mp2 + prediction; its own convergence test decides the answer.
+//
+//   features (kFeat = 8), D = e_i + e_j - e_a - e_b:
+//     0: S*<ij|ab>/D   1: S*<ij|ba>/D   2: S*<ij|ab>   3: -1/D
+//     4: (e_i+e_j)/2   5: (e_a+e_b)/2   6: [i==j]      7: [a==b]
+//   target: S*(t2_ccsd - t2_mp2),   S = kScale
+//   network: 8 -> 256 -> 256 -> 1, SiLU; weights stored in FP16 for the forward and
+//   backward passes, FP32 master copies for the Adam update, FP32 accumulation.
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <random>
+#include <vector>
+
+#include "cc.h"
+
+namespace ucc {
+void count_kernel_launch();
+Ctx& ctx_of(ucc_ctx* h);               // capi.cpp
+void mlp_guess(Ctx& c, ucc_mlp* net);  // t2 guess of the network into the context's T_guess
+
+namespace mlp {
+
+constexpr int kFeat = 8, kHid = 256;
+constexpr double kScale = 100.0;
+
+__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float dsilu(float z) {
+  const float s = 1.0f / (1.0f + __expf(-z));
+  return s * (1.0f + z * (1.0f - s));
+}
+
+template <typename T>
+__device__ __forceinline__ float ld(const T* p, int64_t i);
+template <>
+__device__ __forceinline__ float ld<float>(const float* p, int64_t i) {
+  return p[i];
+}
+template <>
+__device__ __forceinline__ float ld<__half>(const __half* p, int64_t i) {
+  return __half2float(p[i]);
+}
+
+// C[m][n] (+)= sum_k A[m*sAm + k*sAk] * B[k*sBk + n*sBn]; 64x64 tiles, 4x4 per thread,
+// FP32 accumulation, B in FP32 or FP16
+template <typename TB>
+__global__ void __launch_bounds__(256) gemm_f32(int M, int N, int K, const float* A, int64_t sAm, int64_t sAk,
+                                                const TB* B, int64_t sBk, int64_t sBn, float* C, int64_t ldc,
+                                                int accumulate) {
+  __shared__ float As[16][65];
+  __shared__ float Bs[16][65];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    for (int e = threadIdx.x; e < 64 * 16; e += 256) {
+      const int mm = e % 64, kk = e / 64;
+      const int m = m0 + mm, k = k0 + kk;
+      As[kk][mm] = (m < M && k < K) ? A[(int64_t)m * sAm + (int64_t)k * sAk] : 0.f;
+      const int n = n0 + mm;
+      Bs[kk][mm] = (n < N && k < K) ? ld<TB>(B, (int64_t)k * sBk + (int64_t)n * sBn) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; kk++) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int m = m0 + ty + 16 * i;
+    if (m >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int n = n0 + tx + 16 * j;
+      if (n >= N) continue;
+      float* c = C + (int64_t)m * ldc + n;
+      *c = accumulate ? *c + acc[i][j] : acc[i][j];
+    }
+  }
+}
+
+// Z += bias (per column); A = silu(Z)
+__global__ void bias_act(int64_t n, int h, float* Z, const float* b, float* A) {
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n * h; x += (int64_t)gridDim.x * blockDim.x) {
+    const float z = Z[x] + b[x % h];
+    Z[x] = z;
+    if (A) A[x] = silu(z);
+  }
+}
+// y = y + b3 (scalar)
+__global__ void add_scalar(int64_t n, float* y, const float* b) {
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
+    y[x] += b[0];
+}
+// dy = 2 (y - t) / n ; loss partial sums
+__global__ void mse_grad(int64_t n, const float* y, const float* t, float* dy, float* loss_part) {
+  float s = 0.f;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    const float d = y[x] - t[x];
+    dy[x] = 2.f * d / (float)n;
+    s += d * d;
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (threadIdx.x % 32 == 0) atomicAdd(loss_part, s / (float)n);
+}
+// dA (in) -> dZ = dA * silu'(Z), in place
+__global__ void act_grad(int64_t n, const float* Z, float* dA) {
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
+    dA[x] *= dsilu(Z[x]);
+}
+// column sums of an n x h matrix (bias gradients), one thread per column
+__global__ void col_sum(int64_t n, int h, const float* X, float* out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= h) return;
+  float s = 0.f;
+  for (int64_t r = 0; r < n; r++) s += X[r * h + j];
+  out[j] = s;
+}
+// Adam on FP32 masters, then the FP16 working copy
+__global__ void adam(int64_t n, float* w, const float* g, float* m, float* v, __half* wh, float lr, float b1, float b2,
+                     float c1, float c2) {
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    const float gi = g[x];
+    const float mi = b1 * m[x] + (1.f - b1) * gi;
+    const float vi = b2 * v[x] + (1.f - b2) * gi * gi;
+    m[x] = mi;
+    v[x] = vi;
+    const float wi = w[x] - lr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
+    w[x] = wi;
+    if (wh) wh[x] = __float2half(wi);
+  }
+}
+__global__ void to_half(int64_t n, const float* w, __half* wh) {
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
+    wh[x] = __float2half(w[x]);
+}
+// gather rows idx[r] of X (n x f) and t
+__global__ void gather_rows(int64_t nb, int f, const int64_t* idx, const float* X, const float* t, float* Xb,
+                            float* tb) {
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < nb * f; x += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = x / f, c = x % f;
+    Xb[x] = X[idx[r] * f + c];
+    if (c == 0) tb[r] = t[idx[r]];
+  }
+}
+
+// features of every (i,j,a,b) of the loaded Hamiltonian
+__global__ void features_kernel(int no, int nv, const double* Voovv, const double* eps, float* X) {
+  const int64_t n = (int64_t)no * no * nv * nv;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(x % nv);
+    int64_t r = x / nv;
+    const int a = (int)(r % nv);
+    r /= nv;
+    const int j = (int)(r % no), i = (int)(r / no);
+    const double D = ((eps[i] + eps[j]) - eps[no + a]) - eps[no + b];
+    const double v = Voovv[x];
+    const double vx = Voovv[(((int64_t)i * no + j) * nv + b) * nv + a];
+    float* f = X + x * kFeat;
+    f[0] = (float)(kScale * v / D);
+    f[1] = (float)(kScale * vx / D);
+    f[2] = (float)(kScale * v);
+    f[3] = (float)(-1.0 / D);
+    f[4] = (float)(0.5 * (eps[i] + eps[j]));
+    f[5] = (float)(0.5 * (eps[no + a] + eps[no + b]));
+    f[6] = i == j ? 1.f : 0.f;
+    f[7] = a == b ? 1.f : 0.f;
+  }
+}
+// target = S * (t2 - t2_mp2)
+__global__ void targets_kernel(int no, int nv, const double* Voovv, const double* eps, const double* t2, float* y) {
+  const int64_t n = (int64_t)no * no * nv * nv;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(x % nv);
+    int64_t r = x / nv;
+    const int a = (int)(r % nv);
+    r /= nv;
+    const int j = (int)(r % no), i = (int)(r / no);
+    const double D = ((eps[i] + eps[j]) - eps[no + a]) - eps[no + b];
+    y[x] = (float)(kScale * (t2[x] - Voovv[x] / D));
+  }
+}
+// t2 = t2_mp2 + prediction / S, written into the packed guess buffer (t1 = f_ia / D1)
+__global__ void guess_kernel(int no, int nv, const double* Voovv, const double* eps, const float* pred, double* t2) {
+  const int64_t n = (int64_t)no * no * nv * nv;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(x % nv);
+    int64_t r = x / nv;
+    const int a = (int)(r % nv);
+    r /= nv;
+    const int j = (int)(r % no), i = (int)(r / no);
+    const double D = ((eps[i] + eps[j]) - eps[no + a]) - eps[no + b];
+    t2[x] = Voovv[x] / D + (double)pred[x] / kScale;
+  }
+}
+
+unsigned grid1(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
+
+}  // namespace mlp
+}  // namespace ucc
+
+using namespace ucc;
+using namespace ucc::mlp;
+
+struct ucc_mlp {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  // FP32 masters, Adam moments, FP16 copies: W1 [8][256], b1 [256], W2 [256][256], b2, w3 [256], b3 [1]
+  int64_t nparam = 0;
+  float* w = nullptr;  // all parameters, contiguous
+  float* g = nullptr;
+  float* m = nullptr;
+  float* v = nullptr;
+  __half* wh = nullptr;
+  int64_t adam_t = 0;
+  int64_t cap = 0;   // activation buffers sized for this many rows
+  int64_t ycap = 0;  // output / output-gradient buffers
+  float *Z1 = nullptr, *A1 = nullptr, *Z2 = nullptr, *A2 = nullptr, *y = nullptr, *dy = nullptr, *loss = nullptr;
+  int64_t oW1() const { return 0; }
+  int64_t ob1() const { return (int64_t)kFeat * kHid; }
+  int64_t oW2() const { return ob1() + kHid; }
+  int64_t ob2() const { return oW2() + (int64_t)kHid * kHid; }
+  int64_t ow3() const { return ob2() + kHid; }
+  int64_t ob3() const { return ow3() + kHid; }
+  ~ucc_mlp() {
+    for (void* p : {(void*)w, (void*)g, (void*)m, (void*)v, (void*)wh, (void*)Z1, (void*)A1, (void*)Z2, (void*)A2,
+                    (void*)y, (void*)dy, (void*)loss})
+      if (p) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+template <typename F>
+ucc_status mguard(ucc_mlp* n, F&& f) {
+  if (!n) return UCC_BAD_ARGS;
+  n->last_error.clear();
+  try {
+    UCC_CUDA(cudaSetDevice(n->device));
+    f(*n);
+    return UCC_OK;
+  } catch (const Error& e) {
+    n->last_error = e.what();
+    return e.status;
+  } catch (const std::exception& e) {
+    n->last_error = e.what();
+    return UCC_CUDA_ERROR;
+  }
+}
+
+constexpr int64_t kChunk = 1 << 20;  // rows per forward pass (activation buffers)
+
+void ensure_rows(ucc_mlp& n, int64_t rows) {
+  const int64_t act = std::min(rows, kChunk);
+  if (act > n.cap) {
+    for (float** p : {&n.Z1, &n.A1, &n.Z2, &n.A2}) {
+      if (*p) cudaFree(*p);
+      UCC_CUDA(cudaMalloc(p, sizeof(float) * act * kHid));
+    }
+    n.cap = act;
+  }
+  if (rows > n.ycap) {
+    for (float** p : {&n.y, &n.dy}) {
+      if (*p) cudaFree(*p);
+      UCC_CUDA(cudaMalloc(p, sizeof(float) * rows));
+    }
+    n.ycap = rows;
+  }
+}
+
+template <typename TB>
+void gemm(ucc_mlp& n, int M, int N, int K, const float* A, int64_t sAm, int64_t sAk, const TB* B, int64_t sBk,
+          int64_t sBn, float* C, int64_t ldc, bool acc) {
+  dim3 grid((N + 63) / 64, (M + 63) / 64);
+  gemm_f32<TB><<<grid, 256, 0, n.stream>>>(M, N, K, A, sAm, sAk, B, sBk, sBn, C, ldc, acc ? 1 : 0);
+  count_kernel_launch();
+  UCC_CUDA(cudaGetLastError());
+}
+
+// forward pass for rows X[rows][8] -> n.y (chunks of kChunk rows through the activations)
+void forward(ucc_mlp& n, const float* X, int64_t rows) {
+  const __half* W1 = n.wh + n.oW1();
+  const __half* W2 = n.wh + n.oW2();
+  const __half* w3 = n.wh + n.ow3();
+  for (int64_t r0 = 0; r0 < rows; r0 += kChunk) {
+    const int64_t len = std::min(kChunk, rows - r0);
+    const float* Xc = X + r0 * kFeat;
+    float* yc = n.y + r0;
+    gemm(n, (int)len, kHid, kFeat, Xc, kFeat, 1, W1, kHid, 1, n.Z1, kHid, false);
+    bias_act<<<grid1(len * kHid), 256, 0, n.stream>>>(len, kHid, n.Z1, n.w + n.ob1(), n.A1);
+    gemm(n, (int)len, kHid, kHid, n.A1, kHid, 1, W2, kHid, 1, n.Z2, kHid, false);
+    bias_act<<<grid1(len * kHid), 256, 0, n.stream>>>(len, kHid, n.Z2, n.w + n.ob2(), n.A2);
+    gemm(n, (int)len, 1, kHid, n.A2, kHid, 1, w3, 1, 1, yc, 1, false);
+    add_scalar<<<grid1(len), 256, 0, n.stream>>>(len, yc, n.w + n.ob3());
+    for (int k = 0; k < 3; k++) count_kernel_launch();
+    UCC_CUDA(cudaGetLastError());
+  }
+}
+
+// loss and gradients (into n.g) for rows X, targets t; returns mean squared error
+float backward(ucc_mlp& n, const float* X, const float* t, int64_t rows) {
+  UCC_REQUIRE(rows <= kChunk, UCC_BAD_ARGS, "training batch larger than the activation chunk");
+  forward(n, X, rows);
+  UCC_CUDA(cudaMemsetAsync(n.loss, 0, sizeof(float), n.stream));
+  mse_grad<<<grid1(rows), 256, 0, n.stream>>>(rows, n.y, t, n.dy, n.loss);
+  float* g = n.g;
+  // w3, b3
+  gemm(n, kHid, 1, (int)rows, n.A2, 1, kHid, n.dy, 1, 1, g + n.ow3(), 1, false);
+  col_sum<<<1, 32, 0, n.stream>>>(rows, 1, n.dy, g + n.ob3());
+  // dA2 = dy w3^T -> dZ2 (reuse A2 as dZ2 after its use above)
+  gemm(n, (int)rows, kHid, 1, n.dy, 1, 1, n.wh + n.ow3(), 1, 1, n.A2, kHid, false);
+  act_grad<<<grid1(rows * kHid), 256, 0, n.stream>>>(rows * kHid, n.Z2, n.A2);
+  // W2, b2
+  gemm(n, kHid, kHid, (int)rows, n.A1, 1, kHid, n.A2, kHid, 1, g + n.oW2(), kHid, false);
+  col_sum<<<(kHid + 127) / 128, 128, 0, n.stream>>>(rows, kHid, n.A2, g + n.ob2());
+  // dA1 = dZ2 W2^T -> dZ1 (into A1)
+  gemm(n, (int)rows, kHid, kHid, n.A2, kHid, 1, n.wh + n.oW2(), 1, kHid, n.A1, kHid, false);
+  act_grad<<<grid1(rows * kHid), 256, 0, n.stream>>>(rows * kHid, n.Z1, n.A1);
+  // W1, b1
+  gemm(n, kFeat, kHid, (int)rows, X, 1, kFeat, n.A1, kHid, 1, g + n.oW1(), kHid, false);
+  col_sum<<<(kHid + 127) / 128, 128, 0, n.stream>>>(rows, kHid, n.A1, g + n.ob1());
+  for (int k = 0; k < 6; k++) count_kernel_launch();
+  UCC_CUDA(cudaGetLastError());
+  float loss = 0.f;
+  UCC_CUDA(cudaMemcpyAsync(&loss, n.loss, sizeof(float), cudaMemcpyDeviceToHost, n.stream));
+  UCC_CUDA(cudaStreamSynchronize(n.stream));
+  return loss;
+}
+}  // namespace
+
+extern "C" {
+
+ucc_status ucc_mlp_create(ucc_mlp** out, int device, uint64_t seed) {
+  if (!out) return UCC_BAD_ARGS;
+  *out = nullptr;
+  int nd = 0;
+  if (cudaGetDeviceCount(&nd) != cudaSuccess || device < 0 || device >= nd) return UCC_CUDA_ERROR;
+  ucc_mlp* n = new (std::nothrow) ucc_mlp;
+  if (!n) return UCC_OUT_OF_MEMORY;
+  n->device = device;
+  ucc_status st = mguard(n, [&](ucc_mlp& m) {
+    UCC_CUDA(cudaStreamCreateWithFlags(&m.stream, cudaStreamNonBlocking));
+    m.nparam = m.ob3() + 1;
+    UCC_CUDA(cudaMalloc(&m.w, sizeof(float) * m.nparam));
+    UCC_CUDA(cudaMalloc(&m.g, sizeof(float) * m.nparam));
+    UCC_CUDA(cudaMalloc(&m.m, sizeof(float) * m.nparam));
+    UCC_CUDA(cudaMalloc(&m.v, sizeof(float) * m.nparam));
+    UCC_CUDA(cudaMalloc(&m.wh, sizeof(__half) * m.nparam));
+    UCC_CUDA(cudaMalloc(&m.loss, sizeof(float)));
+    UCC_CUDA(cudaMemset(m.m, 0, sizeof(float) * m.nparam));
+    UCC_CUDA(cudaMemset(m.v, 0, sizeof(float) * m.nparam));
+    // He-style initialisation, deterministic in the seed
+    std::vector<float> h(m.nparam, 0.f);
+    std::mt19937_64 rng(seed);
+    std::normal_distribution<float> nd1(0.f, std::sqrt(2.f / kFeat)), nd2(0.f, std::sqrt(2.f / kHid));
+    for (int64_t k = m.oW1(); k < m.ob1(); k++) h[k] = nd1(rng);
+    for (int64_t k = m.oW2(); k < m.ob2(); k++) h[k] = nd2(rng);
+    for (int64_t k = m.ow3(); k < m.ob3(); k++) h[k] = 0.1f * nd2(rng);
+    UCC_CUDA(cudaMemcpy(m.w, h.data(), sizeof(float) * m.nparam, cudaMemcpyHostToDevice));
+    to_half<<<grid1(m.nparam), 256, 0, m.stream>>>(m.nparam, m.w, m.wh);
+    count_kernel_launch();
+    UCC_CUDA(cudaStreamSynchronize(m.stream));
+  });
+  if (st != UCC_OK) {
+    delete n;
+    return st;
+  }
+  *out = n;
+  return UCC_OK;
+}
+
+ucc_status ucc_mlp_destroy(ucc_mlp* n) {
+  if (!n) return UCC_BAD_ARGS;
+  cudaSetDevice(n->device);
+  delete n;
+  return UCC_OK;
+}
+
+const char* ucc_mlp_last_error(ucc_mlp* n) { return n ? n->last_error.c_str() : "null network"; }
+
+int ucc_mlp_num_params(void) {
+  return kFeat * kHid + kHid + kHid * kHid + kHid + kHid + 1;
+}
+
+ucc_status ucc_mlp_get_params(ucc_mlp* n, float* out, size_t count) {
+  return mguard(n, [&](ucc_mlp& m) {
+    UCC_REQUIRE(out && (int64_t)count == m.nparam, UCC_BAD_ARGS, "parameter count mismatch");
+    UCC_CUDA(cudaMemcpy(out, m.w, sizeof(float) * count, cudaMemcpyDeviceToHost));
+  });
+}
+
+ucc_status ucc_mlp_set_params(ucc_mlp* n, const float* in, size_t count) {
+  return mguard(n, [&](ucc_mlp& m) {
+    UCC_REQUIRE(in && (int64_t)count == m.nparam, UCC_BAD_ARGS, "parameter count mismatch");
+    UCC_CUDA(cudaMemcpy(m.w, in, sizeof(float) * count, cudaMemcpyHostToDevice));
+    to_half<<<grid1(m.nparam), 256, 0, m.stream>>>(m.nparam, m.w, m.wh);
+    count_kernel_launch();
+    UCC_CUDA(cudaStreamSynchronize(m.stream));
+  });
+}
+
+ucc_status ucc_mlp_predict(ucc_mlp* n, const float* X, int64_t rows, float* y) {
+  return mguard(n, [&](ucc_mlp& m) {
+    UCC_REQUIRE(X && y && rows >= 1, UCC_BAD_ARGS, "bad arguments");
+    ensure_rows(m, rows);
+    float* dX = nullptr;
+    UCC_CUDA(cudaMallocAsync(&dX, sizeof(float) * rows * kFeat, m.stream));
+    UCC_CUDA(cudaMemcpyAsync(dX, X, sizeof(float) * rows * kFeat, cudaMemcpyHostToDevice, m.stream));
+    forward(m, dX, rows);
+    UCC_CUDA(cudaMemcpyAsync(y, m.y, sizeof(float) * rows, cudaMemcpyDeviceToHost, m.stream));
+    UCC_CUDA(cudaFreeAsync(dX, m.stream));
+    UCC_CUDA(cudaStreamSynchronize(m.stream));
+  });
+}
+
+ucc_status ucc_mlp_loss_grad(ucc_mlp* n, const float* X, const float* t, int64_t rows, float* loss, float* grad,
+                             size_t count) {
+  return mguard(n, [&](ucc_mlp& m) {
+    UCC_REQUIRE(X && t && loss && rows >= 1, UCC_BAD_ARGS, "bad arguments");
+    UCC_REQUIRE(!grad || (int64_t)count == m.nparam, UCC_BAD_ARGS, "gradient count mismatch");
+    ensure_rows(m, rows);
+    float *dX = nullptr, *dt = nullptr;
+    UCC_CUDA(cudaMallocAsync(&dX, sizeof(float) * rows * kFeat, m.stream));
+    UCC_CUDA(cudaMallocAsync(&dt, sizeof(float) * rows, m.stream));
+    UCC_CUDA(cudaMemcpyAsync(dX, X, sizeof(float) * rows * kFeat, cudaMemcpyHostToDevice, m.stream));
+    UCC_CUDA(cudaMemcpyAsync(dt, t, sizeof(float) * rows, cudaMemcpyHostToDevice, m.stream));
+    *loss = backward(m, dX, dt, rows);
+    if (grad) UCC_CUDA(cudaMemcpy(grad, m.g, sizeof(float) * count, cudaMemcpyDeviceToHost));
+    UCC_CUDA(cudaFreeAsync(dX, m.stream));
+    UCC_CUDA(cudaFreeAsync(dt, m.stream));
+    UCC_CUDA(cudaStreamSynchronize(m.stream));
+  });
+}
+
+ucc_status ucc_mlp_train(ucc_mlp* n, const float* X, const float* t, int64_t rows, int epochs, int batch, float lr,
+                         uint64_t seed, float* final_loss) {
+  return mguard(n, [&](ucc_mlp& m) {
+    UCC_REQUIRE(X && t && rows >= 1 && epochs >= 1 && batch >= 1 && lr > 0, UCC_BAD_ARGS, "bad arguments");
+    const int64_t nb = std::min<int64_t>(batch, rows);
+    ensure_rows(m, nb);
+    float *dX = nullptr, *dt = nullptr, *Xb = nullptr, *tb = nullptr;
+    int64_t* didx = nullptr;
+    UCC_CUDA(cudaMallocAsync(&dX, sizeof(float) * rows * kFeat, m.stream));
+    UCC_CUDA(cudaMallocAsync(&dt, sizeof(float) * rows, m.stream));
+    UCC_CUDA(cudaMallocAsync(&Xb, sizeof(float) * nb * kFeat, m.stream));
+    UCC_CUDA(cudaMallocAsync(&tb, sizeof(float) * nb, m.stream));
+    UCC_CUDA(cudaMallocAsync(&didx, sizeof(int64_t) * rows, m.stream));
+    UCC_CUDA(cudaMemcpyAsync(dX, X, sizeof(float) * rows * kFeat, cudaMemcpyHostToDevice, m.stream));
+    UCC_CUDA(cudaMemcpyAsync(dt, t, sizeof(float) * rows, cudaMemcpyHostToDevice, m.stream));
+    std::vector<int64_t> idx(rows);
+    for (int64_t k = 0; k < rows; k++) idx[k] = k;
+    std::mt19937_64 rng(seed);
+    const float b1 = 0.9f, b2 = 0.999f;
+    double epoch_loss = 0.0;
+    for (int ep = 0; ep < epochs; ep++) {
+      std::shuffle(idx.begin(), idx.end(), rng);
+      UCC_CUDA(cudaMemcpyAsync(didx, idx.data(), sizeof(int64_t) * rows, cudaMemcpyHostToDevice, m.stream));
+      UCC_CUDA(cudaStreamSynchronize(m.stream));
+      epoch_loss = 0.0;
+      int64_t steps = 0;
+      for (int64_t s = 0; s + nb <= rows; s += nb, steps++) {
+        gather_rows<<<grid1(nb * kFeat), 256, 0, m.stream>>>(nb, kFeat, didx + s, dX, dt, Xb, tb);
+        count_kernel_launch();
+        epoch_loss += backward(m, Xb, tb, nb);
+        m.adam_t++;
+        const float c1 = 1.f - std::pow(b1, (float)m.adam_t), c2 = 1.f - std::pow(b2, (float)m.adam_t);
+        adam<<<grid1(m.nparam), 256, 0, m.stream>>>(m.nparam, m.w, m.g, m.m, m.v, m.wh, lr, b1, b2, c1, c2);
+        count_kernel_launch();
+      }
+      if (steps) epoch_loss /= (double)steps;
+    }
+    UCC_CUDA(cudaStreamSynchronize(m.stream));
+    for (void* p : {(void*)dX, (void*)dt, (void*)Xb, (void*)tb, (void*)didx}) UCC_CUDA(cudaFreeAsync(p, m.stream));
+    UCC_CUDA(cudaStreamSynchronize(m.stream));
+    if (final_loss) *final_loss = (float)epoch_loss;
+  });
+}
+
+// features / targets of the Hamiltonian loaded in ctx (targets need converged CCSD)
+ucc_status ucc_mlp_features(ucc_ctx* ctx, float* out, size_t rows, int with_targets, float* targets) {
+  if (!ctx || !out) return UCC_BAD_ARGS;
+  Ctx& c = ctx_of(ctx);
+  try {
+    UCC_CUDA(cudaSetDevice(c.device));
+    UCC_REQUIRE(c.loaded, UCC_BAD_STATE, "no Hamiltonian loaded");
+    const int64_t n = (int64_t)c.no * c.no * c.nv * c.nv;
+    UCC_REQUIRE((int64_t)rows == n, UCC_BAD_ARGS, "rows must be no*no*nv*nv");
+    Scratch X(c, sizeof(float) * n * kFeat);
+    features_kernel<<<grid1(n), 256, 0, c.stream>>>(c.no, c.nv, c.get("Voovv").p, c.get("eps").p,
+                                                    static_cast<float*>(X.p));
+    count_kernel_launch();
+    UCC_CUDA(cudaMemcpyAsync(out, X.p, sizeof(float) * n * kFeat, cudaMemcpyDeviceToHost, c.stream));
+    if (with_targets) {
+      UCC_REQUIRE(targets && c.have_ccsd, UCC_BAD_STATE, "targets need converged CCSD amplitudes");
+      Scratch y(c, sizeof(float) * n);
+      targets_kernel<<<grid1(n), 256, 0, c.stream>>>(c.no, c.nv, c.get("Voovv").p, c.get("eps").p,
+                                                     amp2(c, c.get("T").p).p, static_cast<float*>(y.p));
+      count_kernel_launch();
+      UCC_CUDA(cudaMemcpyAsync(targets, y.p, sizeof(float) * n, cudaMemcpyDeviceToHost, c.stream));
+      UCC_CUDA(cudaStreamSynchronize(c.stream));
+    }
+    UCC_CUDA(cudaStreamSynchronize(c.stream));
+    return UCC_OK;
+  } catch (const Error& e) {
+    c.last_error = e.what();
+    return e.status;
+  }
+}
+
+// next ucc_ccsd starts from t1 = f_ia/D1 and t2 = t2_mp2 + network prediction
+ucc_status ucc_mlp_guess(ucc_ctx* ctx, ucc_mlp* net) {
+  if (!ctx || !net) return UCC_BAD_ARGS;
+  Ctx& c = ctx_of(ctx);
+  try {
+    UCC_CUDA(cudaSetDevice(c.device));
+    mlp_guess(c, net);
+    return UCC_OK;
+  } catch (const Error& e) {
+    c.last_error = e.what();
+    return e.status;
+  }
+}
+
+}  // extern "C"
+
+namespace ucc {
+void mlp_guess(Ctx& c, ucc_mlp* net) {
+  {
+    UCC_REQUIRE(c.loaded, UCC_BAD_STATE, "no Hamiltonian loaded");
+    UCC_REQUIRE(net->device == c.device, UCC_BAD_ARGS, "network and context on different devices");
+    const int no = c.no, nv = c.nv;
+    const int64_t n = (int64_t)no * no * nv * nv, n1 = (int64_t)no * nv;
+    ensure_rows(*net, n);
+    Scratch X(c, sizeof(float) * n * kFeat);
+    features_kernel<<<grid1(n), 256, 0, c.stream>>>(no, nv, c.get("Voovv").p, c.get("eps").p,
+                                                    static_cast<float*>(X.p));
+    count_kernel_launch();
+    UCC_CUDA(cudaStreamSynchronize(c.stream));
+    forward(*net, static_cast<float*>(X.p), n);
+    UCC_CUDA(cudaStreamSynchronize(net->stream));
+    if (!c.has("T_guess")) c.alloc("T_guess", {n1 + n}, true);
+    double* g = c.get("T_guess").p;
+    // t1 part: f_ia / (f_ii - f_aa) on the host (small)
+    std::vector<double> t1(n1);
+    const int nact = no + nv;
+    for (int i = 0; i < no; i++)
+      for (int a = 0; a < nv; a++)
+        t1[(size_t)i * nv + a] = c.fock[(size_t)i * nact + no + a] / (c.eps[i] - c.eps[no + a]);
+    UCC_CUDA(cudaMemcpyAsync(g, t1.data(), sizeof(double) * n1, cudaMemcpyHostToDevice, c.stream));
+    guess_kernel<<<grid1(n), 256, 0, c.stream>>>(no, nv, c.get("Voovv").p, c.get("eps").p, net->y, g + n1);
+    count_kernel_launch();
+    UCC_CUDA(cudaStreamSynchronize(c.stream));
+  }
+}
+}  // namespace ucc

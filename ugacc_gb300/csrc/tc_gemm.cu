@@ -29,6 +29,9 @@
 namespace ucc {
 
 void count_kernel_launch();  // kernels_fp64.cu
+// C(epi) = alpha * sum_z P[z] + beta * C(epi) (kernels_fp64.cu)
+void splitk_reduce(Ctx& c, int64_t M, int64_t N, int nsplit, const double* P, double alpha, double beta, double* C,
+                   const GemmEpilogue& epi);
 
 namespace tc {
 
@@ -53,6 +56,9 @@ struct Params {
   const int* a_row0;
   const int* b_row0;
   const int64_t* c_off;
+  // split-K (single problem only): chunk z covers K blocks [z*kchunk, (z+1)*kchunk) of each
+  // of the three split products and writes a plain [M][N] FP64 partial at C + z*M*N
+  int ksplit, kchunk;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -170,9 +176,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   __syncthreads();
   fence_after();
   const uint32_t tmem = *tslot;
-  const int KB = 3 * p.kblocks;
   const int tiles_per = p.mtiles * p.ntiles;
-  const int ntile = tiles_per * (p.nprob ? p.nprob : 1);
+  const int ntile = tiles_per * (p.nprob ? p.nprob : (p.ksplit > 1 ? p.ksplit : 1));
 
   if (warp == 0) {
     if (lane == 0) {
@@ -184,12 +189,17 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int pb = tile / tiles_per, tl = tile - pb * tiles_per;
         const int mt = tl % p.mtiles, nt = tl / p.mtiles;
         const int ar = (p.nprob ? p.a_row0[pb] : 0) + mt * BM, br = (p.nprob ? p.b_row0[pb] : 0) + nt * BN;
-        for (int kb = 0; kb < KB; kb++) {
+        int k0 = 0, kn = p.kblocks;
+        if (p.ksplit > 1) {
+          k0 = pb * p.kchunk;
+          kn = min(p.kblocks - k0, p.kchunk);
+        }
+        for (int kb = 0; kb < 3 * kn; kb++) {
           if (!mbar_wait(&empty[stage], phase ^ 1u, p.err)) {
             ok = false;
             break;
           }
-          const int part = kb / p.kblocks, kk = (kb - part * p.kblocks) * BK;
+          const int part = kb / kn, kk = (k0 + kb - part * kn) * BK;
           mbar_expect_tx(&full[stage], A_BYTES + B_BYTES);
           tma_load(sA + stage * A_BYTES, part < 2 ? &mAhi : &mAlo, &full[stage], kk, ar);
           tma_load(sB + stage * B_BYTES, part == 1 ? &mBlo : &mBhi, &full[stage], kk, br);
@@ -211,10 +221,12 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t phase = 0, aphase = 0;
       bool ok = true;
       for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+        int kn = p.kblocks;
+        if (p.ksplit > 1) kn = min(p.kblocks - (tile / tiles_per) * p.kchunk, p.kchunk);
         if (!mbar_wait(&tempty[acc], aphase ^ 1u, p.err)) break;
         fence_after();
         const uint32_t d = tmem + (uint32_t)(acc * BN);
-        for (int kb = 0; kb < KB; kb++) {
+        for (int kb = 0; kb < 3 * kn; kb++) {
           if (!mbar_wait(&full[stage], phase, p.err)) {
             ok = false;
             break;
@@ -245,11 +257,12 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
       const int pb = tile / tiles_per, tl = tile - pb * tiles_per;
       const int mt = tl % p.mtiles, nt = tl / p.mtiles;
-      double* Cb = p.C + (p.nprob ? p.c_off[pb] : 0);
+      double* Cb = p.C + (p.nprob ? p.c_off[pb] : (p.ksplit > 1 ? (int64_t)pb * p.M * p.N : 0));
       if (!mbar_wait(&tfull[acc], aphase, p.err)) break;
       fence_after();
       const int64_t m = (int64_t)mt * BM + q * 32 + lane;
       const int64_t mo = ep.msplit ? (m / ep.msplit) * ep.s_mhi + (m % ep.msplit) * ep.s_mlo : m * ep.s_mhi;
+      const double alpha = p.alpha, beta = p.beta;
       for (int ch = 0; ch < BN / 32; ch++) {
         uint32_t r[32];
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + ch * 32), r);
@@ -260,8 +273,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int64_t n = n0 + j;
             if (n < p.N) {
               double* cp = Cb + mo + n * ep.s_n;
-              const double v = p.alpha * (double)__uint_as_float(r[j]);
-              *cp = (p.beta == 0.0) ? v : fma(p.beta, *cp, v);
+              const double v = alpha * (double)__uint_as_float(r[j]);
+              *cp = (beta == 0.0) ? v : fma(beta, *cp, v);
             }
           }
         }
@@ -317,8 +330,11 @@ struct Cache {
   int* err = nullptr;
   int sms = 0;
   bool attr_set = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   ~Cache() {
     if (err) cudaFree(err);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
   }
 };
 
@@ -352,6 +368,8 @@ static Cache& cache(Ctx& c) {
     UCC_CUDA(cudaMalloc(&k->err, sizeof(int)));
     UCC_CUDA(cudaMemset(k->err, 0, sizeof(int)));
     UCC_CUDA(cudaDeviceGetAttribute(&k->sms, cudaDevAttrMultiProcessorCount, c.device));
+    UCC_CUDA(cudaEventCreate(&k->ev0));
+    UCC_CUDA(cudaEventCreate(&k->ev1));
   }
   return *static_cast<Cache*>(c.tc_cache.get());
 }
@@ -413,30 +431,73 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
   p.nprob = 0;
   p.a_row0 = p.b_row0 = nullptr;
   p.c_off = nullptr;
+  p.ksplit = 1;
+  p.kchunk = p.kblocks;
   const int tiles = p.mtiles * p.ntiles;
-  const int grid = std::min(tiles, k.sms);
+  // too few output tiles for the SMs and a long K: split K, FP64 partials, fixed-order reduce
+  std::unique_ptr<Scratch> part;
+  if (tiles * 2 <= k.sms && p.kblocks >= 8) {
+    int ks = std::min(k.sms / tiles, p.kblocks / 4);
+    if (ks > 1) {
+      p.kchunk = (p.kblocks + ks - 1) / ks;
+      p.ksplit = (p.kblocks + p.kchunk - 1) / p.kchunk;
+      part = std::make_unique<Scratch>(c, sizeof(double) * M * N * p.ksplit);
+      p.C = part->d();
+      p.alpha = 1.0;
+      p.beta = 0.0;
+      p.epi.msplit = 0;
+      p.epi.s_mhi = N;
+      p.epi.s_n = 1;
+    }
+  }
+  const int grid = std::min(tiles * p.ksplit, k.sms);
+  UCC_CUDA(cudaEventRecord(k.ev0, c.stream));
   gemm_kernel<<<grid, THREADS, SMEM_BYTES, c.stream>>>(a->mhi, a->mlo, b->mhi, b->mlo, p);
   count_kernel_launch();
   c.stats.tc_gemm_launches++;
   UCC_CUDA(cudaGetLastError());
+  if (part) splitk_reduce(c, M, N, p.ksplit, part->d(), alpha, beta, C, epi);
+  UCC_CUDA(cudaEventRecord(k.ev1, c.stream));
   int herr = 0;
   UCC_CUDA(cudaMemcpyAsync(&herr, k.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
   UCC_CUDA(cudaStreamSynchronize(c.stream));  // also keeps the temporary splits alive until the GEMM is done
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, k.ev0, k.ev1);
+  c.stats.tc_gemm_ms += ms;
+  c.stats.tc_gemm_flops += 2.0 * (double)M * (double)N * (double)K;
   if (herr) {
     cudaMemsetAsync(k.err, 0, sizeof(int), c.stream);
     throw Error(UCC_DEVICE_TIMEOUT, "tensor-core GEMM: a pipeline wait timed out");
   }
 }
 
-bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
-                const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn) {
-  if (M < 128 || N < 128 || K < 64 || (double)M * N * K < 1e8) return false;
-  if (M > INT32_MAX || N > INT32_MAX) return false;
+bool tc_eligible(int64_t M, int64_t N, int64_t K) {
+  // small problems stay on the FP64 path; the tensor tile is 128 x 256 x 64
+  if (std::max(M, N) < 64 || K < 16 || (double)M * N * K < 1e7) return false;
+  return M <= INT32_MAX && N <= INT32_MAX;
+}
+
+void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
+                      int64_t sAk, const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm,
+                      int64_t sCn) {
   GemmEpilogue epi;
   epi.msplit = 0;
-  epi.s_mhi = sCm;
-  epi.s_n = sCn;
-  tc_gemm_run(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi);
+  if (M < 128 && N > M) {
+    // short M: compute C^T = B^T A^T so that the long side fills the 128-row MMA tile
+    epi.s_mhi = sCn;
+    epi.s_n = sCm;
+    tc_gemm_run(c, N, M, K, alpha, B, sBn, sBk, A, sAk, sAm, beta, C, epi);
+  } else {
+    epi.s_mhi = sCm;
+    epi.s_n = sCn;
+    tc_gemm_run(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi);
+  }
+}
+
+bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn) {
+  if (!tc_eligible(M, N, K)) return false;
+  tc_gemm_oriented(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, sCm, sCn);
   return true;
 }
 
@@ -575,16 +636,24 @@ bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, double* W3) {
     p.epi.s_n = terms[q].sw;
     p.err = k.err;
     p.nprob = nb;
+    p.ksplit = 1;
+    p.kchunk = p.kblocks;
     p.a_row0 = T.d_arow;
     p.b_row0 = T.d_brow;
     p.c_off = T.d_coff;
     const int tiles = p.mtiles * p.ntiles * nb;
+    UCC_CUDA(cudaEventRecord(k.ev0, c.stream));
     gemm_kernel<<<std::min(tiles, k.sms), THREADS, SMEM_BYTES, c.stream>>>(T.A.mhi, T.A.mlo, T.B.mhi, T.B.mlo, p);
     count_kernel_launch();
     c.stats.tc_gemm_launches++;
     UCC_CUDA(cudaGetLastError());
+    UCC_CUDA(cudaEventRecord(k.ev1, c.stream));
     // the row tables are rewritten for the next term: keep the copies ordered after use
     UCC_CUDA(cudaStreamSynchronize(c.stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, k.ev0, k.ev1);
+    c.stats.tc_gemm_ms += ms;
+    c.stats.tc_gemm_flops += 2.0 * (double)nv2 * (double)nv * (double)(nv + no) * nb;
   }
   int herr = 0;
   UCC_CUDA(cudaMemcpy(&herr, k.err, sizeof(int), cudaMemcpyDeviceToHost));

@@ -141,3 +141,29 @@ def write_input_file(path: str, ham: SyntheticHamiltonian, perts: list[np.ndarra
                 # <p q | r s> = (p r | q s) = sum_Q B[Q,p,r] B[Q,q,s]
                 slab = np.einsum("Qr,Qqs->qrs", Bm[:, p, :], Bm, optimize=True)
                 f.write(np.ascontiguousarray(slab, dtype="<f8").tobytes())
+
+
+# ---------------------------------------------------------------------------------
+# A smooth family of uneven-size Hamiltonians: B(s) = B0 + s * B1 at the largest size
+# (no = 12, nv = 96, naux = 3 * 108), every member sliced to its own (no, nv): the no
+# highest occupied and the nv lowest virtual orbitals of the largest model.
+# ---------------------------------------------------------------------------------
+FAMILY_MAX = (12, 96)
+
+
+def make_family(count: int, seed: int, no_range=(4, 12), nv_range=(20, 96)):
+    nomax, nvmax = FAMILY_MAX
+    base = make_hamiltonian(nomax, nvmax, seed)
+    pert = make_hamiltonian(nomax, nvmax, seed + 1)
+    rng = np.random.default_rng([seed, 99])
+    out = []
+    for k in range(count):
+        s = rng.uniform(0.0, 1.0)
+        no = int(rng.integers(no_range[0], no_range[1] + 1))
+        nv = int(rng.integers(nv_range[0], nv_range[1] + 1))
+        idx = np.r_[np.arange(nomax - no, nomax), np.arange(nomax, nomax + nv)]
+        B = (base.B + s * pert.B)[:, idx][:, :, idx]
+        h = SyntheticHamiltonian(no=no, nv=nv, naux=base.naux, seed=seed, eps=base.eps[idx].copy(),
+                                 B=np.ascontiguousarray(B), extra={"s": s, "member": k})
+        out.append(h)
+    return out

@@ -26,7 +26,10 @@ def main(argv=None):
     ap.add_argument("--triples", action="store_true")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--gemm", type=int, nargs=3, metavar=("M", "N", "K"))
-    ap.add_argument("--print", action="store_true", help="print the iteration tables")
+    ap.add_argument("--print", type=int, nargs="?", const=1, default=0,
+                    help="print the iteration tables (2: also the residual error of every mixed sweep)")
+    ap.add_argument("--switch", type=float, default=1e-5, help="MIXED hand-over residual norm")
+    ap.add_argument("--diis", type=int, default=1, help="0 turns DIIS extrapolation off")
     a = ap.parse_args(argv)
 
     import ugacc_gb300 as U
@@ -44,13 +47,14 @@ def main(argv=None):
     H = U.Hamiltonian.from_synthetic(h)
     prec = a.precision.upper()
     if a.iters > 0:
-        cc = U.CCWfn(H, {"MAXITER": a.iters, "R_CONVERGENCE": 1e-10, "PRECISION": prec, "PRINT": int(a.print)})
+        cc = U.CCWfn(H, {"MAXITER": a.iters, "R_CONVERGENCE": 1e-10, "PRECISION": prec, "PRINT": int(a.print),
+                         "MIXED_SWITCH": a.switch, "DIIS": bool(a.diis)})
         try:
             cc.compute_energy()
         except U.ConvergenceError:
             pass
     if a.triples:
-        cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": prec, "PRINT": int(a.print)})
+        cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": prec, "PRINT": int(a.print), "MIXED_SWITCH": a.switch})
         cc.compute_energy()
         H.ctx.reset_stats()
         cc.triples()
