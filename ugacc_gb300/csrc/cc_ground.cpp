@@ -489,6 +489,15 @@ CCSDResult run_ccsd(Ctx& c) {
       build_t2(c, t1, t2, c.get("tau"), amp2(c, r), &ev);
       c.anchors.mode = 0;
     }
+    if (kind == kSplit || kind == kDelta) {
+      // The exact residual is symmetric under (i,j,a,b) -> (j,i,b,a); rounding of the
+      // tensor-core products is not.  In the antisymmetric sector the Fock terms cancel
+      // and the Jacobi step does not damp, so project the noise out of R2.
+      Tensor R2 = amp2(c, r);
+      Temp S(c, {no, no, nv, nv});
+      transpose_add(c, "ijab->jiba", 1.0, R2, 0.0, S);
+      axpby(c, S->size(), 0.5, S->p, 0.5, R2.p);
+    }
     double noise = -1.0, drift = -1.0;
     if (c.opt.print >= 2 && mixed) {
       // diagnostics: distance of this residual from the FP64 one at the same amplitudes,
