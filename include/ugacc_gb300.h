@@ -120,11 +120,12 @@ ucc_status ucc_get_tensor(ucc_ctx* ctx, const char* name, double* host_out, size
 ucc_status ucc_set_tensor(ucc_ctx* ctx, const char* name, const double* host_in, size_t count);
 
 /* ---- Learned T2 starting amplitudes (no counterpart in the reference; its guess is MP2,
- * ccwfn.cc:75-87).  A small MLP (8 pair features -> 256 -> 256 -> 1, SiLU, FP16 weights,
- * FP32 accumulation) predicts S*(t2_CCSD - t2_MP2) per doubles element, S = 100; the
+ * ccwfn.cc:75-87).  A small MLP (12 pair features -> 256 -> 256 -> 1, SiLU, FP16 weights,
+ * FP32 accumulation) predicts T*(t2_CCSD - t2_MP2) per doubles element, T = 1000; the
  * plain CCSD iteration started from its prediction decides the converged answer.
- * Features of element (i,j,a,b), D = e_i+e_j-e_a-e_b: S<ij|ab>/D, S<ij|ba>/D, S<ij|ab>,
- * -1/D, (e_i+e_j)/2, (e_a+e_b)/2, [i==j], [a==b].  Rows are [no][no][nv][nv] order. */
+ * Features of element (i,j,a,b), D = e_i+e_j-e_a-e_b, S = 100: S<ij|ab>/D, S<ij|ba>/D,
+ * S<ij|ab>, -1/D, (e_i+e_j)/2, (e_a+e_b)/2, [i==j], [a==b], S<ab|ab>, S<ij|ij>,
+ * S(<ia|ia>+<jb|jb>), S(<ia|ai>+<jb|bj>).  Rows are [no][no][nv][nv] order. */
 typedef struct ucc_mlp ucc_mlp;
 ucc_status ucc_mlp_create(ucc_mlp** net, int device, uint64_t seed);
 ucc_status ucc_mlp_destroy(ucc_mlp* net);
@@ -174,6 +175,9 @@ ucc_status ucc_batch_guess_mlp(ucc_batch* b, int index, ucc_mlp* net);
 /* solve every member: e_ccsd, iterations and converged (0/1) are arrays of length members */
 ucc_status ucc_batch_ccsd(ucc_batch* b, const ucc_options* opt, double* e_ccsd, int* iterations, int* converged);
 ucc_status ucc_batch_get_info(ucc_batch* b, ucc_batch_info* out);
+/* pair features / targets of member `index` (ucc_mlp_features semantics; targets after a
+ * solve in which the member converged) */
+ucc_status ucc_batch_features(ucc_batch* b, int index, float* out, size_t rows, int with_targets, float* targets);
 ucc_status ucc_batch_get_t2(ucc_batch* b, int index, double* out, size_t count);
 
 typedef struct ucc_stats {

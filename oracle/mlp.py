@@ -1,13 +1,14 @@
 """numpy restatement of the learned-guess MLP (test infrastructure).
 
-Mirrors ugacc_gb300/csrc/mlp.cu: 8 features -> 256 -> 256 -> 1 with SiLU, parameters in
+Mirrors ugacc_gb300/csrc/mlp.cu: 12 features -> 256 -> 256 -> 1 with SiLU, parameters in
 the order W1[8][256] b1[256] W2[256][256] b2[256] w3[256] b3, mean-squared-error loss.
 The GPU stores the three weight matrices in FP16 for its forward and backward products
 (biases stay FP32), so the comparison rounds them the same way.
 """
 import numpy as np
 
-F, H = 8, 256
+F, H = 12, 256
+F_COUNT = F
 SIZES = [("W1", (F, H)), ("b1", (H,)), ("W2", (H, H)), ("b2", (H,)), ("w3", (H,)), ("b3", (1,))]
 
 
@@ -67,7 +68,8 @@ def loss_grad(p, X, t, half_weights=True):
     return loss, np.concatenate([g[name].ravel() for name, _ in SIZES])
 
 
-SCALE = 100.0  # targets and the correction carried by the network are S * (t2 - t2_mp2)
+SCALE = 100.0     # scale of the integral-valued features
+TARGET = 1000.0   # targets and the network's output are TARGET * (t2 - t2_mp2)
 
 
 def _denominators(no, nv, eps):
@@ -75,26 +77,39 @@ def _denominators(no, nv, eps):
     return ((eo[:, None, None, None] + eo[None, :, None, None]) - ev[None, None, :, None]) - ev[None, None, None, :]
 
 
-def features(no, nv, Voovv, eps):
-    """Pair features of every T2 element (i, j, a, b), row-major: the MP2 amplitude and
-    its exchange partner, the integral, -1/D, the mean occupied and virtual orbital
-    energies and the i == j, a == b flags (the first three scaled by S)."""
+def features(no, nv, V):
+    """Pair features of every T2 element (i, j, a, b), row-major, from the <pq|rs> blocks
+    of `V` (a dict with "oovv", "oooo", "ovov", "vvvv" and "eps"): the MP2 amplitude and its
+    exchange partner, the integral, -1/D, the mean occupied and virtual orbital energies,
+    the i == j and a == b flags, and the diagonal ladder and ring elements <ab|ab>, <ij|ij>,
+    <ia|ia> + <jb|jb>, <ia|ai> + <jb|bj>."""
+    eps = V["eps"]
     D = _denominators(no, nv, eps)
-    V = Voovv.reshape(no, no, nv, nv)
-    Vx = V.transpose(0, 1, 3, 2)
+    Voovv, Voooo, Vovov, Vvvvv = V["oovv"], V["oooo"], V["ovov"], V["vvvv"]
     eo, ev = eps[:no], eps[no:]
-    F = np.empty((no, no, nv, nv, 8))
-    F[..., 0] = SCALE * V / D
-    F[..., 1] = SCALE * Vx / D
-    F[..., 2] = SCALE * V
+    i, j, a, b = np.meshgrid(np.arange(no), np.arange(no), np.arange(nv), np.arange(nv), indexing="ij")
+    F = np.empty((no, no, nv, nv, F_COUNT))
+    F[..., 0] = SCALE * Voovv / D
+    F[..., 1] = SCALE * Voovv.transpose(0, 1, 3, 2) / D
+    F[..., 2] = SCALE * Voovv
     F[..., 3] = -1.0 / D
     F[..., 4] = 0.5 * (eo[:, None, None, None] + eo[None, :, None, None])
     F[..., 5] = 0.5 * (ev[None, None, :, None] + ev[None, None, None, :])
-    F[..., 6] = np.eye(no)[:, :, None, None]
-    F[..., 7] = np.eye(nv)[None, None, :, :]
-    return F.reshape(-1, 8)
+    F[..., 6] = (i == j)
+    F[..., 7] = (a == b)
+    F[..., 8] = SCALE * Vvvvv[a, b, a, b]
+    F[..., 9] = SCALE * Voooo[i, j, i, j]
+    F[..., 10] = SCALE * (Vovov[i, a, i, a] + Vovov[j, b, j, b])
+    F[..., 11] = SCALE * (Voovv[i, i, a, a] + Voovv[j, j, b, b])
+    return F.reshape(-1, F_COUNT)
+
+
+def blocks(ints, no):
+    """The <pq|rs> blocks features() reads, from a full [nact]^4 array."""
+    o, v = slice(0, no), slice(no, None)
+    return {"oovv": ints[o, o, v, v], "oooo": ints[o, o, o, o], "ovov": ints[o, v, o, v], "vvvv": ints[v, v, v, v]}
 
 
 def targets(no, nv, Voovv, eps, t2):
     D = _denominators(no, nv, eps)
-    return (SCALE * (t2.reshape(no, no, nv, nv) - Voovv.reshape(no, no, nv, nv) / D)).ravel()
+    return (TARGET * (t2.reshape(no, no, nv, nv) - Voovv.reshape(no, no, nv, nv) / D)).ravel()

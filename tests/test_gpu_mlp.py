@@ -47,12 +47,13 @@ def test_features_and_targets_match_oracle():
     h = make_hamiltonian(4, 20, 3)
     H = U.Hamiltonian.from_synthetic(h)
     no, nv = h.no, h.nv
-    V = h.ints_physicist()[:no, :no, no:, no:]
-    np.testing.assert_allclose(U.mlp_features(H), M.features(no, nv, V, h.eps), rtol=2e-7, atol=1e-7)
+    ints = h.ints_physicist()
+    blocks = dict(M.blocks(ints, no), eps=h.eps)
+    np.testing.assert_allclose(U.mlp_features(H), M.features(no, nv, blocks), rtol=2e-7, atol=1e-7)
     cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10})
     cc.compute_energy()
     X, t = U.mlp_features(H, with_targets=True)
-    np.testing.assert_allclose(t, M.targets(no, nv, V, h.eps, cc.t2), rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(t, M.targets(no, nv, blocks["oovv"], h.eps, cc.t2), rtol=1e-6, atol=1e-5)
 
 
 def test_training_lowers_the_loss():
@@ -95,3 +96,14 @@ def test_learned_guess_saves_iterations():
         it_mlp.append(n1)
     print("iterations MP2 guess", it_mp2, "learned guess", it_mlp)
     assert sum(it_mlp) < sum(it_mp2)
+
+
+def test_family_workflow_batched_learned_guess():
+    from ugacc_gb300 import family
+    out = family.run(members=24, train=16, seed=11, r_conv=1e-8, epochs=8, row_fraction=1.0, no_range=(4, 8),
+                     nv_range=(20, 48))
+    print(out)
+    assert out["all_members"]["converged"] == 24
+    assert out["test_learned_guess"]["converged"] == out["test_mp2_guess"]["converged"] == 8
+    assert out["max_abs_dE"] < 1e-7
+    assert out["iterations_saved"] > 0

@@ -24,11 +24,18 @@ def test_oracle_gradient_matches_finite_differences():
 def test_oracle_features_layout():
     from ugacc_gb300.generator import make_hamiltonian
     h = make_hamiltonian(3, 5, 0)
-    V = h.ints_physicist()[:3, :3, 3:, 3:]
-    F = M.features(3, 5, V, h.eps)
-    assert F.shape == (3 * 3 * 5 * 5, 8)
-    r = ((1 * 3 + 2) * 5 + 4) * 5 + 0  # (i, j, a, b) = (1, 2, 4, 0)
-    D = h.eps[1] + h.eps[2] - h.eps[3 + 4] - h.eps[3 + 0]
-    assert np.isclose(F[r, 0], M.SCALE * V[1, 2, 4, 0] / D)
-    assert np.isclose(F[r, 1], M.SCALE * V[1, 2, 0, 4] / D)
+    ints = h.ints_physicist()
+    V = dict(M.blocks(ints, 3), eps=h.eps)
+    F = M.features(3, 5, V)
+    assert F.shape == (3 * 3 * 5 * 5, M.F)
+    i, j, a, b = 1, 2, 4, 0
+    r = ((i * 3 + j) * 5 + a) * 5 + b
+    D = h.eps[i] + h.eps[j] - h.eps[3 + a] - h.eps[3 + b]
+    A, B = 3 + a, 3 + b
+    assert np.isclose(F[r, 0], M.SCALE * ints[i, j, A, B] / D)
+    assert np.isclose(F[r, 1], M.SCALE * ints[i, j, B, A] / D)
     assert F[r, 6] == 0 and F[r, 7] == 0
+    assert np.isclose(F[r, 8], M.SCALE * ints[A, B, A, B])
+    assert np.isclose(F[r, 9], M.SCALE * ints[i, j, i, j])
+    assert np.isclose(F[r, 10], M.SCALE * (ints[i, A, i, A] + ints[j, B, j, B]))
+    assert np.isclose(F[r, 11], M.SCALE * (ints[i, i, A, A] + ints[j, j, B, B]))

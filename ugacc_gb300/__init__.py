@@ -133,6 +133,7 @@ def load_library(path: str | None = None):
         "ucc_batch_ccsd": (i, [vp, P(_Options), dp, P(i), P(i)]),
         "ucc_batch_get_info": (i, [vp, P(BatchInfo)]),
         "ucc_batch_get_t2": (i, [vp, i, dp, ctypes.c_size_t]),
+        "ucc_batch_features": (i, [vp, i, fp, ctypes.c_size_t, i, fp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -432,9 +433,9 @@ def _fptr(a: np.ndarray):
 
 
 class MLP:
-    """The guess network of mlp.cu: 8 pair features -> 256 -> 256 -> 1 (SiLU)."""
+    """The guess network of mlp.cu: 12 pair features -> 256 -> 256 -> 1 (SiLU)."""
 
-    NFEAT = 8
+    NFEAT = 12
 
     def __init__(self, device: int = 0, seed: int = 0):
         self.lib = load_library()
@@ -564,6 +565,16 @@ class Batch:
         out = np.empty((no, no, nv, nv))
         self.check(self.lib.ucc_batch_get_t2(self.h, index, _ptr(out), out.size))
         return out
+
+    def features(self, index: int, with_targets: bool = False):
+        """Pair features (and targets after a converged solve) of member `index`."""
+        no, nv = self.sizes[index]
+        n = no * no * nv * nv
+        X = np.empty((n, MLP.NFEAT), dtype=np.float32)
+        t = np.empty(n, dtype=np.float32) if with_targets else None
+        self.check(self.lib.ucc_batch_features(self.h, index, _fptr(X), n, int(with_targets),
+                                               _fptr(t) if with_targets else None))
+        return (X, t) if with_targets else X
 
     def close(self):
         if getattr(self, "h", None):

@@ -32,6 +32,7 @@
 namespace ucc {
 void count_kernel_launch();
 void mlp_guess(Ctx& c, ucc_mlp* net);  // mlp.cu
+void mlp_features(Ctx& c, float* out, size_t rows, float* targets, bool with_targets);
 
 namespace batch {
 
@@ -993,10 +994,20 @@ ucc_status ucc_batch_ccsd(ucc_batch* b, const ucc_options* opt, double* e_ccsd, 
     UCC_CUDA(cudaMemcpy(iterations, B.iterations.p, sizeof(int) * nm, cudaMemcpyDeviceToHost));
     UCC_CUDA(cudaMemcpy(converged, B.converged.p, sizeof(int) * nm, cudaMemcpyDeviceToHost));
     double fl = 0.0;
-    for (int k = 0; k < nm; k++) fl += iterations[k] * flops_ccsd_iter(B.members[k]->no, B.members[k]->nv);
+    for (int k = 0; k < nm; k++) {
+      fl += iterations[k] * flops_ccsd_iter(B.members[k]->no, B.members[k]->nv);
+      B.members[k]->have_ccsd = converged[k] != 0;
+    }
     B.info.sweeps = sweeps;
     B.info.solve_ms = ms;
     B.info.flops = fl;
+  });
+}
+
+ucc_status ucc_batch_features(ucc_batch* b, int index, float* out, size_t rows, int with_targets, float* targets) {
+  return bguard(b, [&](ucc_batch& B) {
+    UCC_REQUIRE(index >= 0 && index < (int)B.members.size(), UCC_BAD_ARGS, "bad member index");
+    mlp_features(*B.members[index], out, rows, targets, with_targets != 0);
   });
 }
 

@@ -5,11 +5,13 @@
 // (ccwfn.cc:75-87 gives the MP2 guess t2 = <ij|ab>/D).  The plain CCSD iteration then
 // starts from t2 = t2_mp2 + prediction; its own convergence test decides the answer.
 //
-//   features (kFeat = 8), D = e_i + e_j - e_a - e_b:
+//   features (kFeat = 12), D = e_i + e_j - e_a - e_b, S = kScale:
 //     0: S*<ij|ab>/D   1: S*<ij|ba>/D   2: S*<ij|ab>   3: -1/D
 //     4: (e_i+e_j)/2   5: (e_a+e_b)/2   6: [i==j]      7: [a==b]
-//   target: S*(t2_ccsd - t2_mp2),   S = kScale
-//   network: 8 -> 256 -> 256 -> 1, SiLU; weights stored in FP16 for the forward and
+//     8: S*<ab|ab>     9: S*<ij|ij>    10: S*(<ia|ia> + <jb|jb>)   11: S*(<ia|ai> + <jb|bj>)
+//   (8-11 are the diagonal ladder and ring elements that dress the MP2 denominator)
+//   target: T*(t2_ccsd - t2_mp2),   T = kTarget
+//   network: 12 -> 256 -> 256 -> 1, SiLU; weights stored in FP16 for the forward and
 //   backward passes, FP32 master copies for the Adam update, FP32 accumulation.
 #include <cuda_fp16.h>
 
@@ -24,11 +26,13 @@ namespace ucc {
 void count_kernel_launch();
 Ctx& ctx_of(ucc_ctx* h);               // capi.cpp
 void mlp_guess(Ctx& c, ucc_mlp* net);  // t2 guess of the network into the context's T_guess
+// pair features (and, with targets, the scaled t2 - t2_mp2 of converged amplitudes) to host
+void mlp_features(Ctx& c, float* out, size_t rows, float* targets, bool with_targets);
 
 namespace mlp {
 
-constexpr int kFeat = 8, kHid = 256;
-constexpr double kScale = 100.0;
+constexpr int kFeat = 12, kHid = 256;
+constexpr double kScale = 100.0, kTarget = 1000.0;
 
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
 __device__ __forceinline__ float dsilu(float z) {
@@ -161,8 +165,10 @@ __global__ void gather_rows(int64_t nb, int f, const int64_t* idx, const float* 
 }
 
 // features of every (i,j,a,b) of the loaded Hamiltonian
-__global__ void features_kernel(int no, int nv, const double* Voovv, const double* eps, float* X) {
+__global__ void features_kernel(int no, int nv, const double* Voovv, const double* Voooo, const double* Vovov,
+                                const double* Vvvvv, const double* eps, float* X) {
   const int64_t n = (int64_t)no * no * nv * nv;
+  const int64_t o = no, v = nv;
   for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
     const int b = (int)(x % nv);
     int64_t r = x / nv;
@@ -170,20 +176,24 @@ __global__ void features_kernel(int no, int nv, const double* Voovv, const doubl
     r /= nv;
     const int j = (int)(r % no), i = (int)(r / no);
     const double D = ((eps[i] + eps[j]) - eps[no + a]) - eps[no + b];
-    const double v = Voovv[x];
+    const double vij = Voovv[x];
     const double vx = Voovv[(((int64_t)i * no + j) * nv + b) * nv + a];
     float* f = X + x * kFeat;
-    f[0] = (float)(kScale * v / D);
+    f[0] = (float)(kScale * vij / D);
     f[1] = (float)(kScale * vx / D);
-    f[2] = (float)(kScale * v);
+    f[2] = (float)(kScale * vij);
     f[3] = (float)(-1.0 / D);
     f[4] = (float)(0.5 * (eps[i] + eps[j]));
     f[5] = (float)(0.5 * (eps[no + a] + eps[no + b]));
     f[6] = i == j ? 1.f : 0.f;
     f[7] = a == b ? 1.f : 0.f;
+    f[8] = (float)(kScale * Vvvvv[((a * v + b) * v + a) * v + b]);                                // <ab|ab>
+    f[9] = (float)(kScale * Voooo[((i * o + j) * o + i) * o + j]);                                // <ij|ij>
+    f[10] = (float)(kScale * (Vovov[((i * v + a) * o + i) * v + a] + Vovov[((j * v + b) * o + j) * v + b]));
+    f[11] = (float)(kScale * (Voovv[((i * o + i) * v + a) * v + a] + Voovv[((j * o + j) * v + b) * v + b]));
   }
 }
-// target = S * (t2 - t2_mp2)
+// target = T * (t2 - t2_mp2)
 __global__ void targets_kernel(int no, int nv, const double* Voovv, const double* eps, const double* t2, float* y) {
   const int64_t n = (int64_t)no * no * nv * nv;
   for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
@@ -193,10 +203,10 @@ __global__ void targets_kernel(int no, int nv, const double* Voovv, const double
     r /= nv;
     const int j = (int)(r % no), i = (int)(r / no);
     const double D = ((eps[i] + eps[j]) - eps[no + a]) - eps[no + b];
-    y[x] = (float)(kScale * (t2[x] - Voovv[x] / D));
+    y[x] = (float)(kTarget * (t2[x] - Voovv[x] / D));
   }
 }
-// t2 = t2_mp2 + prediction / S, written into the packed guess buffer (t1 = f_ia / D1)
+// t2 = t2_mp2 + prediction / T, written into the packed guess buffer (t1 = f_ia / D1)
 __global__ void guess_kernel(int no, int nv, const double* Voovv, const double* eps, const float* pred, double* t2) {
   const int64_t n = (int64_t)no * no * nv * nv;
   for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
@@ -206,7 +216,7 @@ __global__ void guess_kernel(int no, int nv, const double* Voovv, const double* 
     r /= nv;
     const int j = (int)(r % no), i = (int)(r / no);
     const double D = ((eps[i] + eps[j]) - eps[no + a]) - eps[no + b];
-    t2[x] = Voovv[x] / D + (double)pred[x] / kScale;
+    t2[x] = Voovv[x] / D + (double)pred[x] / kTarget;
   }
 }
 
@@ -499,24 +509,7 @@ ucc_status ucc_mlp_features(ucc_ctx* ctx, float* out, size_t rows, int with_targ
   Ctx& c = ctx_of(ctx);
   try {
     UCC_CUDA(cudaSetDevice(c.device));
-    UCC_REQUIRE(c.loaded, UCC_BAD_STATE, "no Hamiltonian loaded");
-    const int64_t n = (int64_t)c.no * c.no * c.nv * c.nv;
-    UCC_REQUIRE((int64_t)rows == n, UCC_BAD_ARGS, "rows must be no*no*nv*nv");
-    Scratch X(c, sizeof(float) * n * kFeat);
-    features_kernel<<<grid1(n), 256, 0, c.stream>>>(c.no, c.nv, c.get("Voovv").p, c.get("eps").p,
-                                                    static_cast<float*>(X.p));
-    count_kernel_launch();
-    UCC_CUDA(cudaMemcpyAsync(out, X.p, sizeof(float) * n * kFeat, cudaMemcpyDeviceToHost, c.stream));
-    if (with_targets) {
-      UCC_REQUIRE(targets && c.have_ccsd, UCC_BAD_STATE, "targets need converged CCSD amplitudes");
-      Scratch y(c, sizeof(float) * n);
-      targets_kernel<<<grid1(n), 256, 0, c.stream>>>(c.no, c.nv, c.get("Voovv").p, c.get("eps").p,
-                                                     amp2(c, c.get("T").p).p, static_cast<float*>(y.p));
-      count_kernel_launch();
-      UCC_CUDA(cudaMemcpyAsync(targets, y.p, sizeof(float) * n, cudaMemcpyDeviceToHost, c.stream));
-      UCC_CUDA(cudaStreamSynchronize(c.stream));
-    }
-    UCC_CUDA(cudaStreamSynchronize(c.stream));
+    mlp_features(c, out, rows, with_targets ? targets : nullptr, with_targets != 0);
     return UCC_OK;
   } catch (const Error& e) {
     c.last_error = e.what();
@@ -541,6 +534,27 @@ ucc_status ucc_mlp_guess(ucc_ctx* ctx, ucc_mlp* net) {
 }  // extern "C"
 
 namespace ucc {
+void mlp_features(Ctx& c, float* out, size_t rows, float* targets, bool with_targets) {
+  UCC_REQUIRE(out, UCC_BAD_ARGS, "null argument");
+  UCC_REQUIRE(c.loaded, UCC_BAD_STATE, "no Hamiltonian loaded");
+  const int64_t n = (int64_t)c.no * c.no * c.nv * c.nv;
+  UCC_REQUIRE((int64_t)rows == n, UCC_BAD_ARGS, "rows must be no*no*nv*nv");
+  Scratch X(c, sizeof(float) * n * kFeat);
+  features_kernel<<<grid1(n), 256, 0, c.stream>>>(c.no, c.nv, c.get("Voovv").p, c.get("Voooo").p, c.get("Vovov").p,
+                                                  c.get("Vvvvv").p, c.get("eps").p, static_cast<float*>(X.p));
+  count_kernel_launch();
+  UCC_CUDA(cudaMemcpyAsync(out, X.p, sizeof(float) * n * kFeat, cudaMemcpyDeviceToHost, c.stream));
+  if (with_targets) {
+    UCC_REQUIRE(targets && c.have_ccsd, UCC_BAD_STATE, "targets need converged CCSD amplitudes");
+    Scratch y(c, sizeof(float) * n);
+    targets_kernel<<<grid1(n), 256, 0, c.stream>>>(c.no, c.nv, c.get("Voovv").p, c.get("eps").p,
+                                                   amp2(c, c.get("T").p).p, static_cast<float*>(y.p));
+    count_kernel_launch();
+    UCC_CUDA(cudaMemcpyAsync(targets, y.p, sizeof(float) * n, cudaMemcpyDeviceToHost, c.stream));
+  }
+  UCC_CUDA(cudaStreamSynchronize(c.stream));
+}
+
 void mlp_guess(Ctx& c, ucc_mlp* net) {
   {
     UCC_REQUIRE(c.loaded, UCC_BAD_STATE, "no Hamiltonian loaded");
@@ -549,7 +563,8 @@ void mlp_guess(Ctx& c, ucc_mlp* net) {
     const int64_t n = (int64_t)no * no * nv * nv, n1 = (int64_t)no * nv;
     ensure_rows(*net, n);
     Scratch X(c, sizeof(float) * n * kFeat);
-    features_kernel<<<grid1(n), 256, 0, c.stream>>>(no, nv, c.get("Voovv").p, c.get("eps").p,
+    features_kernel<<<grid1(n), 256, 0, c.stream>>>(no, nv, c.get("Voovv").p, c.get("Voooo").p,
+                                                    c.get("Vovov").p, c.get("Vvvvv").p, c.get("eps").p,
                                                     static_cast<float*>(X.p));
     count_kernel_launch();
     UCC_CUDA(cudaStreamSynchronize(c.stream));

@@ -30,6 +30,8 @@ def main(argv=None):
                     help="print the iteration tables (2: also the residual error of every mixed sweep)")
     ap.add_argument("--switch", type=float, default=1e-5, help="MIXED hand-over residual norm")
     ap.add_argument("--diis", type=int, default=1, help="0 turns DIIS extrapolation off")
+    ap.add_argument("--ccsd-fp64", action="store_true",
+                    help="with --triples: converge CCSD in FP64, then run (T) at --precision")
     a = ap.parse_args(argv)
 
     import ugacc_gb300 as U
@@ -54,10 +56,14 @@ def main(argv=None):
         except U.ConvergenceError:
             pass
     if a.triples:
-        cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": prec, "PRINT": int(a.print), "MIXED_SWITCH": a.switch})
+        cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": "FP64" if a.ccsd_fp64 else prec, "PRINT": int(a.print),
+                         "MIXED_SWITCH": a.switch})
         cc.compute_energy()
+        if a.ccsd_fp64:
+            cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": prec})
         H.ctx.reset_stats()
-        cc.triples()
+        e_t = cc.triples()
+        print(json.dumps({"e_t": e_t}))
     print(json.dumps(H.ctx.stats()))
     return 0
 
