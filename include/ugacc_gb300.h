@@ -120,12 +120,13 @@ ucc_status ucc_get_tensor(ucc_ctx* ctx, const char* name, double* host_out, size
 ucc_status ucc_set_tensor(ucc_ctx* ctx, const char* name, const double* host_in, size_t count);
 
 /* ---- Learned T2 starting amplitudes (no counterpart in the reference; its guess is MP2,
- * ccwfn.cc:75-87).  A small MLP (12 pair features -> 256 -> 256 -> 1, SiLU, FP16 weights,
+ * ccwfn.cc:75-87).  A small MLP (15 pair features -> 256 -> 256 -> 1, SiLU, FP16 weights,
  * FP32 accumulation) predicts T*(t2_CCSD - t2_MP2) per doubles element, T = 1000; the
  * plain CCSD iteration started from its prediction decides the converged answer.
  * Features of element (i,j,a,b), D = e_i+e_j-e_a-e_b, S = 100: S<ij|ab>/D, S<ij|ba>/D,
  * S<ij|ab>, -1/D, (e_i+e_j)/2, (e_a+e_b)/2, [i==j], [a==b], S<ab|ab>, S<ij|ij>,
- * S(<ia|ia>+<jb|jb>), S(<ia|ai>+<jb|bj>).  Rows are [no][no][nv][nv] order. */
+ * S(<ia|ia>+<jb|jb>), S(<ia|ai>+<jb|bj>), |e_i-e_j|/2, |e_a-e_b|/2, (e_i-e_j)(e_a-e_b)/4,
+ * all invariant under (i,j,a,b) -> (j,i,b,a).  Rows are [no][no][nv][nv] order. */
 typedef struct ucc_mlp ucc_mlp;
 ucc_status ucc_mlp_create(ucc_mlp** net, int device, uint64_t seed);
 ucc_status ucc_mlp_destroy(ucc_mlp* net);

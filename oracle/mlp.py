@@ -1,13 +1,13 @@
 """numpy restatement of the learned-guess MLP (test infrastructure).
 
-Mirrors ugacc_gb300/csrc/mlp.cu: 12 features -> 256 -> 256 -> 1 with SiLU, parameters in
+Mirrors ugacc_gb300/csrc/mlp.cu: 15 features -> 256 -> 256 -> 1 with SiLU, parameters in
 the order W1[8][256] b1[256] W2[256][256] b2[256] w3[256] b3, mean-squared-error loss.
 The GPU stores the three weight matrices in FP16 for its forward and backward products
 (biases stay FP32), so the comparison rounds them the same way.
 """
 import numpy as np
 
-F, H = 12, 256
+F, H = 15, 256
 F_COUNT = F
 SIZES = [("W1", (F, H)), ("b1", (H,)), ("W2", (H, H)), ("b2", (H,)), ("w3", (H,)), ("b3", (1,))]
 
@@ -81,8 +81,9 @@ def features(no, nv, V):
     """Pair features of every T2 element (i, j, a, b), row-major, from the <pq|rs> blocks
     of `V` (a dict with "oovv", "oooo", "ovov", "vvvv" and "eps"): the MP2 amplitude and its
     exchange partner, the integral, -1/D, the mean occupied and virtual orbital energies,
-    the i == j and a == b flags, and the diagonal ladder and ring elements <ab|ab>, <ij|ij>,
-    <ia|ia> + <jb|jb>, <ia|ai> + <jb|bj>."""
+    the i == j and a == b flags, the diagonal ladder and ring elements <ab|ab>, <ij|ij>,
+    <ia|ia> + <jb|jb>, <ia|ai> + <jb|bj>, and the orbital-energy splittings |e_i - e_j|/2,
+    |e_a - e_b|/2, (e_i - e_j)(e_a - e_b)/4 (all invariant under (i,j,a,b) -> (j,i,b,a))."""
     eps = V["eps"]
     D = _denominators(no, nv, eps)
     Voovv, Voooo, Vovov, Vvvvv = V["oovv"], V["oooo"], V["ovov"], V["vvvv"]
@@ -101,6 +102,11 @@ def features(no, nv, V):
     F[..., 9] = SCALE * Voooo[i, j, i, j]
     F[..., 10] = SCALE * (Vovov[i, a, i, a] + Vovov[j, b, j, b])
     F[..., 11] = SCALE * (Voovv[i, i, a, a] + Voovv[j, j, b, b])
+    dij = eo[:, None, None, None] - eo[None, :, None, None]
+    dab = ev[None, None, :, None] - ev[None, None, None, :]
+    F[..., 12] = 0.5 * np.abs(dij)
+    F[..., 13] = 0.5 * np.abs(dab)
+    F[..., 14] = 0.25 * dij * dab
     return F.reshape(-1, F_COUNT)
 
 

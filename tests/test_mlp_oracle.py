@@ -39,3 +39,7 @@ def test_oracle_features_layout():
     assert np.isclose(F[r, 9], M.SCALE * ints[i, j, i, j])
     assert np.isclose(F[r, 10], M.SCALE * (ints[i, A, i, A] + ints[j, B, j, B]))
     assert np.isclose(F[r, 11], M.SCALE * (ints[i, i, A, A] + ints[j, j, B, B]))
+    assert np.isclose(F[r, 14], 0.25 * (h.eps[i] - h.eps[j]) * (h.eps[A] - h.eps[B]))
+    # invariance under the pair swap (i,j,a,b) -> (j,i,b,a)
+    rs = ((j * 3 + i) * 5 + b) * 5 + a
+    np.testing.assert_allclose(F[rs], F[r])

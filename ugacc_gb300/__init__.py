@@ -433,9 +433,9 @@ def _fptr(a: np.ndarray):
 
 
 class MLP:
-    """The guess network of mlp.cu: 12 pair features -> 256 -> 256 -> 1 (SiLU)."""
+    """The guess network of mlp.cu: 15 pair features -> 256 -> 256 -> 1 (SiLU)."""
 
-    NFEAT = 12
+    NFEAT = 15
 
     def __init__(self, device: int = 0, seed: int = 0):
         self.lib = load_library()

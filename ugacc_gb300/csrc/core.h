@@ -273,6 +273,10 @@ void lincomb(Ctx& c, int nvec, const double* const* d_vecs, const double* coef, 
 // (T) energy over a batch of (i>=j>=k) tuples, given W3 for each tuple.
 void triples_energy(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const double* W3,
                     const double* t1, const double* Voovv, const double* eps, double* d_partial);
+// The same from an FP32 W3 (mixed form): per-element arithmetic in FP32, the energy sum
+// in FP64 (compensated).
+void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, const double* t1,
+                        const double* Voovv, const double* eps, double* d_partial);
 
 int64_t launches();  // kernels launched by this library so far (all contexts)
 

@@ -626,7 +626,70 @@ __global__ void triples_energy_kernel(int no, int nv, const int* tuples, const d
   const double tot = block_sum(s + cc);
   if (threadIdx.x == 0) partial[(int64_t)t * nv + a] = tot;
 }
+
+// FP32 W3 (mixed form): the per-element V3/X3/Y3/Z3 algebra in FP32, the sum in FP64
+__global__ void triples_energy_f32_kernel(int no, int nv, const int* tuples, const float* W3, const double* t1,
+                                          const double* Voovv, const double* eps, double* partial) {
+  extern __shared__ float sh[];  // t1 rows i, j, k and the orbital energies of the virtuals
+  const int t = blockIdx.y;
+  const int a = blockIdx.x;
+  const int i = tuples[3 * t], j = tuples[3 * t + 1], k = tuples[3 * t + 2];
+  const int64_t nv2 = (int64_t)nv * nv;
+  float* s1i = sh;
+  float* s1j = sh + nv;
+  float* s1k = sh + 2 * nv;
+  float* sev = sh + 3 * nv;
+  for (int x = threadIdx.x; x < nv; x += blockDim.x) {
+    s1i[x] = (float)t1[(int64_t)i * nv + x];
+    s1j[x] = (float)t1[(int64_t)j * nv + x];
+    s1k[x] = (float)t1[(int64_t)k * nv + x];
+    sev[x] = (float)eps[no + x];
+  }
+  __syncthreads();
+  const float* W = W3 + (int64_t)t * nv2 * nv;
+  const double* Vij = Voovv + ((int64_t)i * no + j) * nv2;
+  const double* Vik = Voovv + ((int64_t)i * no + k) * nv2;
+  const double* Vjk = Voovv + ((int64_t)j * no + k) * nv2;
+  const float eijk = (float)(eps[i] + eps[j] + eps[k]);
+  const float fac = 2.0f - (float)((i == j) + (i == k) + (j == k));
+  const float inv[4] = {1.0f, 0.5f, 0.25f, 0.25f};  // 1 / (1 + #equal index pairs): 0, 1 or 3 pairs
+  double s = 0.0, cc = 0.0;
+  const int npair = (a + 1) * (a + 1);
+  for (int q = threadIdx.x; q < npair; q += blockDim.x) {
+    const int b = q / (a + 1), c = q % (a + 1);
+    if (c > b) continue;
+    auto Wv = [&](int x, int y, int z) { return W[(int64_t)x * nv2 + (int64_t)y * nv + z]; };
+    auto Vv = [&](int x, int y, int z) {
+      const float num = Wv(x, y, z) + (float)Vij[(int64_t)x * nv + y] * s1k[z] +
+                        (float)Vik[(int64_t)x * nv + z] * s1j[y] + (float)Vjk[(int64_t)y * nv + z] * s1i[x];
+      return num * inv[(x == y) + (x == z) + (y == z)];
+    };
+    const float wabc = Wv(a, b, c), wacb = Wv(a, c, b), wbac = Wv(b, a, c);
+    const float wbca = Wv(b, c, a), wcab = Wv(c, a, b), wcba = Wv(c, b, a);
+    const float vabc = Vv(a, b, c), vacb = Vv(a, c, b), vbac = Vv(b, a, c);
+    const float vbca = Vv(b, c, a), vcab = Vv(c, a, b), vcba = Vv(c, b, a);
+    const float X3 = wabc * vabc + wacb * vacb + wbac * vbac + wbca * vbca + wcab * vcab + wcba * vcba;
+    const float Y3 = vabc + vbca + vcab;
+    const float Z3 = vacb + vbac + vcba;
+    const float denom = eijk - (sev[a] + sev[b] + sev[c]);
+    const float e = ((Y3 - 2.0f * Z3) * (wabc + wbca + wcab) + (Z3 - 2.0f * Y3) * (wacb + wbac + wcba) + 3.0f * X3) *
+                    fac / denom;
+    neumaier(s, cc, (double)e);
+  }
+  const double tot = block_sum(s + cc);
+  if (threadIdx.x == 0) partial[(int64_t)t * nv + a] = tot;
+}
 }  // namespace
+
+void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, const double* t1,
+                        const double* Voovv, const double* eps, double* d_partial) {
+  UCC_REQUIRE(ntuple <= 65535, UCC_BAD_ARGS, "triples_energy: too many tuples per batch");
+  dim3 grid((unsigned)nv, (unsigned)ntuple);
+  triples_energy_f32_kernel<<<grid, 256, sizeof(float) * 4 * nv, c.stream>>>(no, nv, d_tuples, W3, t1, Voovv, eps,
+                                                                             d_partial);
+  count_launch();
+  check_launch("triples_energy_f32");
+}
 
 void triples_energy(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const double* W3, const double* t1,
                     const double* Voovv, const double* eps, double* d_partial) {

@@ -5,11 +5,14 @@
 // (ccwfn.cc:75-87 gives the MP2 guess t2 = <ij|ab>/D).  The plain CCSD iteration then
 // starts from t2 = t2_mp2 + prediction; its own convergence test decides the answer.
 //
-//   features (kFeat = 12), D = e_i + e_j - e_a - e_b, S = kScale:
+//   features (kFeat = 15), D = e_i + e_j - e_a - e_b, S = kScale:
 //     0: S*<ij|ab>/D   1: S*<ij|ba>/D   2: S*<ij|ab>   3: -1/D
 //     4: (e_i+e_j)/2   5: (e_a+e_b)/2   6: [i==j]      7: [a==b]
 //     8: S*<ab|ab>     9: S*<ij|ij>    10: S*(<ia|ia> + <jb|jb>)   11: S*(<ia|ai> + <jb|bj>)
-//   (8-11 are the diagonal ladder and ring elements that dress the MP2 denominator)
+//    12: |e_i-e_j|/2  13: |e_a-e_b|/2  14: (e_i-e_j)(e_a-e_b)/4
+//   (8-11 are the diagonal ladder and ring elements that dress the MP2 denominator; every
+//   feature is invariant under (i,j,a,b) -> (j,i,b,a), so the guess keeps the symmetry
+//   of the exact amplitudes)
 //   target: T*(t2_ccsd - t2_mp2),   T = kTarget
 //   network: 12 -> 256 -> 256 -> 1, SiLU; weights stored in FP16 for the forward and
 //   backward passes, FP32 master copies for the Adam update, FP32 accumulation.
@@ -31,7 +34,7 @@ void mlp_features(Ctx& c, float* out, size_t rows, float* targets, bool with_tar
 
 namespace mlp {
 
-constexpr int kFeat = 12, kHid = 256;
+constexpr int kFeat = 15, kHid = 256;
 constexpr double kScale = 100.0, kTarget = 1000.0;
 
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
@@ -191,6 +194,10 @@ __global__ void features_kernel(int no, int nv, const double* Voovv, const doubl
     f[9] = (float)(kScale * Voooo[((i * o + j) * o + i) * o + j]);                                // <ij|ij>
     f[10] = (float)(kScale * (Vovov[((i * v + a) * o + i) * v + a] + Vovov[((j * v + b) * o + j) * v + b]));
     f[11] = (float)(kScale * (Voovv[((i * o + i) * v + a) * v + a] + Voovv[((j * o + j) * v + b) * v + b]));
+    const double dij = eps[i] - eps[j], dab = eps[no + a] - eps[no + b];
+    f[12] = (float)(0.5 * fabs(dij));
+    f[13] = (float)(0.5 * fabs(dab));
+    f[14] = (float)(0.25 * dij * dab);
   }
 }
 // target = T * (t2 - t2_mp2)

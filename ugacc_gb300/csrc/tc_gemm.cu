@@ -59,6 +59,14 @@ struct Params {
   // split-K (single problem only): chunk z covers K blocks [z*kchunk, (z+1)*kchunk) of each
   // of the three split products and writes a plain [M][N] FP64 partial at C + z*M*N
   int ksplit, kchunk;
+  // nterms = 2 (batched problems only): a second product accumulated into the same tile,
+  // A from the second pair of tensor maps at rows a_row1[p], B at rows b_row1[p]
+  int nterms;
+  const int* a_row1;
+  const int* b_row1;
+  // C32 != null: FP32 output C32[off] = alpha * acc (+ C32[off] when beta != 0), no FP64
+  // work in the epilogue (GB300 issues ~4 FP64 operations per clock per SM)
+  float* C32;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -144,7 +152,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
 
 __global__ void __launch_bounds__(THREADS, 1)
     gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
-                const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo, Params p) {
+                const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
+                const __grid_constant__ CUtensorMap mA2hi, const __grid_constant__ CUtensorMap mA2lo, Params p) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = smem;
@@ -188,21 +197,24 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
         const int pb = tile / tiles_per, tl = tile - pb * tiles_per;
         const int mt = tl % p.mtiles, nt = tl / p.mtiles;
-        const int ar = (p.nprob ? p.a_row0[pb] : 0) + mt * BM, br = (p.nprob ? p.b_row0[pb] : 0) + nt * BN;
+        const int ar0 = (p.nprob ? p.a_row0[pb] : 0) + mt * BM, br0 = (p.nprob ? p.b_row0[pb] : 0) + nt * BN;
+        const int ar1 = p.nterms > 1 ? p.a_row1[pb] + mt * BM : 0, br1 = p.nterms > 1 ? p.b_row1[pb] + nt * BN : 0;
         int k0 = 0, kn = p.kblocks;
         if (p.ksplit > 1) {
           k0 = pb * p.kchunk;
           kn = min(p.kblocks - k0, p.kchunk);
         }
-        for (int kb = 0; kb < 3 * kn; kb++) {
+        for (int kb = 0; kb < p.nterms * 3 * kn; kb++) {
           if (!mbar_wait(&empty[stage], phase ^ 1u, p.err)) {
             ok = false;
             break;
           }
-          const int part = kb / kn, kk = (k0 + kb - part * kn) * BK;
+          const int term = kb / (3 * kn), w = kb - term * 3 * kn;
+          const int part = w / kn, kk = (k0 + w - part * kn) * BK;
+          const CUtensorMap* ma = term == 0 ? (part < 2 ? &mAhi : &mAlo) : (part < 2 ? &mA2hi : &mA2lo);
           mbar_expect_tx(&full[stage], A_BYTES + B_BYTES);
-          tma_load(sA + stage * A_BYTES, part < 2 ? &mAhi : &mAlo, &full[stage], kk, ar);
-          tma_load(sB + stage * B_BYTES, part == 1 ? &mBlo : &mBhi, &full[stage], kk, br);
+          tma_load(sA + stage * A_BYTES, ma, &full[stage], kk, term == 0 ? ar0 : ar1);
+          tma_load(sB + stage * B_BYTES, part == 1 ? &mBlo : &mBhi, &full[stage], kk, term == 0 ? br0 : br1);
           ++issued;
           if (++stage == STAGES) {
             stage = 0;
@@ -226,7 +238,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (!mbar_wait(&tempty[acc], aphase ^ 1u, p.err)) break;
         fence_after();
         const uint32_t d = tmem + (uint32_t)(acc * BN);
-        for (int kb = 0; kb < 3 * kn; kb++) {
+        for (int kb = 0; kb < p.nterms * 3 * kn; kb++) {
           if (!mbar_wait(&full[stage], phase, p.err)) {
             ok = false;
             break;
@@ -257,7 +269,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
       const int pb = tile / tiles_per, tl = tile - pb * tiles_per;
       const int mt = tl % p.mtiles, nt = tl / p.mtiles;
-      double* Cb = p.C + (p.nprob ? p.c_off[pb] : (p.ksplit > 1 ? (int64_t)pb * p.M * p.N : 0));
+      const int64_t coff = p.nprob ? p.c_off[pb] : (p.ksplit > 1 ? (int64_t)pb * p.M * p.N : 0);
       if (!mbar_wait(&tfull[acc], aphase, p.err)) break;
       fence_after();
       const int64_t m = (int64_t)mt * BM + q * 32 + lane;
@@ -268,13 +280,39 @@ __global__ void __launch_bounds__(THREADS, 1)
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + ch * 32), r);
         if (m < p.M) {
           const int64_t n0 = (int64_t)nt * BN + ch * 32;
+          if (p.C32) {
+            float* Cf = p.C32 + coff + mo;
+            const float af = (float)alpha;
 #pragma unroll
-          for (int j = 0; j < 32; j++) {
-            const int64_t n = n0 + j;
-            if (n < p.N) {
-              double* cp = Cb + mo + n * ep.s_n;
-              const double v = alpha * (double)__uint_as_float(r[j]);
-              *cp = (beta == 0.0) ? v : fma(beta, *cp, v);
+            for (int j = 0; j < 32; j++) {
+              const int64_t n = n0 + j;
+              if (n < p.N) {
+                float* cp = Cf + n * ep.s_n;
+                const float v = af * __uint_as_float(r[j]);
+                *cp = (beta == 0.0) ? v : *cp + v;
+              }
+            }
+          } else if (alpha == 1.0 && (beta == 0.0 || beta == 1.0)) {
+            double* Cb = p.C + coff + mo;
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+              const int64_t n = n0 + j;
+              if (n < p.N) {
+                double* cp = Cb + n * ep.s_n;
+                const double v = (double)__uint_as_float(r[j]);
+                *cp = (beta == 0.0) ? v : *cp + v;
+              }
+            }
+          } else {
+            double* Cb = p.C + coff + mo;
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+              const int64_t n = n0 + j;
+              if (n < p.N) {
+                double* cp = Cb + n * ep.s_n;
+                const double v = alpha * (double)__uint_as_float(r[j]);
+                *cp = (beta == 0.0) ? v : fma(beta, *cp, v);
+              }
             }
           }
         }
@@ -452,7 +490,10 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
   }
   const int grid = std::min(tiles * p.ksplit, k.sms);
   UCC_CUDA(cudaEventRecord(k.ev0, c.stream));
-  gemm_kernel<<<grid, THREADS, SMEM_BYTES, c.stream>>>(a->mhi, a->mlo, b->mhi, b->mlo, p);
+  p.nterms = 1;
+  p.a_row1 = p.b_row1 = nullptr;
+  p.C32 = nullptr;
+  gemm_kernel<<<grid, THREADS, SMEM_BYTES, c.stream>>>(a->mhi, a->mlo, b->mhi, b->mlo, a->mhi, a->mlo, p);
   count_kernel_launch();
   c.stats.tc_gemm_launches++;
   UCC_CUDA(cudaGetLastError());
@@ -508,15 +549,18 @@ bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const dou
 // batch is one batched launch whose problems are the tuples of the batch.
 // ------------------------------------------------------------------------------------
 namespace tc {
-// dst[(row0 + r) * ld + col0 + k] (hi/lo) = scale * src[r*sr + k*sk], r < rows, k < cols;
-// 32x32 tiles through shared memory so that the destination rows are written coalesced
-__global__ void split_into_kernel(int64_t rows, int64_t cols, const double* src, int64_t sr, int64_t sk, double scale,
-                                  __nv_bfloat16* hi, __nv_bfloat16* lo, int64_t ld, int64_t row0, int64_t col0) {
+// dst[(row0 + r) * ld + col0 + k] (hi/lo) = scale * src[(r / rsplit) * sr_hi + (r % rsplit) * sr + k*sk],
+// r < rows, k < cols; 32x32 tiles through shared memory so that the destination rows are
+// written coalesced
+__global__ void split_into_kernel(int64_t rows, int64_t cols, const double* src, int64_t rsplit, int64_t sr_hi,
+                                  int64_t sr, int64_t sk, double scale, __nv_bfloat16* hi, __nv_bfloat16* lo,
+                                  int64_t ld, int64_t row0, int64_t col0) {
   __shared__ double t[32][33];
   const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
   for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
     const int64_t r = r0 + threadIdx.x, k = k0 + yy;
-    t[yy][threadIdx.x] = (r < rows && k < cols) ? scale * src[r * sr + k * sk] : 0.0;
+    t[yy][threadIdx.x] =
+        (r < rows && k < cols) ? scale * src[(r / rsplit) * sr_hi + (r % rsplit) * sr + k * sk] : 0.0;
   }
   __syncthreads();
   for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
@@ -532,7 +576,7 @@ __global__ void split_into_kernel(int64_t rows, int64_t cols, const double* src,
 }
 
 struct Triples {
-  Split A, B;
+  Split A, A2, B;  // A2: A with its (a,b) row pairs in (b,a) order
   int* d_arow = nullptr;
   int* d_brow = nullptr;
   int64_t* d_coff = nullptr;
@@ -544,11 +588,12 @@ struct Triples {
 };
 
 static void split_into(Ctx& c, int64_t rows, int64_t cols, const double* src, int64_t sr, int64_t sk, double scale,
-                       Split& dst, int64_t row0, int64_t col0) {
+                       Split& dst, int64_t row0, int64_t col0, int64_t rsplit = 0, int64_t sr_hi = 0) {
   dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
   UCC_REQUIRE(grid.y <= 65535, UCC_BAD_ARGS, "split_into: too many rows");
-  split_into_kernel<<<grid, dim3(32, 8), 0, c.stream>>>(rows, cols, src, sr, sk, scale, dst.hi, dst.lo, dst.kp, row0,
-                                                        col0);
+  if (rsplit <= 0) rsplit = rows;  // one level: r * sr
+  split_into_kernel<<<grid, dim3(32, 8), 0, c.stream>>>(rows, cols, src, rsplit, sr_hi, sr, sk, scale, dst.hi, dst.lo,
+                                                        dst.kp, row0, col0);
   count_kernel_launch();
   UCC_CUDA(cudaGetLastError());
 }
@@ -570,6 +615,7 @@ bool mixed_triples_prepare(Ctx& c, int max_batch) {
   Cache& k = cache(c);
   auto T = std::make_shared<Triples>();
   alloc_split(T->A, no * nv2, kp, c.stream);
+  alloc_split(T->A2, no * nv2, kp, c.stream);
   alloc_split(T->B, no * no * nv, kp, c.stream);
   const double* t2 = c.get("T").p + no * nv;
   const double* Vovvv = c.get("Vovvv").p;
@@ -577,6 +623,9 @@ bool mixed_triples_prepare(Ctx& c, int max_batch) {
   for (int64_t x = 0; x < no; x++) {
     split_into(c, nv2, nv, Vovvv + x * nv * nv2, 1, nv2, 1.0, T->A, x * nv2, 0);   // <xe|ab>
     split_into(c, nv2, no, t2 + x * no * nv2, 1, nv2, -1.0, T->A, x * nv2, nv);   // -t2[x][m][a][b]
+    // the same rows in (b,a) order: row b*nv + a
+    split_into(c, nv2, nv, Vovvv + x * nv * nv2, nv, nv2, 1.0, T->A2, x * nv2, 0, nv, 1);
+    split_into(c, nv2, no, t2 + x * no * nv2, nv, nv2, -1.0, T->A2, x * nv2, nv, nv, 1);
   }
   split_into(c, no * no * nv, nv, t2, nv, 1, 1.0, T->B, 0, 0);  // t2[y][z][c][e]
   for (int64_t y = 0; y < no; y++)
@@ -584,10 +633,12 @@ bool mixed_triples_prepare(Ctx& c, int max_batch) {
       split_into(c, nv, no, Vooov + (z * no + y) * no * nv, 1, nv, 1.0, T->B, (y * no + z) * nv, nv);
   make_map(&T->A.mhi, T->A.hi, T->A.rows, kp, BM);
   make_map(&T->A.mlo, T->A.lo, T->A.rows, kp, BM);
+  make_map(&T->A2.mhi, T->A2.hi, T->A2.rows, kp, BM);
+  make_map(&T->A2.mlo, T->A2.lo, T->A2.rows, kp, BM);
   make_map(&T->B.mhi, T->B.hi, T->B.rows, kp, BN);
   make_map(&T->B.mlo, T->B.lo, T->B.rows, kp, BN);
-  UCC_CUDA(cudaMalloc(&T->d_arow, sizeof(int) * max_batch));
-  UCC_CUDA(cudaMalloc(&T->d_brow, sizeof(int) * max_batch));
+  UCC_CUDA(cudaMalloc(&T->d_arow, sizeof(int) * 2 * max_batch));
+  UCC_CUDA(cudaMalloc(&T->d_brow, sizeof(int) * 2 * max_batch));
   UCC_CUDA(cudaMalloc(&T->d_coff, sizeof(int64_t) * max_batch));
   k.triples = T;
   if (!k.attr_set) {
@@ -602,25 +653,34 @@ void mixed_triples_release(Ctx& c) {
   tc::cache(c).triples.reset();
 }
 
-bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, double* W3) {
+bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, float* W3) {
   using namespace tc;
   Cache& k = cache(c);
   Triples& T = *k.triples;
   const int64_t no = c.no, nv = c.nv, nv2 = nv * nv, nv3 = nv2 * nv;
   TriplesTerm terms[6];
   triples_terms(nv, terms);
-  std::vector<int> arow(nb), brow(nb);
+  // The six terms in pairs that write the same W3 layout: the first term of a pair uses
+  // A's natural (a,b) rows, the second the (b,a) copy, so that one tile accumulates both
+  // in tensor memory; every pair's fastest-varying output row index has W3 stride 1 or
+  // its column index does.
+  const int pairs[3][2] = {{0, 5}, {1, 2}, {4, 3}};
+  std::vector<int> arow(2 * nb), brow(2 * nb);
   std::vector<int64_t> coff(nb);
   for (int b = 0; b < nb; b++) coff[b] = b * nv3;
   UCC_CUDA(cudaMemcpyAsync(T.d_coff, coff.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice, c.stream));
-  for (int q = 0; q < 6; q++) {
-    for (int b = 0; b < nb; b++) {
-      const int* ijk = tuples + 3 * b;
-      arow[b] = (int)(ijk[terms[q].x] * nv2);
-      brow[b] = (int)((ijk[terms[q].y] * no + ijk[terms[q].z]) * nv);
+  for (int pq = 0; pq < 3; pq++) {
+    for (int t = 0; t < 2; t++) {
+      const TriplesTerm& tm = terms[pairs[pq][t]];
+      for (int b = 0; b < nb; b++) {
+        const int* ijk = tuples + 3 * b;
+        arow[t * nb + b] = (int)(ijk[tm.x] * nv2);
+        brow[t * nb + b] = (int)((ijk[tm.y] * no + ijk[tm.z]) * nv);
+      }
     }
-    UCC_CUDA(cudaMemcpyAsync(T.d_arow, arow.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c.stream));
-    UCC_CUDA(cudaMemcpyAsync(T.d_brow, brow.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c.stream));
+    UCC_CUDA(cudaMemcpyAsync(T.d_arow, arow.data(), sizeof(int) * 2 * nb, cudaMemcpyHostToDevice, c.stream));
+    UCC_CUDA(cudaMemcpyAsync(T.d_brow, brow.data(), sizeof(int) * 2 * nb, cudaMemcpyHostToDevice, c.stream));
+    const TriplesTerm& t0 = terms[pairs[pq][0]];
     Params p;
     p.M = (int)nv2;
     p.N = (int)nv;
@@ -628,12 +688,13 @@ bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, double* W3) {
     p.mtiles = (int)((nv2 + BM - 1) / BM);
     p.ntiles = (int)((nv + BN - 1) / BN);
     p.alpha = 1.0;
-    p.beta = q == 0 ? 0.0 : 1.0;
-    p.C = W3;
+    p.beta = pq == 0 ? 0.0 : 1.0;
+    p.C = nullptr;
+    p.C32 = W3;  // W3 in FP32: its rounding (~6e-8) is far below the split products' (~5e-6)
     p.epi.msplit = nv;
-    p.epi.s_mhi = terms[q].su;
-    p.epi.s_mlo = terms[q].sv;
-    p.epi.s_n = terms[q].sw;
+    p.epi.s_mhi = t0.su;
+    p.epi.s_mlo = t0.sv;
+    p.epi.s_n = t0.sw;
     p.err = k.err;
     p.nprob = nb;
     p.ksplit = 1;
@@ -641,19 +702,23 @@ bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, double* W3) {
     p.a_row0 = T.d_arow;
     p.b_row0 = T.d_brow;
     p.c_off = T.d_coff;
+    p.nterms = 2;
+    p.a_row1 = T.d_arow + nb;
+    p.b_row1 = T.d_brow + nb;
     const int tiles = p.mtiles * p.ntiles * nb;
     UCC_CUDA(cudaEventRecord(k.ev0, c.stream));
-    gemm_kernel<<<std::min(tiles, k.sms), THREADS, SMEM_BYTES, c.stream>>>(T.A.mhi, T.A.mlo, T.B.mhi, T.B.mlo, p);
+    gemm_kernel<<<std::min(tiles, k.sms), THREADS, SMEM_BYTES, c.stream>>>(T.A.mhi, T.A.mlo, T.B.mhi, T.B.mlo,
+                                                                          T.A2.mhi, T.A2.mlo, p);
     count_kernel_launch();
     c.stats.tc_gemm_launches++;
     UCC_CUDA(cudaGetLastError());
     UCC_CUDA(cudaEventRecord(k.ev1, c.stream));
-    // the row tables are rewritten for the next term: keep the copies ordered after use
+    // the row tables are rewritten for the next pair: keep the copies ordered after use
     UCC_CUDA(cudaStreamSynchronize(c.stream));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, k.ev0, k.ev1);
     c.stats.tc_gemm_ms += ms;
-    c.stats.tc_gemm_flops += 2.0 * (double)nv2 * (double)nv * (double)(nv + no) * nb;
+    c.stats.tc_gemm_flops += 2.0 * 2.0 * (double)nv2 * (double)nv * (double)(nv + no) * nb;
   }
   int herr = 0;
   UCC_CUDA(cudaMemcpy(&herr, k.err, sizeof(int), cudaMemcpyDeviceToHost));

@@ -20,7 +20,7 @@ namespace ucc {
 double flops_triples(double no, double nv) { return 2.0 * no * (no + 1) * (no + 2) * nv * nv * nv * (nv + no); }
 
 // mixed-precision tuple GEMMs (tc_gemm.cu); false if not available for this shape
-bool mixed_triples_batch(Ctx& c, int nbatch, const int* h_tuples, double* W3);
+bool mixed_triples_batch(Ctx& c, int nbatch, const int* h_tuples, float* W3);
 bool mixed_triples_prepare(Ctx& c, int max_batch);
 void mixed_triples_release(Ctx& c);
 
@@ -70,7 +70,7 @@ double run_triples(Ctx& c) {
   for (int t0 = 0; t0 < ntup; t0 += batch) {
     const int nb = std::min(batch, ntup - t0);
     if (mixed) {
-      mixed_triples_batch(c, nb, tuples.data() + 3 * t0, W3.d());
+      mixed_triples_batch(c, nb, tuples.data() + 3 * t0, static_cast<float*>(W3.p));
     } else {
       std::vector<GemmPtrs> all((size_t)nb * 6);
       for (int q = 0; q < 6; q++)
@@ -94,8 +94,12 @@ double run_triples(Ctx& c) {
       // the pointer array is reused by the next batch: keep the copy ordered after use
       UCC_CUDA(cudaStreamSynchronize(c.stream));
     }
-    triples_energy(c, no, nv, nb, static_cast<int*>(dtup.p) + 3 * t0, W3.d(), t1.p, c.get("Voovv").p,
-                   c.get("eps").p, partial.d() + (int64_t)t0 * nv);
+    if (mixed)
+      triples_energy_f32(c, no, nv, nb, static_cast<int*>(dtup.p) + 3 * t0, static_cast<const float*>(W3.p), t1.p,
+                         c.get("Voovv").p, c.get("eps").p, partial.d() + (int64_t)t0 * nv);
+    else
+      triples_energy(c, no, nv, nb, static_cast<int*>(dtup.p) + 3 * t0, W3.d(), t1.p, c.get("Voovv").p,
+                     c.get("eps").p, partial.d() + (int64_t)t0 * nv);
   }
   Scratch et(c, sizeof(double));
   dot_async(c, (int64_t)ntup * nv, partial.d(), nullptr, et.d());

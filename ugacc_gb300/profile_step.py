@@ -58,12 +58,16 @@ def main(argv=None):
     if a.triples:
         cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": "FP64" if a.ccsd_fp64 else prec, "PRINT": int(a.print),
                          "MIXED_SWITCH": a.switch})
-        cc.compute_energy()
+        e_cc = cc.compute_energy()
+        st_cc = H.ctx.stats()
         if a.ccsd_fp64:
             cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": prec})
         H.ctx.reset_stats()
         e_t = cc.triples()
-        print(json.dumps({"e_t": e_t}))
+        print(json.dumps({"e_ccsd": e_cc, "e_t": e_t, "ccsd_ms": st_cc["ccsd_ms"],
+                          "ccsd_iterations": st_cc["ccsd_iterations"], "fp64_iterations": st_cc["fp64_iterations"],
+                          "mixed_iterations": st_cc["mixed_iterations"],
+                          "anchored_iterations": st_cc["anchored_iterations"]}))
     print(json.dumps(H.ctx.stats()))
     return 0
 
