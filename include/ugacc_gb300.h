@@ -196,6 +196,9 @@ typedef struct ucc_stats {
   double tc_gemm_ms;         /* device time of the tensor-core GEMMs (CUDA events) */
   double tc_gemm_flops;      /* their algorithmic FLOPs, 2*M*N*K per GEMM */
   int anchored_iterations;   /* refinement iterations built as FP64 anchor + tensor-core corrections */
+  double fp64_gemm_ms;       /* device time of the FP64 GEMM launches (CUDA events) */
+  double fp64_gemm_flops;    /* their algorithmic FLOPs, 2*M*N*K per GEMM */
+  int64_t fp64_gemm_launches;
 } ucc_stats;
 ucc_status ucc_get_stats(ucc_ctx* ctx, ucc_stats* out);
 ucc_status ucc_reset_stats(ucc_ctx* ctx);

@@ -53,7 +53,8 @@ class Stats(ctypes.Structure):
                 ("ladder_launches", ctypes.c_int64), ("fp64_iterations", ctypes.c_int),
                 ("tc_gemm_launches", ctypes.c_int64), ("mixed_iterations", ctypes.c_int),
                 ("tc_gemm_ms", ctypes.c_double), ("tc_gemm_flops", ctypes.c_double),
-                ("anchored_iterations", ctypes.c_int)]
+                ("anchored_iterations", ctypes.c_int), ("fp64_gemm_ms", ctypes.c_double),
+                ("fp64_gemm_flops", ctypes.c_double), ("fp64_gemm_launches", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -21,6 +21,11 @@ Ctx& ctx_of(ucc_ctx* h) { return h->c; }
 
 Ctx::~Ctx() {
   if (stream) cudaStreamSynchronize(stream);
+  for (auto& t : gemm_timers) {
+    cudaEventDestroy(t.a);
+    cudaEventDestroy(t.b);
+  }
+  for (auto e : event_pool) cudaEventDestroy(e);
   tc_cache.reset();
   perts.clear();
   store.clear();
@@ -335,12 +340,18 @@ ucc_status ucc_set_tensor(ucc_ctx* ctx, const char* name, const double* in, size
 ucc_status ucc_get_stats(ucc_ctx* ctx, ucc_stats* out) {
   return guard(ctx, [&](Ctx& c) {
     UCC_REQUIRE(out, UCC_BAD_ARGS, "null output");
+    UCC_CUDA(cudaSetDevice(c.device));
+    c.resolve_timers();
     *out = c.stats;
   });
 }
 
 ucc_status ucc_reset_stats(ucc_ctx* ctx) {
-  return guard(ctx, [&](Ctx& c) { c.stats = ucc_stats{}; });
+  return guard(ctx, [&](Ctx& c) {
+    UCC_CUDA(cudaSetDevice(c.device));
+    c.resolve_timers();
+    c.stats = ucc_stats{};
+  });
 }
 
 }  // extern "C"

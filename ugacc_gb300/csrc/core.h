@@ -170,6 +170,16 @@ struct Ctx {
   std::vector<std::unique_ptr<Perturbation>> perts;
   ucc_stats stats{};
 
+  // CUDA-event timing of FP64 GEMM launches, resolved into stats lazily
+  struct TimedLaunch {
+    cudaEvent_t a, b;
+    double flops;
+  };
+  std::vector<TimedLaunch> gemm_timers;
+  std::vector<cudaEvent_t> event_pool;
+  cudaEvent_t take_event();
+  void resolve_timers();  // synchronises the stream
+
   ~Ctx();
 };
 

@@ -142,6 +142,32 @@ Fp64Scope::~Fp64Scope() { c.force_fp64 = saved; }
 PrecisionScope::PrecisionScope(Ctx& ctx, bool f) : c(ctx), saved(ctx.force_fp64) { c.force_fp64 = f; }
 PrecisionScope::~PrecisionScope() { c.force_fp64 = saved; }
 
+cudaEvent_t Ctx::take_event() {
+  if (!event_pool.empty()) {
+    cudaEvent_t e = event_pool.back();
+    event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  UCC_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+void Ctx::resolve_timers() {
+  if (gemm_timers.empty()) return;
+  UCC_CUDA(cudaStreamSynchronize(stream));
+  for (auto& t : gemm_timers) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t.a, t.b);
+    stats.fp64_gemm_ms += ms;
+    stats.fp64_gemm_flops += t.flops;
+    stats.fp64_gemm_launches++;
+    event_pool.push_back(t.a);
+    event_pool.push_back(t.b);
+  }
+  gemm_timers.clear();
+}
+
 bool Ctx::is_constant(const double* p) const {
   for (const auto& kv : store) {
     const std::string& n = kv.first;

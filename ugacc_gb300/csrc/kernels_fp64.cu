@@ -192,6 +192,8 @@ void dgemm_strided(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const 
   }
   const bool ak = (sAk == 1) || (sAm != 1 && sAk < sAm);
   const bool bn = (sBn == 1) || (sBk != 1 && sBn < sBk);
+  cudaEvent_t ev0 = c.take_event(), ev1 = c.take_event();
+  cudaEventRecord(ev0, c.stream);
   if (ak && bn)
     dgemm_kernel<true, true><<<grid, GT, 0, c.stream>>>(g);
   else if (ak)
@@ -203,6 +205,9 @@ void dgemm_strided(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const 
   count_launch();
   check_launch("dgemm");
   if (part) splitk_reduce(c, M, N, nsplit, part->d(), alpha, beta, C, epi);
+  cudaEventRecord(ev1, c.stream);
+  c.gemm_timers.push_back({ev0, ev1, 2.0 * (double)M * (double)N * (double)K * (double)batch});
+  if (c.gemm_timers.size() >= 4096) c.resolve_timers();
 }
 
 void splitk_reduce(Ctx& c, int64_t M, int64_t N, int nsplit, const double* P, double alpha, double beta, double* C,

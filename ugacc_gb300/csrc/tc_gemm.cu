@@ -280,29 +280,26 @@ __global__ void __launch_bounds__(THREADS, 1)
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + ch * 32), r);
         if (m < p.M) {
           const int64_t n0 = (int64_t)nt * BN + ch * 32;
+          // with beta != 0 all 32 old values are loaded before the first store, so the
+          // loads are in flight together instead of each waiting behind a store that
+          // might alias it
           if (p.C32) {
             float* Cf = p.C32 + coff + mo;
             const float af = (float)alpha;
+            float old[32];
 #pragma unroll
-            for (int j = 0; j < 32; j++) {
-              const int64_t n = n0 + j;
-              if (n < p.N) {
-                float* cp = Cf + n * ep.s_n;
-                const float v = af * __uint_as_float(r[j]);
-                *cp = (beta == 0.0) ? v : *cp + v;
-              }
-            }
+            for (int j = 0; j < 32; j++) old[j] = (beta != 0.0 && n0 + j < p.N) ? Cf[(n0 + j) * ep.s_n] : 0.f;
+#pragma unroll
+            for (int j = 0; j < 32; j++)
+              if (n0 + j < p.N) Cf[(n0 + j) * ep.s_n] = fmaf(af, __uint_as_float(r[j]), old[j]);
           } else if (alpha == 1.0 && (beta == 0.0 || beta == 1.0)) {
             double* Cb = p.C + coff + mo;
+            double old[32];
 #pragma unroll
-            for (int j = 0; j < 32; j++) {
-              const int64_t n = n0 + j;
-              if (n < p.N) {
-                double* cp = Cb + n * ep.s_n;
-                const double v = (double)__uint_as_float(r[j]);
-                *cp = (beta == 0.0) ? v : *cp + v;
-              }
-            }
+            for (int j = 0; j < 32; j++) old[j] = (beta != 0.0 && n0 + j < p.N) ? Cb[(n0 + j) * ep.s_n] : 0.0;
+#pragma unroll
+            for (int j = 0; j < 32; j++)
+              if (n0 + j < p.N) Cb[(n0 + j) * ep.s_n] = old[j] + (double)__uint_as_float(r[j]);
           } else {
             double* Cb = p.C + coff + mo;
 #pragma unroll
