@@ -66,3 +66,30 @@ def test_mixed_triples_matches_fp64():
     assert H.ctx.stats()["tc_gemm_launches"] == 3  # one batched launch per pair of W3 terms
     # split products carry ~2^-16 relative error into W3; E(T) is a weighted sum of W3*V3
     assert abs(emx - e64) < 1e-8 + 1e-4 * abs(e64)
+
+
+def _lambda_response(h, precision, hand):
+    from ugacc_gb300.generator import make_perturbations
+    H = U.Hamiltonian.from_synthetic(h)
+    cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": precision})
+    cc.compute_energy()
+    hb = U.HBAR(H, cc)
+    lam = U.CCLambda(cc, hb)
+    lam.compute_lambda()
+    pseudo = lam.pseudoenergy()
+    mu = U.CCPert(make_perturbations(h.nact, h.seed)[0], 0.0656, cc, hb, lam)
+    mu.solve("right")
+    if hand == "left":
+        mu.solve("left")
+    a = U.CCResp(mu, mu).linresp(mu, mu)
+    return pseudo, a, H.ctx.stats()
+
+
+@pytest.mark.parametrize("hand", ["right", "left"])
+def test_mixed_lambda_and_response_match_fp64(hand):
+    h = make_hamiltonian(10, 64, 12)
+    p64, a64, _ = _lambda_response(h, "FP64", hand)
+    pmx, amx, st = _lambda_response(h, "MIXED", hand)
+    assert st["tc_gemm_launches"] > 0
+    assert abs(pmx - p64) < 1e-9
+    assert abs(amx - a64) < 1e-8 * max(1.0, abs(a64))

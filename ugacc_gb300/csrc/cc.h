@@ -46,6 +46,36 @@ class Diis {
 // Solve B x = rhs for the bordered DIIS system (same elimination as the oracle's shim).
 std::vector<double> diis_coefficients(const std::vector<double>& Bfull, int n);
 
+// ---- mixed-precision sweep policy (shared by the CCSD, Lambda and perturbed solves) ----
+// split  - residual from BF16 hi+lo split GEMMs, until the residual norm reaches the
+//          split-product noise floor (or stops falling);
+// record - FP64 residual that also records every heavy GEMM as an anchor;
+// delta  - FP64 residual whose heavy GEMMs are anchor + tensor-core corrections.
+// The solve ends only on a record sweep with ||R|| < r_convergence (and at least
+// refine_sweeps record sweeps); a delta sweep that gets there, or stalls, asks for one.
+// With precision FP64 every sweep is plain FP64.
+class MixedSweeps {
+ public:
+  enum Kind { kFp64, kSplit, kRecord, kDelta };
+  explicit MixedSweeps(Ctx& c);
+  ~MixedSweeps();
+  Kind begin();  // kind of the coming sweep, anchors armed for it
+  void end();    // anchors disarmed (call before the Jacobi update)
+  // after the sweep's residual norm: true when the solve has converged; *restart_diis is
+  // set when the DIIS history must start again (this sweep's vector is not added)
+  bool after(double rms, bool* restart_diis);
+  bool mixed() const { return mixed_; }
+  Kind kind() const { return kind_; }
+  int split = 0, record = 0, delta = 0;
+
+ private:
+  Ctx& c_;
+  bool mixed_, refine_, split_phase_, record_next_ = true;
+  int stalls_ = 0, sweeps_ = 0;
+  double rms_prev_ = INFINITY;
+  Kind kind_ = kFp64;
+};
+
 // ---- solver stages ---------------------------------------------------------------------
 struct CCSDResult {
   double e_ccsd = 0.0, e_mp2 = 0.0;

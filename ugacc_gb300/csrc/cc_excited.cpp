@@ -201,7 +201,7 @@ void lambda_l2(Ctx& c, const Tensor& l1, const Tensor& l2, const Tensor& Goo, co
 
 CCSDResult run_lambda(Ctx& c) {  // :93-129
   UCC_REQUIRE(c.have_hbar, UCC_BAD_STATE, "Lambda needs HBAR");
-  Fp64Scope fp64(c);
+  Fp64Scope fp64(c);  // everything outside the residual build
   const int no = c.no, nv = c.nv;
   const int64_t np = npacked(c), n1 = (int64_t)no * nv;
   Tensor Lam = c.alloc("Lam", {np}, false);
@@ -230,6 +230,8 @@ CCSDResult run_lambda(Ctx& c) {  // :93-129
     std::printf("\t  %3d  %20.15f\n", 0, pseudo(Lam.p));
   }
   double rms = INFINITY;
+  bool converged = false;
+  MixedSweeps sw(c);  // MIXED: split, record and delta sweeps; l2 is symmetrised by construction
   int iter;
   for (iter = 1; iter <= c.opt.maxiter; iter++) {
     c.store["Lam"].swap(c.store["Lamold"]);
@@ -237,25 +239,38 @@ CCSDResult run_lambda(Ctx& c) {  // :93-129
     double* ln = c.get("Lam").p;
     double* r = c.get("LR").p;
     Tensor l1 = amp1(c, lo), l2 = amp2(c, lo);
-    lambda_G(c, t2, l2, Goo, Gvv);
-    lambda_l1(c, l1, l2, Goo, Gvv, amp1(c, r));
-    lambda_l2(c, l1, l2, Goo, Gvv, amp2(c, r));
+    const MixedSweeps::Kind kind = sw.begin();
+    {
+      PrecisionScope scope(c, kind != MixedSweeps::kSplit);
+      lambda_G(c, t2, l2, Goo, Gvv);
+      lambda_l1(c, l1, l2, Goo, Gvv, amp1(c, r));
+      lambda_l2(c, l1, l2, Goo, Gvv, amp2(c, r));
+    }
+    sw.end();
     jacobi_update(c, no, nv, eps.p, eps.p + no, 0.0, r, r + n1, lo, lo + n1, ln, ln + n1, sumsq.d());
     double ss = 0.0;
     UCC_CUDA(cudaMemcpyAsync(&ss, sumsq.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     UCC_CUDA(cudaStreamSynchronize(c.stream));
     rms = std::sqrt(ss);
     UCC_REQUIRE(std::isfinite(rms), UCC_NAN_DETECTED, "Lambda residual is not finite");
-    if (rms < c.opt.r_convergence) break;
-    if (c.opt.diis) {
+    bool restart = false;
+    if (sw.after(rms, &restart)) {
+      converged = true;
+      break;
+    }
+    if (restart) diis.reset();
+    if (c.opt.diis && !restart) {
       diis.add(ln, lo);
       if (diis.size() > 2) diis.extrapolate(ln);
     }
-    if (c.opt.print) std::printf("\t  %3d  %20.15f  %5.3e\n", iter, pseudo(ln), rms);
+    if (c.opt.print) {
+      static const char* tag[] = {"", " split", " record", " delta"};
+      std::printf("\t  %3d  %20.15f  %5.3e%s\n", iter, pseudo(ln), rms, tag[kind]);
+    }
   }
   CCSDResult res;
   res.iterations = std::min(iter, c.opt.maxiter);
-  res.converged = rms < c.opt.r_convergence;
+  res.converged = converged;
   res.e_ccsd = pseudo(c.get("Lam").p);
   c.have_lambda = res.converged;
   return res;

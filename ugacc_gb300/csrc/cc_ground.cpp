@@ -419,6 +419,61 @@ double ccsd_energy(Ctx& c, const double* t) { return energy(c, amp1(c, const_cas
 // resolving the update (measured ~1.5e-6 at no=16/nv=160)
 constexpr double kMixedFloor = 2e-6;
 
+MixedSweeps::MixedSweeps(Ctx& c)
+    : c_(c),
+      mixed_(c.opt.precision == UCC_MIXED),
+      refine_(c.opt.precision == UCC_MIXED && c.opt.refine_sweeps > 0),
+      split_phase_(c.opt.precision == UCC_MIXED) {
+  c_.anchors.clear();
+}
+
+MixedSweeps::~MixedSweeps() { c_.anchors.clear(); }
+
+MixedSweeps::Kind MixedSweeps::begin() {
+  kind_ = !mixed_ ? kFp64 : split_phase_ ? kSplit : record_next_ ? kRecord : kDelta;
+  if (kind_ == kRecord) c_.anchors.begin(1);
+  if (kind_ == kDelta) c_.anchors.begin(2);
+  return kind_;
+}
+
+void MixedSweeps::end() { c_.anchors.mode = 0; }
+
+bool MixedSweeps::after(double rms, bool* restart_diis) {
+  *restart_diis = false;
+  sweeps_++;
+  const double rc = c_.opt.r_convergence;
+  bool done = false;
+  if (kind_ == kFp64) {
+    done = rms < rc;
+  } else if (kind_ == kSplit) {
+    split++;
+    if (!refine_ && rms < rc) done = true;
+    // hand over near the split-product noise floor or when the residual stops falling
+    if (!done && refine_ &&
+        (rms < std::max(rc, std::max(c_.opt.mixed_switch, kMixedFloor)) || (sweeps_ > 2 && rms > 0.5 * rms_prev_))) {
+      split_phase_ = false;
+      record_next_ = true;
+      *restart_diis = true;  // the split-sweep history extrapolates a different map
+    }
+  } else if (kind_ == kRecord) {
+    record++;
+    record_next_ = false;
+    stalls_ = 0;
+    done = rms < rc && record >= c_.opt.refine_sweeps;
+  } else {
+    delta++;
+    if (rms < rc) {
+      record_next_ = true;  // confirm with an FP64 residual
+    } else if (rms > 0.7 * rms_prev_) {
+      if (++stalls_ >= 2) record_next_ = true;  // corrections no longer resolved: re-anchor
+    } else {
+      stalls_ = 0;
+    }
+  }
+  rms_prev_ = rms;
+  return done;
+}
+
 CCSDResult run_ccsd(Ctx& c) {
   UCC_REQUIRE(c.loaded, UCC_BAD_STATE, "no Hamiltonian loaded");
   const int no = c.no, nv = c.nv;
@@ -457,39 +512,27 @@ CCSDResult run_ccsd(Ctx& c) {
   }
   Diis diis(c, np, 8);
   std::vector<cudaEvent_t> ev;
-  double rms = INFINITY, rms_prev = INFINITY, eccsd = NAN;
-  // Mixed precision (three kinds of sweep):
-  //  split  - residual from BF16 hi+lo split GEMMs, until the residual norm reaches the
-  //           split-product noise floor (or stops falling);
-  //  record - FP64 residual that also records every heavy GEMM as an anchor;
-  //  delta  - FP64 residual whose heavy GEMMs are anchor + tensor-core corrections.
-  // The solve ends only on a record sweep with ||R|| < r_convergence (and at least
-  // refine_sweeps record sweeps); a delta sweep that gets there, or stalls, asks for one.
-  enum Sweep { kFp64, kSplit, kRecord, kDelta };
-  const bool mixed = c.opt.precision == UCC_MIXED;
-  const bool refine = mixed && c.opt.refine_sweeps > 0;
-  bool split_phase = mixed, record_next = true;
-  int stalls = 0, record_sweeps = 0, delta_sweeps = 0, split_sweeps = 0;
+  double rms = INFINITY, eccsd = NAN;
+  MixedSweeps sw(c);  // mixed precision: split, record and delta sweeps (cc.h)
+  const bool mixed = sw.mixed();
+  bool converged = false;
   int iter = 0;
-  c.anchors.clear();
   for (iter = 1; iter <= c.opt.maxiter; iter++) {
     c.store["T"].swap(c.store["Told"]);  // amp_save, ccwfn.cc:300-309
     double* to = c.get("Told").p;
     double* tn = c.get("T").p;
     double* r = c.get("R").p;
     Tensor t1 = amp1(c, to), t2 = amp2(c, to);
-    const Sweep kind = !mixed ? kFp64 : split_phase ? kSplit : record_next ? kRecord : kDelta;
+    const MixedSweeps::Kind kind = sw.begin();
     {
-      Fp64Scope scope(c, kind != kSplit);
-      if (kind == kRecord) c.anchors.begin(1);
-      if (kind == kDelta) c.anchors.begin(2);
+      Fp64Scope scope(c, kind != MixedSweeps::kSplit);
       build_F(c, t1, c.get("ttau"));
       build_W(c, t1, t2, c.get("tau"));
       build_t1(c, t1, t2, amp1(c, r));
       build_t2(c, t1, t2, c.get("tau"), amp2(c, r), &ev);
-      c.anchors.mode = 0;
     }
-    if (kind == kSplit || kind == kDelta) {
+    sw.end();
+    if (kind == MixedSweeps::kSplit || kind == MixedSweeps::kDelta) {
       // The exact residual is symmetric under (i,j,a,b) -> (j,i,b,a); rounding of the
       // tensor-core products is not.  In the antisymmetric sector the Fock terms cancel
       // and the Jacobi step does not damp, so project the noise out of R2.
@@ -502,21 +545,18 @@ CCSDResult run_ccsd(Ctx& c) {
     if (c.opt.print >= 2 && mixed) {
       // diagnostics: distance of this residual from the FP64 one at the same amplitudes,
       // and of the amplitudes from the last anchor
-      if (kind == kRecord) {
+      if (kind == MixedSweeps::kRecord) {
         c.alloc("T_anchor", {np}, false);
         UCC_CUDA(cudaMemcpyAsync(c.get("T_anchor").p, to, sizeof(double) * np, cudaMemcpyDeviceToDevice, c.stream));
       } else {
         Temp Rx(c, {np});
         {
           Fp64Scope f(c);
-          const int saved = c.anchors.mode;
-          c.anchors.mode = 0;
           ccsd_residual(c, to, Rx->p);
-          c.anchors.mode = saved;
         }
         axpby(c, np, -1.0, r, 1.0, Rx->p);
         noise = std::sqrt(dot(c, np, Rx->p, Rx->p));
-        if (kind == kDelta) {
+        if (kind == MixedSweeps::kDelta) {
           axpby(c, np, 1.0, to, 0.0, Rx->p);
           axpby(c, np, -1.0, c.get("T_anchor").p, 1.0, Rx->p);
           drift = std::sqrt(dot(c, np, Rx->p, Rx->p));
@@ -530,37 +570,13 @@ CCSDResult run_ccsd(Ctx& c) {
     UCC_CUDA(cudaStreamSynchronize(c.stream));
     rms = std::sqrt(ss);
     UCC_REQUIRE(std::isfinite(rms), UCC_NAN_DETECTED, "CCSD residual is not finite");
-    bool keep_history = true;
-    if (kind == kFp64) {
-      if (rms < c.opt.r_convergence) break;
-    } else if (kind == kSplit) {
-      split_sweeps++;
-      if (!refine && rms < c.opt.r_convergence) break;
-      // hand over near the split-product noise floor or when the residual stops falling
-      if (refine && (rms < std::max(c.opt.r_convergence, std::max(c.opt.mixed_switch, kMixedFloor)) ||
-                     (iter > 2 && rms > 0.5 * rms_prev))) {
-        split_phase = false;
-        record_next = true;
-        diis.reset();  // the split-sweep history extrapolates a different map
-        keep_history = false;
-      }
-    } else if (kind == kRecord) {
-      record_sweeps++;
-      record_next = false;
-      stalls = 0;
-      if (rms < c.opt.r_convergence && record_sweeps >= c.opt.refine_sweeps) break;
-    } else {
-      delta_sweeps++;
-      if (rms < c.opt.r_convergence) {
-        record_next = true;  // confirm with an FP64 residual
-      } else if (rms > 0.7 * rms_prev) {
-        if (++stalls >= 2) record_next = true;  // corrections no longer resolved: re-anchor
-      } else {
-        stalls = 0;
-      }
+    bool restart = false;
+    if (sw.after(rms, &restart)) {
+      converged = true;
+      break;
     }
-    rms_prev = rms;
-    if (c.opt.diis && keep_history) {
+    if (restart) diis.reset();
+    if (c.opt.diis && !restart) {
       diis.add(tn, to);
       if (diis.size() > 2) diis.extrapolate(tn);
     }
@@ -575,11 +591,10 @@ CCSDResult run_ccsd(Ctx& c) {
       std::printf("\n");
     }
   }
-  c.anchors.clear();
   if (c.has("T_anchor")) c.drop("T_anchor");
-  c.stats.mixed_iterations = split_sweeps;
-  c.stats.anchored_iterations = delta_sweeps;
-  const int fp64_iters = mixed ? record_sweeps : std::min(iter, c.opt.maxiter);
+  c.stats.mixed_iterations = sw.split;
+  c.stats.anchored_iterations = sw.delta;
+  const int fp64_iters = mixed ? sw.record : std::min(iter, c.opt.maxiter);
   tau_of(c.get("T").p);
   UCC_CUDA(cudaStreamSynchronize(c.stream));
   for (size_t k = 0; k + 1 < ev.size(); k += 2) {
@@ -595,7 +610,7 @@ CCSDResult run_ccsd(Ctx& c) {
   }
   res.iterations = std::min(iter, c.opt.maxiter);
   res.e_ccsd = eccsd;
-  res.converged = rms < c.opt.r_convergence;
+  res.converged = converged;
   c.stats.fp64_iterations = fp64_iters;
   c.have_ccsd = res.converged;
   return res;

@@ -427,31 +427,46 @@ CCSDResult pert_solve(Ctx& c, int h, bool right) {  // ccpert.cc:177-229
     std::printf("\t-------------------------------------\n\t  %3d  %20.15f\n", 0, pseudoresponse(c, p, c.get(cur).p));
   }
   double rms = INFINITY;
+  bool converged = false;
+  MixedSweeps sw(c);  // MIXED: split, record and delta sweeps; X2/Y2 are symmetrised by construction
   int iter;
   for (iter = 1; iter <= c.opt.maxiter; iter++) {
     c.store[cur].swap(c.store[old]);
     double* o = c.get(old).p;
     double* nw = c.get(cur).p;
-    if (right)
-      build_X(c, p, amp1(c, o), amp2(c, o), amp1(c, R->p), amp2(c, R->p));
-    else
-      build_Y(c, p, amp1(c, o), amp2(c, o), amp1(c, R->p), amp2(c, R->p));
+    const MixedSweeps::Kind kind = sw.begin();
+    {
+      PrecisionScope scope(c, kind != MixedSweeps::kSplit);
+      if (right)
+        build_X(c, p, amp1(c, o), amp2(c, o), amp1(c, R->p), amp2(c, R->p));
+      else
+        build_Y(c, p, amp1(c, o), amp2(c, o), amp1(c, R->p), amp2(c, R->p));
+    }
+    sw.end();
     jacobi_update(c, no, nv, hd.p, hd.p + no, p.omega, R->p, R->p + n1, o, o + n1, nw, nw + n1, sumsq.d());
     double ss = 0.0;
     UCC_CUDA(cudaMemcpyAsync(&ss, sumsq.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     UCC_CUDA(cudaStreamSynchronize(c.stream));
     rms = std::sqrt(ss);
     UCC_REQUIRE(std::isfinite(rms), UCC_NAN_DETECTED, "perturbed-wavefunction residual is not finite");
-    if (rms < c.opt.r_convergence) break;
-    if (c.opt.diis) {
+    bool restart = false;
+    if (sw.after(rms, &restart)) {
+      converged = true;
+      break;
+    }
+    if (restart) diis.reset();
+    if (c.opt.diis && !restart) {
       diis.add(nw, o);
       if (diis.size() > 2) diis.extrapolate(nw);
     }
-    if (c.opt.print) std::printf("\t  %3d  %20.15f  %5.3e\n", iter, pseudoresponse(c, p, nw), rms);
+    if (c.opt.print) {
+      static const char* tag[] = {"", " split", " record", " delta"};
+      std::printf("\t  %3d  %20.15f  %5.3e%s\n", iter, pseudoresponse(c, p, nw), rms, tag[kind]);
+    }
   }
   CCSDResult res;
   res.iterations = std::min(iter, c.opt.maxiter);
-  res.converged = rms < c.opt.r_convergence;
+  res.converged = converged;
   res.e_ccsd = pseudoresponse(c, p, c.get(cur).p);
   if (res.converged) (right ? p.right_done : p.left_done) = true;
   return res;
