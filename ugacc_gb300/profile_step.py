@@ -30,6 +30,9 @@ def main(argv=None):
                     help="print the iteration tables (2: also the residual error of every mixed sweep)")
     ap.add_argument("--switch", type=float, default=1e-5, help="MIXED hand-over residual norm")
     ap.add_argument("--diis", type=int, default=1, help="0 turns DIIS extrapolation off")
+    ap.add_argument("--response", action="store_true",
+                    help="CCSD, HBAR, Lambda, densities and the static + dynamic dipole polarizability "
+                         "(3 symmetric perturbations, omega 0 and 0.0656, right-hand solves)")
     ap.add_argument("--ccsd-fp64", action="store_true",
                     help="with --triples: converge CCSD in FP64, then run (T) at --precision")
     a = ap.parse_args(argv)
@@ -68,6 +71,32 @@ def main(argv=None):
                           "ccsd_iterations": st_cc["ccsd_iterations"], "fp64_iterations": st_cc["fp64_iterations"],
                           "mixed_iterations": st_cc["mixed_iterations"],
                           "anchored_iterations": st_cc["anchored_iterations"]}))
+    if a.response:
+        from ugacc_gb300.generator import RESPONSE_OMEGAS, make_perturbations
+        cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": prec, "PRINT": int(a.print), "MIXED_SWITCH": a.switch})
+        e_cc = cc.compute_energy()
+        hb = U.HBAR(H, cc)
+        lam = U.CCLambda(cc, hb)
+        lam.compute_lambda()
+        dens = U.CCDensity(cc, lam)
+        e1, e2 = dens.onepdm(), dens.twopdm()
+        perts = make_perturbations(h.nact, a.seed)
+        alphas = {}
+        for w in RESPONSE_OMEGAS:
+            mu = [U.CCPert(perts[x], w, cc, hb, lam) for x in range(3)]
+            for m in mu:
+                m.solve("right")
+            tens = []
+            for p in range(3):
+                row = []
+                for q in range(3):
+                    r = U.CCResp(mu[p], mu[q])
+                    row.append(r.linresp(mu[p], mu[q]) if p == q else
+                               0.5 * r.linresp(mu[p], mu[q]) + 0.5 * r.linresp(mu[q], mu[p]))
+                tens.append(row)
+            alphas[str(w)] = tens
+        print(json.dumps({"e_ccsd": e_cc, "pseudoenergy": lam.pseudoenergy(), "e_onepdm": e1, "e_twopdm": e2,
+                          "alpha": alphas}))
     print(json.dumps(H.ctx.stats()))
     return 0
 
