@@ -73,7 +73,7 @@ class MixedSweeps {
   bool mixed_, refine_, split_phase_, record_next_ = true;
   int stalls_ = 0, sweeps_ = 0;
   double rms_prev_ = INFINITY;
-  Kind kind_ = kFp64;
+  Kind kind_ = kFp64, last_ = kFp64;
 };
 
 // ---- solver stages ---------------------------------------------------------------------

@@ -448,9 +448,10 @@ bool MixedSweeps::after(double rms, bool* restart_diis) {
   } else if (kind_ == kSplit) {
     split++;
     if (!refine_ && rms < rc) done = true;
-    // hand over near the split-product noise floor or when the residual stops falling
-    if (!done && refine_ &&
-        (rms < std::max(rc, std::max(c_.opt.mixed_switch, kMixedFloor)) || (sweeps_ > 2 && rms > 0.5 * rms_prev_))) {
+    // hand over near the split-product noise floor, or when the residual stops falling
+    // within three decades of it (early sweeps of a hard system fall slowly too)
+    const double level = std::max(rc, std::max(c_.opt.mixed_switch, kMixedFloor));
+    if (!done && refine_ && (rms < level || (sweeps_ > 2 && rms < 1e3 * level && rms > 0.5 * rms_prev_))) {
       split_phase_ = false;
       record_next_ = true;
       *restart_diis = true;  // the split-sweep history extrapolates a different map
@@ -460,6 +461,9 @@ bool MixedSweeps::after(double rms, bool* restart_diis) {
     record_next_ = false;
     stalls_ = 0;
     done = rms < rc && record >= c_.opt.refine_sweeps;
+    // the FP64 residual is well above what the last delta sweep reported: those sweeps'
+    // anchor was too far away and their vectors would mislead the extrapolation
+    if (!done && last_ == kDelta && rms > 2.0 * rms_prev_) *restart_diis = true;
   } else {
     delta++;
     if (rms < rc) {
@@ -471,6 +475,7 @@ bool MixedSweeps::after(double rms, bool* restart_diis) {
     }
   }
   rms_prev_ = rms;
+  last_ = kind_;
   return done;
 }
 
