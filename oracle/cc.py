@@ -293,6 +293,69 @@ class CCWfn:
                     ET += term[mask].sum()
         return ET
 
+    # ------------------------------------------------- (T) gradient pieces
+    def N3_ijk(self, i, j, k):  # ccwfn.cc:1492-1515, numerator (the caller divides by D3)
+        H, t1, t2 = self.H, self.t1, self.t2
+        Voovv, fov = H.V("oovv"), H.fblk("ov")
+        return (ein("ab,c->abc", Voovv[i, j], t1[k]) + ein("ac,b->abc", Voovv[i, k], t1[j])
+                + ein("bc,a->abc", Voovv[j, k], t1[i]) + ein("ab,c->abc", t2[i, j], fov[k])
+                + ein("ac,b->abc", t2[i, k], fov[j]) + ein("bc,a->abc", t2[j, k], fov[i]))
+
+    def tgrad(self):  # ccwfn.cc:1150-1316 (tgrad_ooc)
+        """s1, s2 and the (T) density pieces; M3 = W3/D3 and N3 over every ordered (i,j,k)."""
+        H, t1, t2 = self.H, self.t1, self.t2
+        no, nv = H.no, H.nv
+        eo, ev = np.diag(H.f)[:no], np.diag(H.f)[no:]
+        Voovv, Vooov, Vvovv = H.V("oovv"), H.V("ooov"), H.V("vovv")
+        dv = ev[:, None, None] + ev[None, :, None] + ev[None, None, :]
+        M = np.zeros((no, no, no, nv, nv, nv))
+        N = np.zeros_like(M)
+        for i in range(no):
+            for j in range(no):
+                for k in range(no):
+                    d3 = eo[i] + eo[j] + eo[k] - dv
+                    M[i, j, k] = self.W3_ijk(i, j, k) / d3  # M3_ijk, ccwfn.cc:1420-1454
+                    N[i, j, k] = self.N3_ijk(i, j, k) / d3
+
+        def perm6(A, w):  # 8A(abc) - 4A(bac) - 4A(acb) - 4A(cba) + 2A(cab) + 2A(bca) over the last three axes
+            o = A.ndim - 3
+            T = lambda p: A.transpose(tuple(range(o)) + tuple(o + q for q in p))
+            return w[0] * A - w[1] * T((1, 0, 2)) - w[1] * T((0, 2, 1)) - w[1] * T((2, 1, 0)) + w[2] * T((1, 2, 0)) \
+                + w[2] * T((2, 0, 1))
+
+        X = perm6(M, (8.0, 4.0, 2.0))
+        Y = perm6(N, (8.0, 4.0, 2.0))
+        # Z3[a][b][c] = 2(M[abc] - M[acb]) - (M[bac] - M[bca])
+        Z = 2.0 * (M - M.transpose(0, 1, 2, 3, 5, 4)) - (M.transpose(0, 1, 2, 4, 3, 5) - M.transpose(0, 1, 2, 5, 3, 4))
+        Q = 2.0 * X + Y
+        s1 = np.zeros((no, nv))
+        X2 = np.zeros((no, no, nv, nv))
+        Doo, Dvv, Dov = np.zeros((no, no)), np.zeros((nv, nv)), np.zeros((no, nv))
+        Goovv = np.zeros((no, no, nv, nv))
+        Gooov = np.zeros((no, no, no, nv))
+        Gvvvo = np.zeros((nv, nv, nv, no))
+        for i in range(no):
+            for j in range(no):
+                for k in range(no):
+                    m, z, q = M[i, j, k], Z[i, j, k], Q[i, j, k]
+                    Dvv[np.arange(nv), np.arange(nv)] += 0.5 * ein("abc,abc->a", m, X[i, j, k] + Y[i, j, k])
+                    Dov[i] += ein("abc,bc->a", m - m.transpose(2, 1, 0), 4.0 * t2[j, k] - 2.0 * t2[j, k].T)
+                    s1[i] += ein("abc,bc->a", 4.0 * m - 4.0 * m.transpose(1, 0, 2) - 2.0 * m.transpose(0, 2, 1)
+                                 + 2.0 * m.transpose(1, 2, 0), Voovv[j, k])
+                    Goovv[i, j] += 4.0 * ein("c,abc->ab", t1[k], z)
+                    X2[i] -= ein("abc,lc->lab", q, Vooov[j, k])
+                    Gooov[j, i] -= ein("abc,lbc->la", q, t2[:, k])
+                    X2[i, j] += ein("abc,dbc->ad", q, Vvovv[:, k])
+                    Gvvvo[:, :, :, j] += ein("abc,cd->abd", q, t2[k, i])
+        # second pass over (a,b,c) with occupied permutations (M3_abc/N3_abc, :1226-1250)
+        Mo = M.transpose(3, 4, 5, 0, 1, 2)
+        No = N.transpose(3, 4, 5, 0, 1, 2)
+        Xo, Yo = perm6(Mo, (8.0, 4.0, 2.0)), perm6(No, (8.0, 4.0, 2.0))
+        Doo[np.arange(no), np.arange(no)] -= 0.5 * ein("abcijk,abcijk->i", Mo, Xo + Yo)
+        s2 = X2 + X2.transpose(1, 0, 3, 2)
+        self.tg = dict(s1=s1, s2=s2, Doo=Doo, Dvv=Dvv, Dov=Dov, Goovv=Goovv, Gooov=Gooov, Gvvvo=Gvvvo)
+        return self.tg
+
 
 # --------------------------------------------------------------------------------------
 # HBAR                                                                      (hbar.cc)
@@ -371,12 +434,18 @@ class CCLambda:
         R -= ein("mnae,iemn->ia", l2, hb.Hovoo)
         R -= ein("ef,eifa->ia", Gvv, 2.0 * hb.Hvovv - hb.Hvovv.swapaxes(2, 3))
         R -= ein("mn,mina->ia", Goo, 2.0 * hb.Hooov - hb.Hooov.transpose(1, 0, 2, 3))
+        tg = getattr(self.cc, "tg", None)
+        if tg is not None:  # WFN=CCSD_T, DERTYPE=FIRST: :181
+            R += tg["s1"]
         return R
 
     def build_l2(self, l1, l2, Goo, Gvv):  # :215-289
         hb, H = self.hb, self.H
         Loovv = H.L("oovv")
         Z = Loovv.copy()
+        tg = getattr(self.cc, "tg", None)
+        if tg is not None:  # WFN=CCSD_T, DERTYPE=FIRST: :243
+            Z += 0.5 * tg["s2"]
         Z += 2.0 * ein("ia,jb->ijab", l1, hb.Hov) - ein("ja,ib->ijab", l1, hb.Hov)
         Z += ein("ijeb,ea->ijab", l2, hb.Hvv)
         Z -= ein("mjab,im->ijab", l2, hb.Hoo)
@@ -433,6 +502,11 @@ class CCDensity:
         self.Dvo = l1.T.copy()
         self.Dov = 2.0 * t1 + ein("me,imae->ia", l1, 2.0 * t2 - tau.transpose(1, 0, 2, 3))
         self.Dov -= ein("mnef,ma,inef->ia", l2, t1, t2) + ein("mnef,ie,mnaf->ia", l2, t1, t2)
+        tg = getattr(self.cc, "tg", None)
+        if tg is not None:  # the (T) pieces the densities start from, ccdensity.cc:44-69
+            self.Doo += tg["Doo"]
+            self.Dvv += tg["Dvv"]
+            self.Dov += tg["Dov"]
         return ein("ij,ij->", self.H.fblk("oo"), self.Doo) + ein("ab,ab->", self.H.fblk("vv"), self.Dvv)
 
     def twopdm(self):  # :153-339
@@ -453,6 +527,9 @@ class CCDensity:
         G += (ein("kmef,ma,ijef->ijka", l2, t1, t2) + ein("kmef,ie,mjaf->ijka", l2, t1, t2)
               + ein("kmef,jf,imea->ijka", l2, t1, t2))
         G += ein("kmef,ma,ie,jf->ijka", l2, t1, t1, t1)
+        tg = getattr(self.cc, "tg", None)
+        if tg is not None:
+            G += tg["Gooov"]
         E["ooov"] = ein("ijka,ijka->", V("ooov"), G)
         # Gvvvo, :237-259
         G = ein("mc,miab->abci", l1, 2.0 * tau - tau.transpose(1, 0, 2, 3))
@@ -462,6 +539,8 @@ class CCDensity:
         G -= (ein("nmce,mb,niae->abci", l2, t1, t2) + ein("nmce,na,mibe->abci", l2, t1, t2)
               + ein("nmce,ie,nmab->abci", l2, t1, t2))
         G -= ein("nmce,mb,na,ie->abci", l2, t1, t1, t1)
+        if tg is not None:
+            G += tg["Gvvvo"]
         E["vvvo"] = ein("abci,abci->", V("vvvo"), G)
         # Govov, :268-276
         G = -ein("ia,jb->iajb", t1, l1)
@@ -485,6 +564,8 @@ class CCDensity:
               + ein("mnef,ma,ie,njbf->ijab", l2, t1, t1, t2) + ein("mnef,nb,jf,miae->ijab", l2, t1, t1, t2)
               + ein("mnef,na,je,imfb->ijab", l2, t1, t1, t2) + ein("mnef,if,mb,njae->ijab", l2, t1, t1, t2))
         G += ein("mnef,ma,nb,ie,jf->ijab", l2, t1, t1, t1, t1)
+        if tg is not None:
+            G += tg["Goovv"]
         E["oovv"] = 0.5 * ein("ijab,ijab->", V("oovv"), G)
         self.E2 = E
         return sum(E.values())

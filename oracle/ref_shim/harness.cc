@@ -173,6 +173,17 @@ int main(int argc, char** argv) {
     out.num("e_ccsd", ecc);
     out.mat("t1", cc->t1_, no, nv);
     out.t4("t2", cc->t2_, no, no, nv, nv);
+    if (kv["WFN"] == "CCSD_T" && kv["DERTYPE"] == "FIRST") {
+      // (T) gradient pieces left by compute_energy's tgrad_ooc (ccwfn.cc:252-255)
+      out.mat("s1", cc->s1_, no, nv);
+      out.t4("s2", cc->s2_, no, no, nv, nv);
+      out.mat("DooT", cc->Doo_, no, no);
+      out.mat("DvvT", cc->Dvv_, nv, nv);
+      out.mat("DovT", cc->Dov_, no, nv);
+      out.t4("GoovvT", cc->Goovv_, no, no, nv, nv);
+      out.t4("GooovT", cc->Gooov_, no, no, no, nv);
+      out.t4("GvvvoT", cc->Gvvvo_, nv, nv, nv, no);
+    }
 
     const std::string trip = kv["TRIPLES"];
     if (trip == "ooc" || trip == "all") {

@@ -54,6 +54,11 @@ CASES = {
     "prime": (7, 13, 7, [("ccsd_t", dict(DERTYPE="FIRST", TRIPLES="all"), ALL_T)]),
     # more virtuals than a 32-wide tile
     "mid": (6, 40, 5, [("ccsd_t", dict(DERTYPE="NONE", TRIPLES="all"), ["t1"])]),
+    # CCSD(T) first derivatives: the (T) gradient pieces (s1, s2, (T) densities), the
+    # Lambda equations with s1/s2 and the densities that start from the (T) pieces
+    "tgrad": (4, 11, 9, [("ccsd_t_first", dict(WFN="CCSD_T", DERTYPE="FIRST"),
+                          ["t1", "t2", "s1", "s2", "DooT", "DvvT", "DovT", "GoovvT", "GooovT", "GvvvoT",
+                           "l1", "l2", "Doo", "Dvv", "Dov"])]),
 }
 BIG = {
     # the plain FP64 CCSD(T) workload itself (no=16, nv=160, seed 1); hours on one core
@@ -120,9 +125,11 @@ def main():
     ap.add_argument("--big", action="store_true", help="also the no=16/nv=160 case (hours)")
     ap.add_argument("--only", nargs="*")
     ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--build-dir", default="_ref", help="build directory under oracle/")
     a = ap.parse_args()
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REFERENCE={a.reference}"], check=True)
-    binary = os.path.join(ROOT, "oracle", "_ref", "ugacc_ref")
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REFERENCE={a.reference}", f"OUT={a.build_dir}"],
+                   check=True)
+    binary = os.path.join(ROOT, "oracle", a.build_dir, "ugacc_ref")
     cases = dict(CASES)
     if a.big:
         cases.update(BIG)

@@ -22,7 +22,10 @@ def test_ccsd_and_triples(name):
     meta, arr = load(name)
     h, perts, H, cc = _pipeline(meta)
     for tag, run in meta["runs"].items():
-        assert abs(cc.eccsd - run["e_ccsd"]) < ETOL
+        if run["options"].get("WFN") == "CCSD_T":  # compute_energy returned E_CCSD + E_(T)
+            assert abs(cc.eccsd + cc.tcorr_tjl() - run["e_ccsd"]) < ETOL
+        else:
+            assert abs(cc.eccsd - run["e_ccsd"]) < ETOL
         # iteration-by-iteration energies of the reference's table (same DIIS procedure)
         ref_iters = [e for _, e in run["tables"]["ccsd"][1:]]
         assert len(ref_iters) == len(cc.iter_energies)
@@ -112,3 +115,29 @@ def test_not_converged_raises():
     cc = O.CCWfn(O.Hamiltonian(h), maxiter=1, r_convergence=1e-10)
     with pytest.raises(O.NotConverged):
         cc.compute_energy()
+
+
+def test_triples_gradient_pieces_lambda_and_densities():
+    """WFN=CCSD_T, DERTYPE=FIRST: tgrad_ooc's s1, s2 and (T) density pieces
+    (ccwfn.cc:1150-1316), the Lambda equations with s1/s2 (cclambda.cc:181,243) and the
+    densities that start from the (T) pieces (ccdensity.cc:44-69)."""
+    meta, arr = load("tgrad")
+    h, perts, H, cc = _pipeline(meta)
+    tag, run = next(iter(meta["runs"].items()))
+    tg = cc.tgrad()
+    for k in ["s1", "s2", "Doo", "Dvv", "Dov", "Goovv", "Gooov", "Gvvvo"]:
+        ref = arr[f"{tag}/{k}" if k in ("s1", "s2") else f"{tag}/{k}T"]
+        np.testing.assert_allclose(tg[k], ref, atol=1e-16 + 1e-12 * np.abs(ref).max(), rtol=0, err_msg=k)
+    hb = O.HBAR(H, cc)
+    lam = O.CCLambda(cc, hb)
+    lam.compute_lambda()
+    assert abs(lam.pseudoenergy() - run["pseudoenergy"]) < ETOL
+    np.testing.assert_allclose(lam.l1, arr[f"{tag}/l1"], atol=TTOL, rtol=0)
+    np.testing.assert_allclose(lam.l2, arr[f"{tag}/l2"], atol=TTOL, rtol=0)
+    dens = O.CCDensity(cc, lam)
+    e1, e2 = dens.onepdm(), dens.twopdm()
+    assert abs(e1 - run["e_onepdm"]) < ETOL and abs(e2 - run["e_twopdm"]) < ETOL
+    # with the (T) pieces the density energy is the CCSD(T) energy
+    assert abs(e1 + e2 - run["e_ccsd"]) < 1e-12
+    for k in ["Doo", "Dvv", "Dov"]:
+        np.testing.assert_allclose(getattr(dens, k), arr[f"{tag}/{k}"], atol=TTOL, rtol=0)
