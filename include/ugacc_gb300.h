@@ -73,6 +73,14 @@ ucc_status ucc_ccsd(ucc_ctx* ctx, double* e_ccsd, int* iterations);
  * equals tcorr_ooc (:745-793) and tcorr (:647-743). */
 ucc_status ucc_triples(ucc_ctx* ctx, double* e_t);
 
+/* Replaces: CCWfn::tgrad_ooc (ccwfn.cc:1150-1316), run by compute_energy for
+ * WFN=CCSD_T, DERTYPE=FIRST (:252-255): the (T) pieces of the CCSD(T) first derivatives.
+ * Afterwards ucc_lambda adds s1 / s2/2 to its residuals (cclambda.cc:181,243) and
+ * ucc_density starts from the (T) parts of Doo, Dvv, Dov, Goovv, Gooov, Gvvvo
+ * (ccdensity.cc:44-69), until the next ucc_ccsd.  Tensors: "s1" "s2" "DooT" "DvvT" "DovT"
+ * "GoovvT" "GooovT" "GvvvoT" (reference array layouts). */
+ucc_status ucc_triples_gradient(ucc_ctx* ctx);
+
 /* Replaces: HBAR::HBAR (hbar.cc:8-228). */
 ucc_status ucc_hbar(ucc_ctx* ctx);
 

@@ -89,6 +89,8 @@ class CCWfn {
     if (opt_.wfn == "CCSD_T") {
       check(H_->ctx(), ucc_triples(H_->ctx(), &et_));
       e += et_;
+      // (T) gradient pieces for the derivative stages (ccwfn.cc:252-255)
+      if (opt_.dertype == "FIRST") check(H_->ctx(), ucc_triples_gradient(H_->ctx()));
     }
     return e;
   }

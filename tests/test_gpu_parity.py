@@ -26,7 +26,10 @@ def test_ccsd_triples_vs_reference(name):
     h, _ = hamiltonian(meta)
     H, cc = gpu_pipeline(h)
     tag, run = next(iter(meta["runs"].items()))
-    assert abs(cc.eccsd - run["e_ccsd"]) < ETOL
+    if run["options"].get("WFN") == "CCSD_T":  # the reference returned E_CCSD + E_(T)
+        assert abs(cc.eccsd + cc.triples() - run["e_ccsd"]) < ETOL
+    else:
+        assert abs(cc.eccsd - run["e_ccsd"]) < ETOL
     assert cc.iterations == len(run["tables"]["ccsd"])  # same DIIS, same iteration count
     if f"{tag}/t1" in arr:
         np.testing.assert_allclose(cc.t1, arr[f"{tag}/t1"], atol=TTOL, rtol=0)
@@ -123,3 +126,50 @@ def test_stage_order_is_enforced():
     with pytest.raises(U.UccError) as e:
         H.ctx.check(H.ctx.lib.ucc_hbar(H.ctx.h))
     assert e.value.status == 5
+
+
+def test_triples_gradient_vs_reference():
+    """WFN=CCSD_T, DERTYPE=FIRST: s1, s2 and the (T) density pieces (ccwfn.cc:1150-1316),
+    then Lambda with s1/s2 and the densities starting from the (T) pieces."""
+    meta, arr = load("tgrad")
+    h, _ = hamiltonian(meta)
+    tag, run = next(iter(meta["runs"].items()))
+    H, cc = gpu_pipeline(h, WFN="CCSD_T", DERTYPE="FIRST")
+    assert abs(cc.eccsd + cc.et - run["e_ccsd"]) < ETOL
+    no, nv = h.no, h.nv
+    shapes = {"s1": (no, nv), "s2": (no, no, nv, nv), "DooT": (no, no), "DvvT": (nv, nv), "DovT": (no, nv),
+              "GoovvT": (no, no, nv, nv), "GooovT": (no, no, no, nv), "GvvvoT": (nv, nv, nv, no)}
+    for name, shp in shapes.items():
+        ref = arr[f"{tag}/{name}"]
+        got = H.ctx.get(name, shp)
+        np.testing.assert_allclose(got, ref, atol=1e-20 + 1e-10 * np.abs(ref).max(), rtol=0, err_msg=name)
+    hb = U.HBAR(H, cc)
+    lam = U.CCLambda(cc, hb)
+    lam.compute_lambda()
+    assert abs(lam.pseudoenergy() - run["pseudoenergy"]) < ETOL
+    np.testing.assert_allclose(lam.l1, arr[f"{tag}/l1"], atol=TTOL, rtol=0)
+    np.testing.assert_allclose(lam.l2, arr[f"{tag}/l2"], atol=TTOL, rtol=0)
+    dens = U.CCDensity(cc, lam)
+    e1, e2 = dens.onepdm(), dens.twopdm()
+    assert abs(e1 - run["e_onepdm"]) < ETOL and abs(e2 - run["e_twopdm"]) < ETOL
+    assert abs(e1 + e2 - (cc.eccsd + cc.et)) < 1e-10  # E(density) = E_CCSD(T)
+    for k in ["Doo", "Dvv", "Dov"]:
+        np.testing.assert_allclose(H.ctx.get(k, arr[f"{tag}/{k}"].shape), arr[f"{tag}/{k}"], atol=TTOL, rtol=0)
+
+
+def test_triples_gradient_vs_oracle_larger():
+    """The same pieces at no=5, nv=24 (several tuple batches) against the oracle."""
+    h = make_hamiltonian(5, 24, 31)
+    H, cc = gpu_pipeline(h, WFN="CCSD_T", DERTYPE="FIRST")
+    Ho = O.Hamiltonian(h)
+    co = O.CCWfn(Ho, r_convergence=1e-10)
+    co.compute_energy()
+    tg = co.tgrad()
+    no, nv = h.no, h.nv
+    pairs = {"s1": ("s1", (no, nv)), "s2": ("s2", (no, no, nv, nv)), "Doo": ("DooT", (no, no)),
+             "Dvv": ("DvvT", (nv, nv)), "Dov": ("DovT", (no, nv)), "Goovv": ("GoovvT", (no, no, nv, nv)),
+             "Gooov": ("GooovT", (no, no, no, nv)), "Gvvvo": ("GvvvoT", (nv, nv, nv, no))}
+    for k, (name, shp) in pairs.items():
+        ref = tg[k]
+        np.testing.assert_allclose(H.ctx.get(name, shp), ref, atol=1e-20 + 1e-9 * np.abs(ref).max(), rtol=0,
+                                   err_msg=k)

@@ -101,6 +101,7 @@ def load_library(path: str | None = None):
         "ucc_load_hamiltonian_df": (i, [vp, i, i, i, dp, dp]),
         "ucc_ccsd": (i, [vp, dp, P(i)]),
         "ucc_triples": (i, [vp, dp]),
+        "ucc_triples_gradient": (i, [vp]),
         "ucc_hbar": (i, [vp]),
         "ucc_lambda": (i, [vp, dp, P(i)]),
         "ucc_density": (i, [vp, dp, dp]),
@@ -274,7 +275,14 @@ class CCWfn:
         if self.options["WFN"] == "CCSD_T":
             self.et = self.triples()
             total += self.et
+            if self.options["DERTYPE"] == "FIRST":  # ccwfn.cc:252-255
+                self.triples_gradient()
         return total
+
+    def triples_gradient(self):
+        """ccwfn.cc:1150-1316 (tgrad_ooc): s1, s2 and the (T) density pieces, which the
+        following CCLambda and CCDensity include."""
+        self.ctx.check(self.ctx.lib.ucc_triples_gradient(self.ctx.h))
 
     def triples(self) -> float:
         """ccwfn.cc:795-852 (tcorr_ooc_TJL)."""

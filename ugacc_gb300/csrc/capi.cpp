@@ -59,7 +59,7 @@ void reset_state(Ctx& c) {
   c.perts.clear();
   c.store.clear();
   c.shapes.clear();
-  c.loaded = c.have_ccsd = c.have_hbar = c.have_lambda = false;
+  c.loaded = c.have_ccsd = c.have_hbar = c.have_lambda = c.have_tgrad = false;
 }
 }  // namespace
 
@@ -192,6 +192,18 @@ ucc_status ucc_triples(ucc_ctx* ctx, double* et) {
     c.stats.triples_flops += flops_triples(c.no, c.nv);
     c.stats.kernel_launches += launches() - l0;
     if (et) *et = e;
+  });
+}
+
+ucc_status ucc_triples_gradient(ucc_ctx* ctx) {
+  return guard(ctx, [&](Ctx& c) {
+    UCC_CUDA(cudaSetDevice(c.device));
+    const int64_t l0 = launches();
+    Timer tm(c.stream);
+    tm.start();
+    run_triples_gradient(c);
+    c.stats.triples_ms += tm.stop_ms();
+    c.stats.kernel_launches += launches() - l0;
   });
 }
 

@@ -87,6 +87,7 @@ void ccsd_alloc(Ctx& c);                                         // CCSD work ar
 void ccsd_residual(Ctx& c, const double* t_old, double* r);      // R(t_old), tau/ttau current
 double ccsd_energy(Ctx& c, const double* t);                     // E from t and the stored tau
 double run_triples(Ctx& c);
+void run_triples_gradient(Ctx& c);  // tgrad.cu
 void run_hbar(Ctx& c);
 CCSDResult run_lambda(Ctx& c);
 void run_density(Ctx& c, double* e1, double* e2);

@@ -174,6 +174,7 @@ void lambda_l1(Ctx& c, const Tensor& l1, const Tensor& l2, const Tensor& Goo, co
   contract(c, "mnae,iemn->ia", -1.0, l2, c.get("Hovoo"), 1.0, R1);
   contract(c, "ef,eifa->ia", -1.0, Gvv, c.get("Hvovv_x"), 1.0, R1);
   contract(c, "mn,mina->ia", -1.0, Goo, c.get("Hooov_x"), 1.0, R1);
+  if (c.have_tgrad) axpby(c, R1.size(), 1.0, c.get("TS1").p, 1.0, R1.p);  // cclambda.cc:181
 }
 
 void lambda_l2(Ctx& c, const Tensor& l1, const Tensor& l2, const Tensor& Goo, const Tensor& Gvv, Tensor R2) {
@@ -181,6 +182,7 @@ void lambda_l2(Ctx& c, const Tensor& l1, const Tensor& l2, const Tensor& Goo, co
   Temp Z(c, {no, no, nv, nv});
   Tensor Loovv = L(c, "oovv"), Hov = c.get("Hov");
   copy_into(c, Loovv, Z);
+  if (c.have_tgrad) axpby(c, Z->size(), 0.5, c.get("TS2").p, 1.0, Z->p);  // cclambda.cc:243
   contract(c, "ia,jb->ijab", 2.0, l1, Hov, 1.0, Z);
   contract(c, "ja,ib->ijab", -1.0, l1, Hov, 1.0, Z);
   contract(c, "ijeb,ea->ijab", 1.0, l2, c.get("Hvv"), 1.0, Z);
@@ -310,6 +312,11 @@ void run_density(Ctx& c, double* e1, double* e2) {
     Temp Z(c, {nv, nv});
     contract(c, "mnef,mnaf->ea", 1.0, l2, t2, 0.0, Z);
     contract(c, "ie,ea->ia", -1.0, t1, Z, 1.0, Dov);
+  }
+  if (c.have_tgrad) {  // the (T) pieces the densities start from, ccdensity.cc:44-69
+    axpby(c, Doo.size(), 1.0, c.get("TDoo").p, 1.0, Doo.p);
+    axpby(c, Dvv.size(), 1.0, c.get("TDvv").p, 1.0, Dvv.p);
+    axpby(c, Dov.size(), 1.0, c.get("TDov").p, 1.0, Dov.p);
   }
   *e1 = dot_all(c, Fk(c, "oo"), Doo) + dot_all(c, Fk(c, "vv"), Dvv);
 
@@ -459,6 +466,11 @@ void run_density(Ctx& c, double* e1, double* e2) {
     contract(c, "mnij,ma->nija", 1.0, W2, t1, 0.0, W10);
     contract(c, "nija,nb->ijab", 1.0, W10, t1, 1.0, G);
     E[5] = 0.5 * dot_all(c, V(c, "oovv"), G);
+  }
+  if (c.have_tgrad) {  // Eooov, Evvvo, Eoovv of the (T) pieces (ccdensity.cc:225-330)
+    E[2] += dot_all(c, V(c, "ooov"), c.get("TGooov"));
+    E[3] += dot_all(c, V(c, "vvvo"), c.get("TGvvvo"));
+    E[5] += 0.5 * dot_all(c, V(c, "oovv"), c.get("TGoovv"));
   }
   *e2 = E[0] + E[1] + E[2] + E[3] + E[4] + E[5];
   if (c.opt.print) {

@@ -618,6 +618,7 @@ CCSDResult run_ccsd(Ctx& c) {
   res.converged = converged;
   c.stats.fp64_iterations = fp64_iters;
   c.have_ccsd = res.converged;
+  c.have_tgrad = false;  // new amplitudes: earlier (T) gradient pieces no longer apply
   return res;
 }
 

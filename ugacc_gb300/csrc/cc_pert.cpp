@@ -544,6 +544,12 @@ Tensor named_tensor(Ctx& c, const std::string& name) {
   if (name == "t2") return amp2(c, c.get("T").p);
   if (name == "l1") return amp1(c, c.get("Lam").p);
   if (name == "l2") return amp2(c, c.get("Lam").p);
+  if (name == "s1") return c.get("TS1");
+  if (name == "s2") return c.get("TS2");
+  static const char* tg[][2] = {{"DooT", "TDoo"},     {"DvvT", "TDvv"},     {"DovT", "TDov"},
+                                {"GoovvT", "TGoovv"}, {"GooovT", "TGooov"}, {"GvvvoT", "TGvvvo"}};
+  for (auto& p : tg)
+    if (name == p[0]) return c.get(p[1]);
   static const char* direct[] = {"tau",   "Doo",   "Dvv",   "Dov",   "Dvo",   "Hov",   "Hoo",  "Hvv",
                                  "Hoooo", "Hvvvv", "Hvovv", "Hooov", "Hovvo", "Hovov", "Hvvvo", "Hovoo"};
   for (const char* d : direct)

@@ -125,6 +125,7 @@ struct Ctx {
 
   int no = 0, nv = 0, naux = 0;
   bool loaded = false, have_ccsd = false, have_hbar = false, have_lambda = false;
+  bool have_tgrad = false;  // (T) gradient pieces present: Lambda and the densities include them
   std::vector<double> eps;  // orbital energies (diagonal of the Fock matrix)
   std::vector<double> fock;  // [nact][nact]
 

@@ -1,0 +1,241 @@
+// (T) contributions to CCSD(T) first derivatives: tgrad_ooc of ccwfn.cc:1150-1316.
+//
+// For every ordered occupied triple (i,j,k) the connected and disconnected triples
+//   M3(abc) = W3_ijk(abc) / D3,   N3(abc) = [<ij|ab> t1_kc + <ik|ac> t1_jb + <jk|bc> t1_ia
+//                                           + t2_ijab f_kc + t2_ikac f_jb + t2_jkbc f_ia] / D3
+// (ccwfn.cc:1420-1454, 1492-1515) give
+//   X3 = 8M(abc) - 4M(bac) - 4M(acb) - 4M(cba) + 2M(cab) + 2M(bca),  Y3 the same of N3,
+//   Z3 = 2(M(abc) - M(acb)) - (M(bac) - M(bca)),  Q3 = 2 X3 + Y3,
+// and the pieces
+//   Dvv[a][a] += 1/2 sum_bc M3 (X3+Y3)          Dov[i][a] += sum_bc (M3 - M3(cba)) (4 t2_jkbc - 2 t2_jkcb)
+//   s1[i][a]  += sum_bc (4M - 4M(bac) - 2M(acb) + 2M(cab)) <jk|bc>
+//   Goovv[i][j][a][b] += 4 sum_c t1_kc Z3        X2[i][l][a][b] -= sum_c Q3 <jk|lc>
+//   Gooov[j][i][l][a] -= sum_bc Q3 t2_lkbc       X2[i][j][a][d] += sum_bc Q3 <dk|bc>
+//   Gvvvo[a][b][d][j] += sum_c Q3 t2_kicd        s2 = X2 + X2(ji,ba)
+// The reference's second pass over (a,b,c) (:1226-1250) forms the same M3 and N3 values
+// indexed by the occupied triple; because M3 and N3 are invariant under a simultaneous
+// permutation of (i,j,k) and (a,b,c), its occupied-permutation X3/Y3 equal the virtual
+// ones here, so Doo[i][i] -= 1/2 sum_{jk,abc} M3 (X3+Y3) reuses the Dvv partial sums.
+//
+// Tuples are processed in batches (fixed i, a range of j, every k); W3 comes from the
+// FP64 tuple GEMMs of the (T) energy, the element-wise work from the kernels below, and
+// the four O(no^3 nv^4)-class sums from the contraction engine.  FP64 throughout.
+#include <algorithm>
+
+#include "cc.h"
+#include "engine.h"
+
+namespace ucc {
+
+void count_kernel_launch();
+void triples_operands_fp64(Ctx& c, Tensor& Acat, Tensor& Bcat);
+void triples_w3_fp64(Ctx& c, const Tensor& Acat, const Tensor& Bcat, const int* h_tuples, int nb, double* W3,
+                     GemmPtrs* d_ptrs);
+
+namespace {
+
+// W3 -> M3 in place; N3
+__global__ void tg_prep_kernel(int no, int nv, int nt, const int* __restrict__ tuples, double* M, double* N,
+                               const double* __restrict__ eps, const double* __restrict__ t1,
+                               const double* __restrict__ t2, const double* __restrict__ Voovv,
+                               const double* __restrict__ fov) {
+  const int64_t nv2 = (int64_t)nv * nv, nv3 = nv2 * nv, total = (int64_t)nt * nv3;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (int64_t)gridDim.x * blockDim.x) {
+    const int t = (int)(x / nv3);
+    int64_t r = x - (int64_t)t * nv3;
+    const int a = (int)(r / nv2);
+    r -= (int64_t)a * nv2;
+    const int b = (int)(r / nv), c = (int)(r - (int64_t)b * nv);
+    const int i = tuples[3 * t], j = tuples[3 * t + 1], k = tuples[3 * t + 2];
+    const double* ev = eps + no;
+    double D = eps[i] + eps[j] + eps[k];
+    D -= ev[a] + ev[b] + ev[c];
+    const int64_t ij = ((int64_t)i * no + j) * nv2, ik = ((int64_t)i * no + k) * nv2, jk = ((int64_t)j * no + k) * nv2;
+    const double num = Voovv[ij + (int64_t)a * nv + b] * t1[(int64_t)k * nv + c] +
+                       Voovv[ik + (int64_t)a * nv + c] * t1[(int64_t)j * nv + b] +
+                       Voovv[jk + (int64_t)b * nv + c] * t1[(int64_t)i * nv + a] +
+                       t2[ij + (int64_t)a * nv + b] * fov[(int64_t)k * nv + c] +
+                       t2[ik + (int64_t)a * nv + c] * fov[(int64_t)j * nv + b] +
+                       t2[jk + (int64_t)b * nv + c] * fov[(int64_t)i * nv + a];
+    M[x] = M[x] / D;
+    N[x] = num / D;
+  }
+}
+
+__device__ double block_sum(double v) {
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) / 32;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+  if (w == 0)
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// one block per (a, tuple): Q3 and Z3 of the a-slice, and the per-(tuple, a) sums of the
+// Dvv diagonal, Dov and s1 terms
+__global__ void tg_reduce_kernel(int no, int nv, const int* __restrict__ tuples, const double* __restrict__ M,
+                                 const double* __restrict__ N, const double* __restrict__ t2,
+                                 const double* __restrict__ Voovv, double* Q, double* Z, double* pdvv, double* pdov,
+                                 double* ps1) {
+  const int a = blockIdx.x, t = blockIdx.y;
+  const int j = tuples[3 * t + 1], k = tuples[3 * t + 2];
+  const int64_t nv2 = (int64_t)nv * nv, nv3 = nv2 * nv;
+  const double* m = M + (int64_t)t * nv3;
+  const double* n = N + (int64_t)t * nv3;
+  const double* t2jk = t2 + ((int64_t)j * no + k) * nv2;
+  const double* vjk = Voovv + ((int64_t)j * no + k) * nv2;
+  double* q = Q + (int64_t)t * nv3 + (int64_t)a * nv2;
+  double* z = Z + (int64_t)t * nv3 + (int64_t)a * nv2;
+  double sdvv = 0.0, sdov = 0.0, ss1 = 0.0;
+  auto at = [&](const double* A, int x, int y, int w) { return A[((int64_t)x * nv + y) * nv + w]; };
+  for (int e = threadIdx.x; e < nv2; e += blockDim.x) {
+    const int b = e / nv, c = e - b * nv;
+    const double mabc = at(m, a, b, c), mbac = at(m, b, a, c), macb = at(m, a, c, b);
+    const double mcba = at(m, c, b, a), mcab = at(m, c, a, b), mbca = at(m, b, c, a);
+    const double X3 = 8.0 * mabc - 4.0 * mbac - 4.0 * macb - 4.0 * mcba + 2.0 * mcab + 2.0 * mbca;
+    const double Y3 = 8.0 * at(n, a, b, c) - 4.0 * at(n, b, a, c) - 4.0 * at(n, a, c, b) - 4.0 * at(n, c, b, a) +
+                      2.0 * at(n, c, a, b) + 2.0 * at(n, b, c, a);
+    q[e] = 2.0 * X3 + Y3;
+    z[e] = 2.0 * (mabc - macb) - (mbac - mbca);
+    sdvv += 0.5 * mabc * (X3 + Y3);
+    sdov += (mabc - mcba) * (4.0 * t2jk[(int64_t)b * nv + c] - 2.0 * t2jk[(int64_t)c * nv + b]);
+    ss1 += (4.0 * mabc - 4.0 * mbac - 2.0 * macb + 2.0 * mcab) * vjk[(int64_t)b * nv + c];
+  }
+  sdvv = block_sum(sdvv);
+  sdov = block_sum(sdov);
+  ss1 = block_sum(ss1);
+  if (threadIdx.x == 0) {
+    pdvv[(int64_t)t * nv + a] = sdvv;
+    pdov[(int64_t)t * nv + a] = sdov;
+    ps1[(int64_t)t * nv + a] = ss1;
+  }
+}
+
+// fixed-order sums over the batch's tuples (all share the first index i)
+__global__ void tg_accumulate_kernel(int no, int nv, int nt, int i, const double* __restrict__ pdvv,
+                                     const double* __restrict__ pdov, const double* __restrict__ ps1, double* Dvv,
+                                     double* Dov, double* s1, double* Doo) {
+  double sdoo = 0.0;
+  for (int a = threadIdx.x; a < nv; a += blockDim.x) {
+    double dv = 0.0, dov = 0.0, s = 0.0;
+    for (int t = 0; t < nt; t++) {
+      dv += pdvv[(int64_t)t * nv + a];
+      dov += pdov[(int64_t)t * nv + a];
+      s += ps1[(int64_t)t * nv + a];
+    }
+    Dvv[(int64_t)a * nv + a] += dv;
+    Dov[(int64_t)i * nv + a] += dov;
+    s1[(int64_t)i * nv + a] += s;
+    sdoo += dv;
+  }
+  sdoo = block_sum(sdoo);
+  if (threadIdx.x == 0) Doo[(int64_t)i * no + i] -= sdoo;
+}
+
+Tensor select(const Tensor& T, int axis, int64_t idx) {  // T with one axis fixed
+  Tensor r;
+  r.p = T.p + idx * T.s[axis];
+  r.rank = T.rank - 1;
+  for (int k = 0, o = 0; k < T.rank; k++) {
+    if (k == axis) continue;
+    r.d[o] = T.d[k];
+    r.s[o] = T.s[k];
+    o++;
+  }
+  return r;
+}
+
+}  // namespace
+
+void run_triples_gradient(Ctx& c) {
+  UCC_REQUIRE(c.have_ccsd, UCC_BAD_STATE, "the (T) gradient needs converged CCSD amplitudes");
+  Fp64Scope fp64(c);
+  const int no = c.no, nv = c.nv;
+  const int64_t nv2 = (int64_t)nv * nv, nv3 = nv2 * nv;
+  double* T = c.get("T").p;
+  Tensor t1 = amp1(c, T), t2 = amp2(c, T);
+  Tensor S1 = c.alloc("TS1", {no, nv}, true);
+  Tensor X2 = c.alloc("TX2", {no, no, nv, nv}, true);
+  Tensor Doo = c.alloc("TDoo", {no, no}, true);
+  Tensor Dvv = c.alloc("TDvv", {nv, nv}, true);
+  Tensor Dov = c.alloc("TDov", {no, nv}, true);
+  Tensor Goovv = c.alloc("TGoovv", {no, no, nv, nv}, true);
+  Tensor Gooov = c.alloc("TGooov", {no, no, no, nv}, true);
+  Tensor Gvvvo = c.alloc("TGvvvo", {nv, nv, nv, no}, true);
+  Tensor Acat, Bcat;
+  triples_operands_fp64(c, Acat, Bcat);
+
+  // batch = (fixed i, nj values of j, every k): M3, N3, Q3, Z3 of each tuple plus the
+  // engine's gathered copies of Q3 / Z3
+  size_t free_b = 0, total_b = 0;
+  UCC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const double budget = std::min<double>(24.0e9, 0.3 * (double)free_b);
+  const int nj = (int)std::max<int64_t>(1, std::min<int64_t>(no, (int64_t)(budget / (6.0 * 8.0 * nv3 * no))));
+  const int ntmax = nj * no;
+  Scratch Mb(c, sizeof(double) * nv3 * ntmax), Nb(c, sizeof(double) * nv3 * ntmax);
+  Scratch Qb(c, sizeof(double) * nv3 * ntmax), Zb(c, sizeof(double) * nv3 * ntmax);
+  Scratch part(c, sizeof(double) * 3 * (size_t)ntmax * nv);
+  Scratch dtup(c, sizeof(int) * 3 * ntmax);
+  Scratch dptr(c, sizeof(GemmPtrs) * 6 * ntmax);
+  double* pdvv = part.d();
+  double* pdov = pdvv + (size_t)ntmax * nv;
+  double* ps1 = pdov + (size_t)ntmax * nv;
+  const double* eps = c.get("eps").p;
+  const double* Voovv = c.get("Voovv").p;
+  const double* fov = Fk(c, "ov").p;
+  Tensor Vooov = c.get("Vooov"), Vvovv = V(c, "vovv");
+  std::vector<int> tuples;
+  for (int i = 0; i < no; i++) {
+    for (int j0 = 0; j0 < no; j0 += nj) {
+      const int nb = std::min(nj, no - j0), nt = nb * no;
+      tuples.clear();
+      for (int j = j0; j < j0 + nb; j++)
+        for (int k = 0; k < no; k++) {
+          tuples.push_back(i);
+          tuples.push_back(j);
+          tuples.push_back(k);
+        }
+      UCC_CUDA(cudaMemcpyAsync(dtup.p, tuples.data(), sizeof(int) * tuples.size(), cudaMemcpyHostToDevice, c.stream));
+      triples_w3_fp64(c, Acat, Bcat, tuples.data(), nt, Mb.d(), static_cast<GemmPtrs*>(dptr.p));
+      const int64_t total = (int64_t)nt * nv3;
+      const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 152 * 32));
+      tg_prep_kernel<<<g, 256, 0, c.stream>>>(no, nv, nt, static_cast<int*>(dtup.p), Mb.d(), Nb.d(), eps, t1.p, t2.p,
+                                             Voovv, fov);
+      count_kernel_launch();
+      UCC_REQUIRE(nt <= 65535, UCC_BAD_ARGS, "(T) gradient: too many tuples per batch");
+      tg_reduce_kernel<<<dim3((unsigned)nv, (unsigned)nt), 256, 0, c.stream>>>(
+          no, nv, static_cast<int*>(dtup.p), Mb.d(), Nb.d(), t2.p, Voovv, Qb.d(), Zb.d(), pdvv, pdov, ps1);
+      count_kernel_launch();
+      tg_accumulate_kernel<<<1, 256, 0, c.stream>>>(no, nv, nt, i, pdvv, pdov, ps1, Dvv.p, Dov.p, S1.p, Doo.p);
+      count_kernel_launch();
+      UCC_CUDA(cudaGetLastError());
+      const Tensor Q = make_view(Qb.d(), {nb, no, nv, nv, nv}), Z = make_view(Zb.d(), {nb, no, nv, nv, nv});
+      // Goovv[i][j][a][b] += 4 sum_kc t1[k][c] Z3
+      contract(c, "jkabc,kc->jab", 4.0, Z, t1, 1.0, narrow(Goovv.slice0(i), 0, j0, nb));
+      // X2[i][l][a][b] -= sum_jkc Q3 <jk|lc>
+      contract(c, "jkabc,jklc->lab", -1.0, Q, narrow(Vooov, 0, j0, nb), 1.0, X2.slice0(i));
+      // Gooov[j][i][l][a] -= sum_kbc Q3 t2[l][k][b][c]
+      contract(c, "jkabc,lkbc->jla", -1.0, Q, t2, 1.0, select(narrow(Gooov, 0, j0, nb), 1, i));
+      // X2[i][j][a][d] += sum_kbc Q3 <dk|bc>
+      contract(c, "jkabc,dkbc->jad", 1.0, Q, Vvovv, 1.0, narrow(X2.slice0(i), 0, j0, nb));
+      // Gvvvo[a][b][d][j] += sum_kc Q3 t2[k][i][c][d]
+      contract(c, "jkabc,kcd->abdj", 1.0, Q, select(t2, 1, i), 1.0, narrow(Gvvvo, 3, j0, nb));
+    }
+  }
+  // s2 = X2 + X2(ji,ba)
+  Tensor S2 = c.alloc("TS2", {no, no, nv, nv}, false);
+  transpose_add(c, "jiba->ijab", 1.0, X2, 0.0, S2);
+  axpby(c, S2.size(), 1.0, X2.p, 1.0, S2.p);
+  UCC_CUDA(cudaStreamSynchronize(c.stream));
+  c.drop("TX2");
+  c.drop("T3_A");
+  c.drop("T3_B");
+  c.have_tgrad = true;
+}
+
+}  // namespace ucc

@@ -24,12 +24,58 @@ bool mixed_triples_batch(Ctx& c, int nbatch, const int* h_tuples, float* W3);
 bool mixed_triples_prepare(Ctx& c, int max_batch);
 void mixed_triples_release(Ctx& c);
 
+// FP64 operands: A_x (no x (nv+no) x nv^2) and B_yz (no^2 x (nv+no) x nv), as stored
+// blocks "T3_A" / "T3_B" (dropped by the caller)
+void triples_operands_fp64(Ctx& c, Tensor& Acat, Tensor& Bcat) {
+  const int no = c.no, nv = c.nv;
+  const int64_t nv2 = (int64_t)nv * nv, Kp = nv + no;
+  Tensor t2 = amp2(c, c.get("T").p);
+  Acat = c.alloc("T3_A", {no, Kp, nv2}, false);
+  Tensor Ae = narrow(Acat, 1, 0, nv), Am = narrow(Acat, 1, nv, no);
+  permute_add(c, make_view(c.get("Vovvv").p, {no, nv, nv2}), 1.0, 0.0, Ae);
+  permute_add(c, make_view(t2.p, {no, no, nv2}), -1.0, 0.0, Am);
+  Bcat = c.alloc("T3_B", {no, no, Kp, nv}, false);
+  Tensor Be = narrow(Bcat, 2, 0, nv), Bm = narrow(Bcat, 2, nv, no);
+  permute_add(c, view(t2, "yzce->yzec"), 1.0, 0.0, Be);
+  permute_add(c, view(c.get("Vooov"), "zymc->yzmc"), 1.0, 0.0, Bm);
+}
+
+// W3 of nb tuples (host triples (i,j,k)) into W3 + b*nv^3, FP64; d_ptrs holds 6*nb
+// pointer triples and is reused: the call synchronises before returning
+void triples_w3_fp64(Ctx& c, const Tensor& Acat, const Tensor& Bcat, const int* h_tuples, int nb, double* W3,
+                     GemmPtrs* d_ptrs) {
+  const int no = c.no, nv = c.nv;
+  const int64_t nv2 = (int64_t)nv * nv, nv3 = nv2 * nv, Kp = nv + no;
+  TriplesTerm terms[6];
+  triples_terms(nv, terms);
+  std::vector<GemmPtrs> all((size_t)nb * 6);
+  for (int q = 0; q < 6; q++)
+    for (int b = 0; b < nb; b++) {
+      const int* ijk = h_tuples + 3 * b;
+      const TriplesTerm& tm = terms[q];
+      all[(size_t)q * nb + b] = {Acat.p + (int64_t)ijk[tm.x] * Kp * nv2,
+                                 Bcat.p + ((int64_t)ijk[tm.y] * no + ijk[tm.z]) * Kp * nv, W3 + (int64_t)b * nv3};
+    }
+  UCC_CUDA(cudaMemcpyAsync(d_ptrs, all.data(), sizeof(GemmPtrs) * all.size(), cudaMemcpyHostToDevice, c.stream));
+  for (int q = 0; q < 6; q++) {
+    GemmEpilogue epi;
+    epi.msplit = nv;
+    epi.s_mhi = terms[q].su;
+    epi.s_mlo = terms[q].sv;
+    epi.s_n = terms[q].sw;
+    dgemm_strided(c, nv2, nv, Kp, 1.0, nullptr, 1, nv2, nullptr, nv, 1, q == 0 ? 0.0 : 1.0, nullptr, epi, nb, 0, 0, 0,
+                  d_ptrs + (size_t)q * nb);
+  }
+  // the pointer array is reused by the next batch: keep the copy ordered after use
+  UCC_CUDA(cudaStreamSynchronize(c.stream));
+}
+
 double run_triples(Ctx& c) {
   UCC_REQUIRE(c.have_ccsd, UCC_BAD_STATE, "(T) needs converged CCSD amplitudes");
   const int no = c.no, nv = c.nv;
-  const int64_t nv2 = (int64_t)nv * nv, nv3 = nv2 * nv, Kp = nv + no;
+  const int64_t nv2 = (int64_t)nv * nv, nv3 = nv2 * nv;
   double* T = c.get("T").p;
-  Tensor t1 = amp1(c, T), t2 = amp2(c, T);
+  Tensor t1 = amp1(c, T);
 
   std::vector<int> tuples;
   for (int i = 0; i < no; i++)
@@ -51,49 +97,17 @@ double run_triples(Ctx& c) {
   Scratch partial(c, sizeof(double) * (size_t)ntup * nv);
 
   const bool mixed = c.opt.precision == UCC_MIXED && !c.force_fp64 && mixed_triples_prepare(c, batch);
-  // FP64 path: concatenated operands A_x (no x (nv+no) x nv^2) and B_yz (no^2 x (nv+no) x nv)
+  // FP64 path: concatenated operands A_x and B_yz
   Tensor Acat, Bcat;
-  if (!mixed) {
-    Acat = c.alloc("T3_A", {no, Kp, nv2}, false);
-    Tensor Ae = narrow(Acat, 1, 0, nv), Am = narrow(Acat, 1, nv, no);
-    permute_add(c, make_view(c.get("Vovvv").p, {no, nv, nv2}), 1.0, 0.0, Ae);
-    permute_add(c, make_view(t2.p, {no, no, nv2}), -1.0, 0.0, Am);
-    Bcat = c.alloc("T3_B", {no, no, Kp, nv}, false);
-    Tensor Be = narrow(Bcat, 2, 0, nv), Bm = narrow(Bcat, 2, nv, no);
-    permute_add(c, view(t2, "yzce->yzec"), 1.0, 0.0, Be);
-    permute_add(c, view(c.get("Vooov"), "zymc->yzmc"), 1.0, 0.0, Bm);
-  }
-  TriplesTerm terms[6];
-  triples_terms(nv, terms);
+  if (!mixed) triples_operands_fp64(c, Acat, Bcat);
   Scratch dptr(c, sizeof(GemmPtrs) * batch * 6);
   GemmPtrs* dp = static_cast<GemmPtrs*>(dptr.p);
   for (int t0 = 0; t0 < ntup; t0 += batch) {
     const int nb = std::min(batch, ntup - t0);
-    if (mixed) {
+    if (mixed)
       mixed_triples_batch(c, nb, tuples.data() + 3 * t0, static_cast<float*>(W3.p));
-    } else {
-      std::vector<GemmPtrs> all((size_t)nb * 6);
-      for (int q = 0; q < 6; q++)
-        for (int b = 0; b < nb; b++) {
-          const int* ijk = &tuples[3 * (t0 + b)];
-          const TriplesTerm& tm = terms[q];
-          all[(size_t)q * nb + b] = {Acat.p + (int64_t)ijk[tm.x] * Kp * nv2,
-                                     Bcat.p + ((int64_t)ijk[tm.y] * no + ijk[tm.z]) * Kp * nv,
-                                     W3.d() + (int64_t)b * nv3};
-        }
-      UCC_CUDA(cudaMemcpyAsync(dp, all.data(), sizeof(GemmPtrs) * all.size(), cudaMemcpyHostToDevice, c.stream));
-      for (int q = 0; q < 6; q++) {
-        GemmEpilogue epi;
-        epi.msplit = nv;
-        epi.s_mhi = terms[q].su;
-        epi.s_mlo = terms[q].sv;
-        epi.s_n = terms[q].sw;
-        dgemm_strided(c, nv2, nv, Kp, 1.0, nullptr, 1, nv2, nullptr, nv, 1, q == 0 ? 0.0 : 1.0, nullptr, epi, nb, 0,
-                      0, 0, dp + (size_t)q * nb);
-      }
-      // the pointer array is reused by the next batch: keep the copy ordered after use
-      UCC_CUDA(cudaStreamSynchronize(c.stream));
-    }
+    else
+      triples_w3_fp64(c, Acat, Bcat, tuples.data() + 3 * t0, nb, W3.d(), dp);
     if (mixed)
       triples_energy_f32(c, no, nv, nb, static_cast<int*>(dtup.p) + 3 * t0, static_cast<const float*>(W3.p), t1.p,
                          c.get("Voovv").p, c.get("eps").p, partial.d() + (int64_t)t0 * nv);
