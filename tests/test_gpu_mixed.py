@@ -93,3 +93,27 @@ def test_mixed_lambda_and_response_match_fp64(hand):
     assert st["tc_gemm_launches"] > 0
     assert abs(pmx - p64) < 1e-9
     assert abs(amx - a64) < 1e-8 * max(1.0, abs(a64))
+
+
+def _tgrad_pipeline(h, precision):
+    H = U.Hamiltonian.from_synthetic(h)
+    cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": precision, "WFN": "CCSD_T", "DERTYPE": "FIRST"})
+    e = cc.compute_energy()
+    no, nv = h.no, h.nv
+    s1, s2 = H.ctx.get("s1", (no, nv)), H.ctx.get("s2", (no, no, nv, nv))
+    hb = U.HBAR(H, cc)
+    lam = U.CCLambda(cc, hb)
+    lam.compute_lambda()
+    dens = U.CCDensity(cc, lam)
+    return e, s1, s2, dens.onepdm() + dens.twopdm(), H.ctx.stats()
+
+
+def test_mixed_triples_gradient_matches_fp64():
+    h = make_hamiltonian(6, 64, 21)
+    e64, s1_64, s2_64, ed64, _ = _tgrad_pipeline(h, "FP64")
+    emx, s1_mx, s2_mx, edmx, st = _tgrad_pipeline(h, "MIXED")
+    assert st["tc_gemm_launches"] > 0
+    assert abs(ed64 - e64) < 1e-9 and abs(edmx - emx) < 2e-8  # E(density) = E_CCSD(T)
+    np.testing.assert_allclose(s1_mx, s1_64, atol=1e-4 * np.abs(s1_64).max(), rtol=0)
+    np.testing.assert_allclose(s2_mx, s2_64, atol=1e-4 * np.abs(s2_64).max(), rtol=0)
+    assert abs(edmx - ed64) < 1e-7

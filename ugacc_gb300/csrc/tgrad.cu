@@ -19,8 +19,11 @@
 //
 // Tuples are processed in batches (fixed i, a range of j, every k); W3 comes from the
 // FP64 tuple GEMMs of the (T) energy, the element-wise work from the kernels below, and
-// the four O(no^3 nv^4)-class sums from the contraction engine.  FP64 throughout.
+// the four O(no^3 nv^4)-class sums from the contraction engine.  FP64, or with MIXED
+// precision W3 from the tensor-core tuple GEMMs and split contractions (the pieces are
+// small corrections that enter Lambda and the densities linearly).
 #include <algorithm>
+#include <memory>
 
 #include "cc.h"
 #include "engine.h"
@@ -28,14 +31,18 @@
 namespace ucc {
 
 void count_kernel_launch();
+bool mixed_triples_batch(Ctx& c, int nbatch, const int* h_tuples, float* W3);
+bool mixed_triples_prepare(Ctx& c, int max_batch);
+void mixed_triples_release(Ctx& c);
 void triples_operands_fp64(Ctx& c, Tensor& Acat, Tensor& Bcat);
 void triples_w3_fp64(Ctx& c, const Tensor& Acat, const Tensor& Bcat, const int* h_tuples, int nb, double* W3,
                      GemmPtrs* d_ptrs);
 
 namespace {
 
-// W3 -> M3 in place; N3
-__global__ void tg_prep_kernel(int no, int nv, int nt, const int* __restrict__ tuples, double* M, double* N,
+// W3 (FP64, or FP32 from the tensor-core tuple GEMMs) -> M3; N3
+template <typename TW>
+__global__ void tg_prep_kernel(int no, int nv, int nt, const int* __restrict__ tuples, const TW* W, double* M, double* N,
                                const double* __restrict__ eps, const double* __restrict__ t1,
                                const double* __restrict__ t2, const double* __restrict__ Voovv,
                                const double* __restrict__ fov) {
@@ -57,7 +64,7 @@ __global__ void tg_prep_kernel(int no, int nv, int nt, const int* __restrict__ t
                        t2[ij + (int64_t)a * nv + b] * fov[(int64_t)k * nv + c] +
                        t2[ik + (int64_t)a * nv + c] * fov[(int64_t)j * nv + b] +
                        t2[jk + (int64_t)b * nv + c] * fov[(int64_t)i * nv + a];
-    M[x] = M[x] / D;
+    M[x] = (double)W[x] / D;
     N[x] = num / D;
   }
 }
@@ -154,7 +161,6 @@ Tensor select(const Tensor& T, int axis, int64_t idx) {  // T with one axis fixe
 
 void run_triples_gradient(Ctx& c) {
   UCC_REQUIRE(c.have_ccsd, UCC_BAD_STATE, "the (T) gradient needs converged CCSD amplitudes");
-  Fp64Scope fp64(c);
   const int no = c.no, nv = c.nv;
   const int64_t nv2 = (int64_t)nv * nv, nv3 = nv2 * nv;
   double* T = c.get("T").p;
@@ -167,8 +173,9 @@ void run_triples_gradient(Ctx& c) {
   Tensor Goovv = c.alloc("TGoovv", {no, no, nv, nv}, true);
   Tensor Gooov = c.alloc("TGooov", {no, no, no, nv}, true);
   Tensor Gvvvo = c.alloc("TGvvvo", {nv, nv, nv, no}, true);
-  Tensor Acat, Bcat;
-  triples_operands_fp64(c, Acat, Bcat);
+  // MIXED: W3 from the tensor-core tuple GEMMs (FP32 W3) and split contractions; the
+  // element-wise algebra and every accumulation stay FP64
+  const bool mixed = c.opt.precision == UCC_MIXED && !c.force_fp64;
 
   // batch = (fixed i, nj values of j, every k): M3, N3, Q3, Z3 of each tuple plus the
   // engine's gathered copies of Q3 / Z3
@@ -177,6 +184,11 @@ void run_triples_gradient(Ctx& c) {
   const double budget = std::min<double>(24.0e9, 0.3 * (double)free_b);
   const int nj = (int)std::max<int64_t>(1, std::min<int64_t>(no, (int64_t)(budget / (6.0 * 8.0 * nv3 * no))));
   const int ntmax = nj * no;
+  Tensor Acat, Bcat;
+  const bool tc = mixed && mixed_triples_prepare(c, ntmax);
+  if (!tc) triples_operands_fp64(c, Acat, Bcat);
+  std::unique_ptr<Scratch> W32;
+  if (tc) W32 = std::make_unique<Scratch>(c, sizeof(float) * nv3 * ntmax);
   Scratch Mb(c, sizeof(double) * nv3 * ntmax), Nb(c, sizeof(double) * nv3 * ntmax);
   Scratch Qb(c, sizeof(double) * nv3 * ntmax), Zb(c, sizeof(double) * nv3 * ntmax);
   Scratch part(c, sizeof(double) * 3 * (size_t)ntmax * nv);
@@ -201,11 +213,18 @@ void run_triples_gradient(Ctx& c) {
           tuples.push_back(k);
         }
       UCC_CUDA(cudaMemcpyAsync(dtup.p, tuples.data(), sizeof(int) * tuples.size(), cudaMemcpyHostToDevice, c.stream));
-      triples_w3_fp64(c, Acat, Bcat, tuples.data(), nt, Mb.d(), static_cast<GemmPtrs*>(dptr.p));
       const int64_t total = (int64_t)nt * nv3;
       const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 152 * 32));
-      tg_prep_kernel<<<g, 256, 0, c.stream>>>(no, nv, nt, static_cast<int*>(dtup.p), Mb.d(), Nb.d(), eps, t1.p, t2.p,
-                                             Voovv, fov);
+      if (tc) {
+        mixed_triples_batch(c, nt, tuples.data(), static_cast<float*>(W32->p));
+        tg_prep_kernel<float><<<g, 256, 0, c.stream>>>(no, nv, nt, static_cast<int*>(dtup.p),
+                                                       static_cast<const float*>(W32->p), Mb.d(), Nb.d(), eps, t1.p,
+                                                       t2.p, Voovv, fov);
+      } else {
+        triples_w3_fp64(c, Acat, Bcat, tuples.data(), nt, Mb.d(), static_cast<GemmPtrs*>(dptr.p));
+        tg_prep_kernel<double><<<g, 256, 0, c.stream>>>(no, nv, nt, static_cast<int*>(dtup.p), Mb.d(), Mb.d(),
+                                                        Nb.d(), eps, t1.p, t2.p, Voovv, fov);
+      }
       count_kernel_launch();
       UCC_REQUIRE(nt <= 65535, UCC_BAD_ARGS, "(T) gradient: too many tuples per batch");
       tg_reduce_kernel<<<dim3((unsigned)nv, (unsigned)nt), 256, 0, c.stream>>>(
@@ -233,8 +252,12 @@ void run_triples_gradient(Ctx& c) {
   axpby(c, S2.size(), 1.0, X2.p, 1.0, S2.p);
   UCC_CUDA(cudaStreamSynchronize(c.stream));
   c.drop("TX2");
-  c.drop("T3_A");
-  c.drop("T3_B");
+  if (tc) {
+    mixed_triples_release(c);
+  } else {
+    c.drop("T3_A");
+    c.drop("T3_B");
+  }
   c.have_tgrad = true;
 }
 
