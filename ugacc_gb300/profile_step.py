@@ -33,6 +33,7 @@ def main(argv=None):
     ap.add_argument("--response", action="store_true",
                     help="CCSD, HBAR, Lambda, densities and the static + dynamic dipole polarizability "
                          "(3 symmetric perturbations, omega 0 and 0.0656, right-hand solves)")
+    ap.add_argument("--tgrad", action="store_true", help="with --triples: also the (T) gradient pieces")
     ap.add_argument("--ccsd-fp64", action="store_true",
                     help="with --triples: converge CCSD in FP64, then run (T) at --precision")
     a = ap.parse_args(argv)
@@ -67,6 +68,11 @@ def main(argv=None):
             cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": prec})
         H.ctx.reset_stats()
         e_t = cc.triples()
+        if a.tgrad:
+            st_t = H.ctx.stats()
+            H.ctx.reset_stats()
+            cc.triples_gradient()
+            print(json.dumps({"tgrad_ms": H.ctx.stats()["triples_ms"], "triples_ms": st_t["triples_ms"]}))
         print(json.dumps({"e_ccsd": e_cc, "e_t": e_t, "ccsd_ms": st_cc["ccsd_ms"],
                           "ccsd_iterations": st_cc["ccsd_iterations"], "fp64_iterations": st_cc["fp64_iterations"],
                           "mixed_iterations": st_cc["mixed_iterations"],
