@@ -42,7 +42,11 @@ typedef struct ucc_ctx ucc_ctx;
  * contractions (particle ladder, rings, (T)) as BF16 hi+lo split products with FP32
  * accumulation on the tensor cores and keeps denominators, updates, DIIS, norms and
  * energies in FP64, followed by FP64 refinement sweeps. */
-typedef enum ucc_precision { UCC_FP64 = 0, UCC_MIXED = 1 } ucc_precision;
+typedef enum ucc_precision {
+  UCC_FP64 = 0,
+  UCC_MIXED = 1,
+  UCC_MIXED_FINE = 2 /* ucc_gemm only: three-part split, K in FP64-summed chunks (refinement corrections) */
+} ucc_precision;
 
 /* Solver options: the reference's psi4 options (ugacc.cc:57-68) plus the new ones. */
 typedef struct ucc_options {

@@ -117,3 +117,16 @@ def test_mixed_triples_gradient_matches_fp64():
     np.testing.assert_allclose(s1_mx, s1_64, atol=1e-4 * np.abs(s1_64).max(), rtol=0)
     np.testing.assert_allclose(s2_mx, s2_64, atol=1e-4 * np.abs(s2_64).max(), rtol=0)
     assert abs(edmx - ed64) < 1e-7
+
+
+def test_fine_split_gemm_matches_fp64():
+    """UCC_MIXED_FINE: three-part split, K in chunks summed in FP64 (in-kernel chunks)."""
+    rng = np.random.default_rng(8)
+    ctx = U.Context()
+    for (M, N, K) in [(200, 300, 500), (256, 512, 4096)]:
+        A, B = rng.standard_normal((M, K)), rng.standard_normal((K, N))
+        C0 = rng.standard_normal((M, N))
+        ref = 0.5 * A @ B + 0.25 * C0
+        got = ctx.gemm(A, B, C0, alpha=0.5, beta=0.25, precision=U.MIXED_FINE)
+        scale = 0.5 * np.abs(A) @ np.abs(B)
+        assert np.all(np.abs(got - ref) <= SPLIT_RTOL * scale + 1e-12)

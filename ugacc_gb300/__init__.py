@@ -23,7 +23,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "ugacc_gb300.h")
 UCC_OK, UCC_NOT_CONVERGED = 0, 1
 STATUS = {0: "ok", 1: "not converged", 2: "nan detected", 3: "out of memory", 4: "bad arguments",
           5: "bad state", 6: "cuda error", 7: "device timeout", 8: "unsupported"}
-FP64, MIXED = 0, 1
+FP64, MIXED, MIXED_FINE = 0, 1, 2
 LEFT, RIGHT = 0, 1
 
 

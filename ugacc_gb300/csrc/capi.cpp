@@ -8,6 +8,9 @@
 namespace ucc {
 void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                  const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi);
+void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi, int parts,
+                 int kc);
 }
 
 using namespace ucc;
@@ -300,7 +303,8 @@ ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t
                     double alpha, const double* A, const double* B, double beta, double* C) {
   return guard(ctx, [&](Ctx& c) {
     UCC_REQUIRE(A && B && C && M >= 1 && N >= 1 && K >= 1, UCC_BAD_ARGS, "ucc_gemm: bad arguments");
-    UCC_REQUIRE(precision == UCC_FP64 || precision == UCC_MIXED, UCC_BAD_ARGS, "ucc_gemm: bad precision");
+    UCC_REQUIRE(precision == UCC_FP64 || precision == UCC_MIXED || precision == UCC_MIXED_FINE, UCC_BAD_ARGS,
+                "ucc_gemm: bad precision");
     UCC_CUDA(cudaSetDevice(c.device));
     Scratch dA(c, sizeof(double) * M * K), dB(c, sizeof(double) * K * N), dC(c, sizeof(double) * M * N);
     UCC_CUDA(cudaMemcpyAsync(dA.p, A, sizeof(double) * M * K, cudaMemcpyHostToDevice, c.stream));
@@ -313,6 +317,8 @@ ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t
     epi.s_n = 1;
     if (precision == UCC_MIXED)
       tc_gemm_run(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi);
+    else if (precision == UCC_MIXED_FINE)
+      tc_gemm_run(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi, 3, 16);
     else
       dgemm_strided(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi, 1, 0, 0, 0, nullptr);
     UCC_CUDA(cudaMemcpyAsync(C, dC.p, sizeof(double) * M * N, cudaMemcpyDeviceToHost, c.stream));

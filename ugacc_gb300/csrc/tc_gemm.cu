@@ -67,7 +67,26 @@ struct Params {
   // C32 != null: FP32 output C32[off] = alpha * acc (+ C32[off] when beta != 0), no FP64
   // work in the epilogue (GB300 issues ~4 FP64 operations per clock per SM)
   float* C32;
+  // nparts = 3: operands split hi + mid + lo (third maps), six products hi.hi, hi.mid,
+  // mid.hi, hi.lo, mid.mid, lo.hi (representation error ~2^-25 instead of ~2^-17)
+  int nparts;
+  // kc > 0: the K range of every tile runs in chunks of kc K blocks, each chunk's FP32
+  // accumulator added into the FP64 output by the epilogue (the first with beta, the
+  // rest with 1), which bounds the FP32 accumulation chain; FP64 output only
+  int kc;
 };
+
+// the split products of one K block: (A part, B part), part 0 = hi, 1 = lo (2 parts) or
+// 0 = hi, 1 = mid, 2 = lo (3 parts)
+__device__ __forceinline__ void seg_parts(int nparts, int seg, int& pa, int& pb) {
+  if (nparts == 3) {  // A parts 0,0,1,0,1,2 and B parts 0,1,0,2,1,0, two bits per segment
+    pa = (2320 >> (2 * seg)) & 3;
+    pb = (388 >> (2 * seg)) & 3;
+  } else {
+    pa = seg == 2 ? 1 : 0;
+    pb = seg == 1 ? 1 : 0;
+  }
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ unsigned long long gtimer() {
@@ -153,7 +172,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
 __global__ void __launch_bounds__(THREADS, 1)
     gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
                 const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
-                const __grid_constant__ CUtensorMap mA2hi, const __grid_constant__ CUtensorMap mA2lo, Params p) {
+                const __grid_constant__ CUtensorMap mA2hi, const __grid_constant__ CUtensorMap mA2lo,
+                const __grid_constant__ CUtensorMap mAmid, const __grid_constant__ CUtensorMap mBmid, Params p) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = smem;
@@ -187,6 +207,9 @@ __global__ void __launch_bounds__(THREADS, 1)
   const uint32_t tmem = *tslot;
   const int tiles_per = p.mtiles * p.ntiles;
   const int ntile = tiles_per * (p.nprob ? p.nprob : (p.ksplit > 1 ? p.ksplit : 1));
+  const int nseg = p.nparts == 3 ? 6 : 3;
+  // K chunks of one tile (in-kernel chunking) and the K blocks of chunk ch
+  const int nch = p.kc > 0 ? (p.kblocks + p.kc - 1) / p.kc : 1;
 
   if (warp == 0) {
     if (lane == 0) {
@@ -199,26 +222,35 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int mt = tl % p.mtiles, nt = tl / p.mtiles;
         const int ar0 = (p.nprob ? p.a_row0[pb] : 0) + mt * BM, br0 = (p.nprob ? p.b_row0[pb] : 0) + nt * BN;
         const int ar1 = p.nterms > 1 ? p.a_row1[pb] + mt * BM : 0, br1 = p.nterms > 1 ? p.b_row1[pb] + nt * BN : 0;
-        int k0 = 0, kn = p.kblocks;
-        if (p.ksplit > 1) {
-          k0 = pb * p.kchunk;
-          kn = min(p.kblocks - k0, p.kchunk);
-        }
-        for (int kb = 0; kb < p.nterms * 3 * kn; kb++) {
-          if (!mbar_wait(&empty[stage], phase ^ 1u, p.err)) {
-            ok = false;
-            break;
+        for (int ch = 0; ch < nch && ok; ch++) {
+          int k0 = 0, kn = p.kblocks;
+          if (p.ksplit > 1) {
+            k0 = pb * p.kchunk;
+            kn = min(p.kblocks - k0, p.kchunk);
+          } else if (p.kc > 0) {
+            k0 = ch * p.kc;
+            kn = min(p.kblocks - k0, p.kc);
           }
-          const int term = kb / (3 * kn), w = kb - term * 3 * kn;
-          const int part = w / kn, kk = (k0 + w - part * kn) * BK;
-          const CUtensorMap* ma = term == 0 ? (part < 2 ? &mAhi : &mAlo) : (part < 2 ? &mA2hi : &mA2lo);
-          mbar_expect_tx(&full[stage], A_BYTES + B_BYTES);
-          tma_load(sA + stage * A_BYTES, ma, &full[stage], kk, term == 0 ? ar0 : ar1);
-          tma_load(sB + stage * B_BYTES, part == 1 ? &mBlo : &mBhi, &full[stage], kk, term == 0 ? br0 : br1);
-          ++issued;
-          if (++stage == STAGES) {
-            stage = 0;
-            phase ^= 1u;
+          for (int kb = 0; kb < p.nterms * nseg * kn; kb++) {
+            if (!mbar_wait(&empty[stage], phase ^ 1u, p.err)) {
+              ok = false;
+              break;
+            }
+            const int term = kb / (nseg * kn), w = kb - term * nseg * kn;
+            const int seg = w / kn, kk = (k0 + w - seg * kn) * BK;
+            int pa, pbp;
+            seg_parts(p.nparts, seg, pa, pbp);
+            const CUtensorMap* ma = term == 0 ? (pa == 0 ? &mAhi : (pa == 1 && p.nparts == 3) ? &mAmid : &mAlo)
+                                              : (pa == 0 ? &mA2hi : &mA2lo);
+            const CUtensorMap* mb = pbp == 0 ? &mBhi : (pbp == 1 && p.nparts == 3) ? &mBmid : &mBlo;
+            mbar_expect_tx(&full[stage], A_BYTES + B_BYTES);
+            tma_load(sA + stage * A_BYTES, ma, &full[stage], kk, term == 0 ? ar0 : ar1);
+            tma_load(sB + stage * B_BYTES, mb, &full[stage], kk, term == 0 ? br0 : br1);
+            ++issued;
+            if (++stage == STAGES) {
+              stage = 0;
+              phase ^= 1u;
+            }
           }
         }
       }
@@ -233,31 +265,39 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t phase = 0, aphase = 0;
       bool ok = true;
       for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
-        int kn = p.kblocks;
-        if (p.ksplit > 1) kn = min(p.kblocks - (tile / tiles_per) * p.kchunk, p.kchunk);
-        if (!mbar_wait(&tempty[acc], aphase ^ 1u, p.err)) break;
-        fence_after();
-        const uint32_t d = tmem + (uint32_t)(acc * BN);
-        for (int kb = 0; kb < p.nterms * 3 * kn; kb++) {
-          if (!mbar_wait(&full[stage], phase, p.err)) {
+        for (int ch = 0; ch < nch && ok; ch++) {
+          int kn = p.kblocks;
+          if (p.ksplit > 1)
+            kn = min(p.kblocks - (tile / tiles_per) * p.kchunk, p.kchunk);
+          else if (p.kc > 0)
+            kn = min(p.kblocks - ch * p.kc, p.kc);
+          if (!mbar_wait(&tempty[acc], aphase ^ 1u, p.err)) {
             ok = false;
             break;
           }
           fence_after();
-          const uint64_t ad = sdesc(sA + stage * A_BYTES), bd = sdesc(sB + stage * B_BYTES);
+          const uint32_t d = tmem + (uint32_t)(acc * BN);
+          for (int kb = 0; kb < p.nterms * nseg * kn; kb++) {
+            if (!mbar_wait(&full[stage], phase, p.err)) {
+              ok = false;
+              break;
+            }
+            fence_after();
+            const uint64_t ad = sdesc(sA + stage * A_BYTES), bd = sdesc(sB + stage * B_BYTES);
 #pragma unroll
-          for (int k = 0; k < BK / 16; k++)  // +32 bytes along K per 16-element step
-            mma(d, ad + (uint64_t)(k * 2), bd + (uint64_t)(k * 2), (kb | k) != 0);
-          mma_commit(&empty[stage]);
-          if (++stage == STAGES) {
-            stage = 0;
-            phase ^= 1u;
+            for (int k = 0; k < BK / 16; k++)  // +32 bytes along K per 16-element step
+              mma(d, ad + (uint64_t)(k * 2), bd + (uint64_t)(k * 2), (kb | k) != 0);
+            mma_commit(&empty[stage]);
+            if (++stage == STAGES) {
+              stage = 0;
+              phase ^= 1u;
+            }
           }
-        }
-        mma_commit(&tfull[acc]);
-        if (++acc == 2) {
-          acc = 0;
-          aphase ^= 1u;
+          mma_commit(&tfull[acc]);
+          if (++acc == 2) {
+            acc = 0;
+            aphase ^= 1u;
+          }
         }
       }
     }
@@ -266,15 +306,21 @@ __global__ void __launch_bounds__(THREADS, 1)
     int acc = 0;
     uint32_t aphase = 0;
     const GemmEpilogue ep = p.epi;
-    for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x)
+    for (int kch = 0; kch < nch; kch++) {
       const int pb = tile / tiles_per, tl = tile - pb * tiles_per;
       const int mt = tl % p.mtiles, nt = tl / p.mtiles;
       const int64_t coff = p.nprob ? p.c_off[pb] : (p.ksplit > 1 ? (int64_t)pb * p.M * p.N : 0);
-      if (!mbar_wait(&tfull[acc], aphase, p.err)) break;
+      if (!mbar_wait(&tfull[acc], aphase, p.err)) {
+        ok = false;
+        break;
+      }
       fence_after();
       const int64_t m = (int64_t)mt * BM + q * 32 + lane;
       const int64_t mo = ep.msplit ? (m / ep.msplit) * ep.s_mhi + (m % ep.msplit) * ep.s_mlo : m * ep.s_mhi;
-      const double alpha = p.alpha, beta = p.beta;
+      // later K chunks of a tile add onto the earlier ones
+      const double alpha = p.alpha, beta = kch == 0 ? p.beta : 1.0;
       for (int ch = 0; ch < BN / 32; ch++) {
         uint32_t r[32];
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + ch * 32), r);
@@ -331,15 +377,22 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 // FP64 rows x cols view (strides sr, sk) -> bf16 hi/lo [rows][kp], zero padded to kp
+// (mid != null: three parts, x = hi + mid + lo, each the bf16 rounding of what remains)
 __global__ void split_kernel(int64_t rows, int64_t cols, int64_t kp, const double* x, int64_t sr, int64_t sk,
-                             __nv_bfloat16* hi, __nv_bfloat16* lo) {
+                             __nv_bfloat16* hi, __nv_bfloat16* lo, __nv_bfloat16* mid) {
   const int64_t n = rows * kp;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = i / kp, k = i - r * kp;
     const double v = k < cols ? x[r * sr + k * sk] : 0.0;
     const __nv_bfloat16 h = __double2bfloat16(v);
     hi[i] = h;
-    lo[i] = __double2bfloat16(v - (double)__bfloat162float(h));
+    double rest = v - (double)__bfloat162float(h);
+    if (mid) {
+      const __nv_bfloat16 m = __double2bfloat16(rest);
+      mid[i] = m;
+      rest -= (double)__bfloat162float(m);
+    }
+    lo[i] = __double2bfloat16(rest);
   }
 }
 
@@ -349,15 +402,17 @@ __global__ void split_kernel(int64_t rows, int64_t cols, int64_t kp, const doubl
 struct Split {
   __nv_bfloat16* hi = nullptr;
   __nv_bfloat16* lo = nullptr;
+  __nv_bfloat16* mid = nullptr;  // three-part splits only
   int64_t rows = 0, kp = 0;
-  CUtensorMap mhi, mlo;
+  CUtensorMap mhi, mlo, mmid;
   ~Split() {
     if (hi) cudaFree(hi);
     if (lo) cudaFree(lo);
+    if (mid) cudaFree(mid);
   }
 };
 
-using Key = std::tuple<const double*, int64_t, int64_t, int64_t, int64_t, int>;
+using Key = std::tuple<const double*, int64_t, int64_t, int64_t, int64_t, int, int>;
 struct Triples;
 struct Cache {
   std::map<Key, std::unique_ptr<Split>> ops;
@@ -411,10 +466,10 @@ static Cache& cache(Ctx& c) {
 
 // split (and cache when the source is a constant block) a rows x cols FP64 operand
 static Split* prepare(Ctx& c, const double* x, int64_t rows, int64_t cols, int64_t sr, int64_t sk, int box_rows,
-                      std::unique_ptr<Split>& temp) {
+                      std::unique_ptr<Split>& temp, int parts = 2) {
   Cache& k = cache(c);
   const bool constant = c.is_constant(x);
-  Key key{x, rows, cols, sr, sk, box_rows};
+  Key key{x, rows, cols, sr, sk, box_rows, parts};
   if (constant) {
     auto it = k.ops.find(key);
     if (it != k.ops.end()) return it->second.get();
@@ -424,13 +479,15 @@ static Split* prepare(Ctx& c, const double* x, int64_t rows, int64_t cols, int64
   s->kp = (cols + BK - 1) / BK * BK;
   UCC_CUDA(cudaMalloc(&s->hi, sizeof(__nv_bfloat16) * rows * s->kp));
   UCC_CUDA(cudaMalloc(&s->lo, sizeof(__nv_bfloat16) * rows * s->kp));
+  if (parts == 3) UCC_CUDA(cudaMalloc(&s->mid, sizeof(__nv_bfloat16) * rows * s->kp));
   const int64_t n = rows * s->kp;
   const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)k.sms * 16);
-  split_kernel<<<blocks, 256, 0, c.stream>>>(rows, cols, s->kp, x, sr, sk, s->hi, s->lo);
+  split_kernel<<<blocks, 256, 0, c.stream>>>(rows, cols, s->kp, x, sr, sk, s->hi, s->lo, s->mid);
   count_kernel_launch();
   UCC_CUDA(cudaGetLastError());
   make_map(&s->mhi, s->hi, rows, s->kp, box_rows);
   make_map(&s->mlo, s->lo, rows, s->kp, box_rows);
+  if (parts == 3) make_map(&s->mmid, s->mid, rows, s->kp, box_rows);
   Split* raw = s.get();
   if (constant)
     k.ops[key] = std::move(s);
@@ -442,12 +499,14 @@ static Split* prepare(Ctx& c, const double* x, int64_t rows, int64_t cols, int64
 }  // namespace tc
 
 void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
-                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi) {
+                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi, int parts,
+                 int kc) {
   using namespace tc;
+  UCC_REQUIRE(parts == 2 || parts == 3, UCC_BAD_ARGS, "tensor-core GEMM: 2 or 3 split parts");
   Cache& k = cache(c);
   std::unique_ptr<Split> ta, tb;
-  Split* a = prepare(c, A, M, K, sAm, sAk, BM, ta);
-  Split* b = prepare(c, B, N, K, sBn, sBk, BN, tb);
+  Split* a = prepare(c, A, M, K, sAm, sAk, BM, ta, parts);
+  Split* b = prepare(c, B, N, K, sBn, sBk, BN, tb, parts);
   if (!k.attr_set) {
     UCC_CUDA(cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     k.attr_set = true;
@@ -471,7 +530,8 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
   const int tiles = p.mtiles * p.ntiles;
   // too few output tiles for the SMs and a long K: split K, FP64 partials, fixed-order reduce
   std::unique_ptr<Scratch> part;
-  if (tiles * 2 <= k.sms && p.kblocks >= 8) {
+  p.kc = kc > 0 && kc < p.kblocks ? kc : 0;
+  if (p.kc == 0 && tiles * 2 <= k.sms && p.kblocks >= 8) {
     int ks = std::min(k.sms / tiles, p.kblocks / 4);
     if (ks > 1) {
       p.kchunk = (p.kblocks + ks - 1) / ks;
@@ -490,7 +550,9 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
   p.nterms = 1;
   p.a_row1 = p.b_row1 = nullptr;
   p.C32 = nullptr;
-  gemm_kernel<<<grid, THREADS, SMEM_BYTES, c.stream>>>(a->mhi, a->mlo, b->mhi, b->mlo, a->mhi, a->mlo, p);
+  p.nparts = parts;
+  gemm_kernel<<<grid, THREADS, SMEM_BYTES, c.stream>>>(a->mhi, a->mlo, b->mhi, b->mlo, a->mhi, a->mlo,
+                                                      parts == 3 ? a->mmid : a->mhi, parts == 3 ? b->mmid : b->mhi, p);
   count_kernel_launch();
   c.stats.tc_gemm_launches++;
   UCC_CUDA(cudaGetLastError());
@@ -509,6 +571,11 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
   }
 }
 
+void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi) {
+  tc_gemm_run(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, 2, 0);
+}
+
 bool tc_eligible(int64_t M, int64_t N, int64_t K) {
   // small problems stay on the FP64 path; the tensor tile is 128 x 256 x 64
   if (std::max(M, N) < 64 || K < 16 || (double)M * N * K < 1e7) return false;
@@ -517,25 +584,25 @@ bool tc_eligible(int64_t M, int64_t N, int64_t K) {
 
 void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
                       int64_t sAk, const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm,
-                      int64_t sCn) {
+                      int64_t sCn, int parts, int kc) {
   GemmEpilogue epi;
   epi.msplit = 0;
   if (M < 128 && N > M) {
     // short M: compute C^T = B^T A^T so that the long side fills the 128-row MMA tile
     epi.s_mhi = sCn;
     epi.s_n = sCm;
-    tc_gemm_run(c, N, M, K, alpha, B, sBn, sBk, A, sAk, sAm, beta, C, epi);
+    tc_gemm_run(c, N, M, K, alpha, B, sBn, sBk, A, sAk, sAm, beta, C, epi, parts, kc);
   } else {
     epi.s_mhi = sCm;
     epi.s_n = sCn;
-    tc_gemm_run(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi);
+    tc_gemm_run(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, parts, kc);
   }
 }
 
 bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn) {
   if (!tc_eligible(M, N, K)) return false;
-  tc_gemm_oriented(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, sCm, sCn);
+  tc_gemm_oriented(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, sCm, sCn, 2, 0);
   return true;
 }
 
@@ -704,8 +771,10 @@ bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, float* W3) {
     p.b_row1 = T.d_brow + nb;
     const int tiles = p.mtiles * p.ntiles * nb;
     UCC_CUDA(cudaEventRecord(k.ev0, c.stream));
+    p.nparts = 2;
+    p.kc = 0;
     gemm_kernel<<<std::min(tiles, k.sms), THREADS, SMEM_BYTES, c.stream>>>(T.A.mhi, T.A.mlo, T.B.mhi, T.B.mlo,
-                                                                          T.A2.mhi, T.A2.mlo, p);
+                                                                          T.A2.mhi, T.A2.mlo, T.A.mhi, T.B.mhi, p);
     count_kernel_launch();
     c.stats.tc_gemm_launches++;
     UCC_CUDA(cudaGetLastError());
