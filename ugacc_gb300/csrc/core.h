@@ -289,6 +289,15 @@ void triples_energy(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, con
 void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, const double* t1,
                         const double* Voovv, const double* eps, double* d_partial);
 
+// Pair-symmetric particle ladder (sum_ef <ab|ef> tau_ijef = S + sign A over packed pairs):
+// Vp[a<=b][e<=f] = <ab|ef> + <ab|fe> (<ab|ee> on e == f), Vm[a<b][e<f] = <ab|ef> - <ab|fe>;
+// Tp[i<=j][e<=f] = (tau_ijef + tau_ijfe)/2 (tau_ijee on e == f), Tm[i<j][e<f] = (tau_ijef - tau_ijfe)/2;
+// R2[ijab] += S[ij][ab] + sign A[ij][ab] over the sorted pairs.  Pairs p <= q are
+// numbered q(q+1)/2 + p, strict pairs q(q-1)/2 + p.
+void pack_vvvv(Ctx& c, int nv, const double* V, double* Vp, double* Vm);
+void pack_tau(Ctx& c, int no, int nv, const double* tau, double* Tp, double* Tm);
+void unpack_ladder(Ctx& c, int no, int nv, const double* S, const double* A, double* R2);
+
 int64_t launches();  // kernels launched by this library so far (all contexts)
 
 }  // namespace ucc

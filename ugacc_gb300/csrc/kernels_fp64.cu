@@ -686,6 +686,118 @@ __global__ void triples_energy_f32_kernel(int no, int nv, const int* tuples, con
 }
 }  // namespace
 
+// ------------------------------------------------------------------------------------
+// Pair-symmetric particle ladder.  Pairs p <= q are numbered q(q+1)/2 + p, strict pairs
+// p < q are numbered q(q-1)/2 + p.
+// ------------------------------------------------------------------------------------
+namespace {
+__device__ __forceinline__ void pair_le(int64_t P, int& p, int& q) {
+  int j = (int)((sqrt(8.0 * (double)P + 1.0) - 1.0) * 0.5);
+  while ((int64_t)(j + 1) * (j + 2) / 2 <= P) j++;
+  while ((int64_t)j * (j + 1) / 2 > P) j--;
+  q = j;
+  p = (int)(P - (int64_t)j * (j + 1) / 2);
+}
+__device__ __forceinline__ void pair_lt(int64_t Q, int& p, int& q) {
+  int j = (int)((sqrt(8.0 * (double)Q + 1.0) + 1.0) * 0.5);
+  while ((int64_t)j * (j + 1) / 2 <= Q) j++;
+  while (j > 1 && (int64_t)(j - 1) * j / 2 > Q) j--;
+  q = j;
+  p = (int)(Q - (int64_t)j * (j - 1) / 2);
+}
+
+// Vp[ab][ef] = <ab|ef> + <ab|fe> (e < f), <ab|ee> (e == f), a <= b;  Vm[ab][ef] = <ab|ef> - <ab|fe>, a < b, e < f
+__global__ void pack_vvvv_kernel(int nv, const double* __restrict__ V, double* Vp, double* Vm) {
+  const int64_t np = (int64_t)nv * (nv + 1) / 2, nm = (int64_t)nv * (nv - 1) / 2;
+  const int64_t nv2 = (int64_t)nv * nv;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < np * np + nm * nm;
+       x += (int64_t)gridDim.x * blockDim.x) {
+    int a, b, e, f;
+    if (x < np * np) {
+      pair_le(x / np, a, b);
+      pair_le(x % np, e, f);
+      const double* v = V + ((int64_t)a * nv + b) * nv2;
+      Vp[x] = e == f ? v[(int64_t)e * nv + e] : v[(int64_t)e * nv + f] + v[(int64_t)f * nv + e];
+    } else {
+      const int64_t y = x - np * np;
+      pair_lt(y / nm, a, b);
+      pair_lt(y % nm, e, f);
+      const double* v = V + ((int64_t)a * nv + b) * nv2;
+      Vm[y] = v[(int64_t)e * nv + f] - v[(int64_t)f * nv + e];
+    }
+  }
+}
+
+// Tp[ij][ef] = (tau_ijef + tau_ijfe)/2 (e < f), tau_ijee (e == f), i <= j;  Tm = (tau_ijef - tau_ijfe)/2, i < j, e < f
+__global__ void pack_tau_kernel(int no, int nv, const double* __restrict__ tau, double* Tp, double* Tm) {
+  const int64_t op = (int64_t)no * (no + 1) / 2, om = (int64_t)no * (no - 1) / 2;
+  const int64_t vp = (int64_t)nv * (nv + 1) / 2, vm = (int64_t)nv * (nv - 1) / 2;
+  const int64_t nv2 = (int64_t)nv * nv;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < op * vp + om * vm;
+       x += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, e, f;
+    if (x < op * vp) {
+      pair_le(x / vp, i, j);
+      pair_le(x % vp, e, f);
+      const double* t = tau + ((int64_t)i * no + j) * nv2;
+      Tp[x] = e == f ? t[(int64_t)e * nv + e] : 0.5 * (t[(int64_t)e * nv + f] + t[(int64_t)f * nv + e]);
+    } else {
+      const int64_t y = x - op * vp;
+      pair_lt(y / vm, i, j);
+      pair_lt(y % vm, e, f);
+      const double* t = tau + ((int64_t)i * no + j) * nv2;
+      Tm[y] = 0.5 * (t[(int64_t)e * nv + f] - t[(int64_t)f * nv + e]);
+    }
+  }
+}
+
+// R2[ijab] += S[(i,j) sorted][(a,b) sorted] + sign * A[...], sign = (-1)^[i>j] (-1)^[a>b],
+// A = 0 on i == j or a == b
+__global__ void unpack_ladder_kernel(int no, int nv, const double* __restrict__ S, const double* __restrict__ A,
+                                     double* R2) {
+  const int64_t n = (int64_t)no * no * nv * nv;
+  const int64_t vp = (int64_t)nv * (nv + 1) / 2, vm = (int64_t)nv * (nv - 1) / 2;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(x % nv);
+    int64_t r = x / nv;
+    const int a = (int)(r % nv);
+    r /= nv;
+    const int j = (int)(r % no), i = (int)(r / no);
+    const int i0 = min(i, j), j0 = max(i, j), a0 = min(a, b), b0 = max(a, b);
+    double v = S[((int64_t)j0 * (j0 + 1) / 2 + i0) * vp + (int64_t)b0 * (b0 + 1) / 2 + a0];
+    if (i != j && a != b) {
+      const double am = A[((int64_t)j0 * (j0 - 1) / 2 + i0) * vm + (int64_t)b0 * (b0 - 1) / 2 + a0];
+      v += ((i > j) != (a > b)) ? -am : am;
+    }
+    R2[x] += v;
+  }
+}
+}  // namespace
+
+void pack_vvvv(Ctx& c, int nv, const double* V, double* Vp, double* Vm) {
+  UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
+  const int64_t np = (int64_t)nv * (nv + 1) / 2, nm = (int64_t)nv * (nv - 1) / 2;
+  pack_vvvv_kernel<<<grid_for(np * np + nm * nm), 256, 0, c.stream>>>(nv, V, Vp, Vm);
+  count_launch();
+  check_launch("pack_vvvv");
+}
+
+void pack_tau(Ctx& c, int no, int nv, const double* tau, double* Tp, double* Tm) {
+  UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
+  const int64_t n = (int64_t)no * (no + 1) / 2 * nv * (nv + 1) / 2 + (int64_t)no * (no - 1) / 2 * nv * (nv - 1) / 2;
+  pack_tau_kernel<<<grid_for(n), 256, 0, c.stream>>>(no, nv, tau, Tp, Tm);
+  count_launch();
+  check_launch("pack_tau");
+}
+
+void unpack_ladder(Ctx& c, int no, int nv, const double* S, const double* A, double* R2) {
+  UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
+  const int64_t n = (int64_t)no * no * nv * nv;
+  unpack_ladder_kernel<<<grid_for(n), 256, 0, c.stream>>>(no, nv, S, A, R2);
+  count_launch();
+  check_launch("unpack_ladder");
+}
+
 void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, const double* t1,
                         const double* Voovv, const double* eps, double* d_partial) {
   UCC_REQUIRE(ntuple <= 65535, UCC_BAD_ARGS, "triples_energy: too many tuples per batch");
