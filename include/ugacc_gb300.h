@@ -45,7 +45,9 @@ typedef struct ucc_ctx ucc_ctx;
 typedef enum ucc_precision {
   UCC_FP64 = 0,
   UCC_MIXED = 1,
-  UCC_MIXED_FINE = 2 /* ucc_gemm only: three-part split, K in FP64-summed chunks (refinement corrections) */
+  UCC_MIXED_FINE = 2, /* ucc_gemm only: three-part split, K in FP64-summed chunks (refinement corrections) */
+  UCC_FP64_SLICED = 3 /* ucc_gemm only: FP64-accurate product of exact bf16 slices on the tensor cores (the
+                         form the FP64 work of MIXED solves runs in) */
 } ucc_precision;
 
 /* Solver options: the reference's psi4 options (ugacc.cc:57-68) plus the new ones. */
@@ -57,6 +59,9 @@ typedef struct ucc_options {
   int refine_sweeps;      /* FP64 sweeps after a MIXED solve, default 2 */
   int print;              /* 0 silent, 1 iteration table on stdout */
   double mixed_switch;    /* MIXED: residual norm at which FP64 sweeps take over, default 1e-5 */
+  int ooc;                /* OOC, default 0 as the plugin (ugacc.cc:67): the (T) gradient's Doo and Dvv
+                             are full matrices (tgrad, ccwfn.cc:998-1021); 1: their diagonals only
+                             (tgrad_ooc, ccwfn.cc:1203,1247). Every other piece is the same. */
 } ucc_options;
 
 void ucc_options_default(ucc_options* opt);
@@ -77,8 +82,9 @@ ucc_status ucc_ccsd(ucc_ctx* ctx, double* e_ccsd, int* iterations);
  * equals tcorr_ooc (:745-793) and tcorr (:647-743). */
 ucc_status ucc_triples(ucc_ctx* ctx, double* e_t);
 
-/* Replaces: CCWfn::tgrad_ooc (ccwfn.cc:1150-1316), run by compute_energy for
- * WFN=CCSD_T, DERTYPE=FIRST (:252-255): the (T) pieces of the CCSD(T) first derivatives.
+/* Replaces: CCWfn::tgrad (ccwfn.cc:854-1142, OOC=0) and CCWfn::tgrad_ooc (:1150-1316, OOC=1),
+ * run by compute_energy for WFN=CCSD_T, DERTYPE=FIRST (:252-255): the (T) pieces of the
+ * CCSD(T) first derivatives, computed triple by triple in both cases (T3/L3 are never stored).
  * Afterwards ucc_lambda adds s1 / s2/2 to its residuals (cclambda.cc:181,243) and
  * ucc_density starts from the (T) parts of Doo, Dvv, Dov, Goovv, Gooov, Gvvvo
  * (ccdensity.cc:44-69), until the next ucc_ccsd.  Tensors: "s1" "s2" "DooT" "DvvT" "DovT"
@@ -211,6 +217,9 @@ typedef struct ucc_stats {
   double fp64_gemm_ms;       /* device time of the FP64 GEMM launches (CUDA events) */
   double fp64_gemm_flops;    /* their algorithmic FLOPs, 2*M*N*K per GEMM */
   int64_t fp64_gemm_launches;
+  double sliced_gemm_ms;     /* device time of the sliced FP64 tensor-core GEMMs (slicing included) */
+  double sliced_gemm_flops;  /* their algorithmic FLOPs, 2*M*N*K per GEMM */
+  int64_t sliced_gemm_launches;
 } ucc_stats;
 ucc_status ucc_get_stats(ucc_ctx* ctx, ucc_stats* out);
 ucc_status ucc_reset_stats(ucc_ctx* ctx);

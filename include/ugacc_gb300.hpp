@@ -40,7 +40,7 @@ struct Options {
   std::string wfn = "CCSD", dertype = "NONE", myhand = "RIGHT", precision = "FP64";
   int maxiter = 100, refine_sweeps = 2, print = 0;
   double r_convergence = 1e-7, my_omega = 0.0, mixed_switch = 1e-5;
-  bool diis = true;
+  bool diis = true, ooc = false;
 };
 
 class Hamiltonian {
@@ -79,6 +79,7 @@ class CCWfn {
     u.refine_sweeps = o.refine_sweeps;
     u.print = o.print;
     u.mixed_switch = o.mixed_switch;
+    u.ooc = o.ooc ? 1 : 0;
     check(H_->ctx(), ucc_set_options(H_->ctx(), &u));
   }
   // ccwfn.cc:188-258: CCSD correlation energy, plus (T) for WFN == CCSD_T

@@ -301,8 +301,12 @@ class CCWfn:
                 + ein("bc,a->abc", Voovv[j, k], t1[i]) + ein("ab,c->abc", t2[i, j], fov[k])
                 + ein("ac,b->abc", t2[i, k], fov[j]) + ein("bc,a->abc", t2[j, k], fov[i]))
 
-    def tgrad(self):  # ccwfn.cc:1150-1316 (tgrad_ooc)
-        """s1, s2 and the (T) density pieces; M3 = W3/D3 and N3 over every ordered (i,j,k)."""
+    def tgrad(self, ooc: bool = False):  # ccwfn.cc:1150-1316 (tgrad_ooc), :854-1142 (tgrad)
+        """s1, s2 and the (T) density pieces; M3 = W3/D3 and N3 over every ordered (i,j,k).
+
+        ooc=True follows tgrad_ooc (Doo, Dvv diagonal); ooc=False (the plugin's default,
+        ugacc.cc:67) the in-core tgrad, whose stored t3 is M3 and whose l3 contracts like
+        X3 + Y3, giving the full Doo and Dvv of ccwfn.cc:998-1021."""
         H, t1, t2 = self.H, self.t1, self.t2
         no, nv = H.no, H.nv
         eo, ev = np.diag(H.f)[:no], np.diag(H.f)[no:]
@@ -352,6 +356,9 @@ class CCWfn:
         No = N.transpose(3, 4, 5, 0, 1, 2)
         Xo, Yo = perm6(Mo, (8.0, 4.0, 2.0)), perm6(No, (8.0, 4.0, 2.0))
         Doo[np.arange(no), np.arange(no)] -= 0.5 * ein("abcijk,abcijk->i", Mo, Xo + Yo)
+        if not ooc:  # ccwfn.cc:999-1021
+            Doo = -0.5 * ein("ilmdef,jlmdef->ij", M, X + Y)
+            Dvv = 0.5 * ein("ijkbde,ijkade->ab", M, X + Y)
         s2 = X2 + X2.transpose(1, 0, 3, 2)
         self.tg = dict(s1=s1, s2=s2, Doo=Doo, Dvv=Dvv, Dov=Dov, Goovv=Goovv, Gooov=Gooov, Gvvvo=Gvvvo)
         return self.tg

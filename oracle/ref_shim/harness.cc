@@ -109,7 +109,8 @@ int main(int argc, char** argv) {
   }
   std::map<std::string, std::string> kv = {{"WFN", "CCSD"},     {"DERTYPE", "NONE"},    {"MAXITER", "100"},
                                            {"R_CONVERGENCE", "1e-10"}, {"DIIS", "1"},   {"TRIPLES", "none"},
-                                           {"MY_OMEGA", "0.0"}, {"MYHAND", "RIGHT"},    {"DUMP", "0"}};
+                                           {"MY_OMEGA", "0.0"}, {"MYHAND", "RIGHT"},    {"DUMP", "0"},
+                                           {"OOC", "1"}};
   for (int k = 3; k < argc; k++) {
     std::string a = argv[k];
     auto eq = a.find('=');
@@ -143,7 +144,7 @@ int main(int argc, char** argv) {
     options.set_int("MAXITER", std::atoi(kv["MAXITER"].c_str()));
     options.set_double("R_CONVERGENCE", std::atof(kv["R_CONVERGENCE"].c_str()));
     options.set_bool("DIIS", kv["DIIS"] == "1");
-    options.set_bool("OOC", true);
+    options.set_bool("OOC", kv["OOC"] == "1");  // the plugin's default is false (ugacc.cc:67)
     options.set_double("MY_OMEGA", std::atof(kv["MY_OMEGA"].c_str()));
 
     auto ref = std::make_shared<Wavefunction>(options);
@@ -174,7 +175,7 @@ int main(int argc, char** argv) {
     out.mat("t1", cc->t1_, no, nv);
     out.t4("t2", cc->t2_, no, no, nv, nv);
     if (kv["WFN"] == "CCSD_T" && kv["DERTYPE"] == "FIRST") {
-      // (T) gradient pieces left by compute_energy's tgrad_ooc (ccwfn.cc:252-255)
+      // (T) gradient pieces left by compute_energy's tgrad_ooc or tgrad (ccwfn.cc:252-255)
       out.mat("s1", cc->s1_, no, nv);
       out.t4("s2", cc->s2_, no, no, nv, nv);
       out.mat("DooT", cc->Doo_, no, no);

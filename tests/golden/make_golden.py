@@ -56,8 +56,12 @@ CASES = {
     "mid": (6, 40, 5, [("ccsd_t", dict(DERTYPE="NONE", TRIPLES="all"), ["t1"])]),
     # CCSD(T) first derivatives: the (T) gradient pieces (s1, s2, (T) densities), the
     # Lambda equations with s1/s2 and the densities that start from the (T) pieces
+    # (OOC=1: tcorr_ooc + tgrad_ooc; OOC=0, the plugin's default: tcorr + tgrad over stored T3/L3)
     "tgrad": (4, 11, 9, [("ccsd_t_first", dict(WFN="CCSD_T", DERTYPE="FIRST"),
                           ["t1", "t2", "s1", "s2", "DooT", "DvvT", "DovT", "GoovvT", "GooovT", "GvvvoT",
+                           "l1", "l2", "Doo", "Dvv", "Dov"]),
+                         ("ccsd_t_first_incore", dict(WFN="CCSD_T", DERTYPE="FIRST", OOC="0"),
+                          ["s1", "s2", "DooT", "DvvT", "DovT", "GoovvT", "GooovT", "GvvvoT",
                            "l1", "l2", "Doo", "Dvv", "Dov"])]),
 }
 BIG = {

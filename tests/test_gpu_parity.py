@@ -128,13 +128,15 @@ def test_stage_order_is_enforced():
     assert e.value.status == 5
 
 
-def test_triples_gradient_vs_reference():
-    """WFN=CCSD_T, DERTYPE=FIRST: s1, s2 and the (T) density pieces (ccwfn.cc:1150-1316),
-    then Lambda with s1/s2 and the densities starting from the (T) pieces."""
+@pytest.mark.parametrize("tag,ooc", [("ccsd_t_first", True), ("ccsd_t_first_incore", False)])
+def test_triples_gradient_vs_reference(tag, ooc):
+    """WFN=CCSD_T, DERTYPE=FIRST: s1, s2 and the (T) density pieces of tgrad_ooc
+    (ccwfn.cc:1150-1316, OOC=1) or tgrad (:854-1142, OOC=0: full Doo/Dvv), then Lambda
+    with s1/s2 and the densities starting from the (T) pieces."""
     meta, arr = load("tgrad")
     h, _ = hamiltonian(meta)
-    tag, run = next(iter(meta["runs"].items()))
-    H, cc = gpu_pipeline(h, WFN="CCSD_T", DERTYPE="FIRST")
+    run = meta["runs"][tag]
+    H, cc = gpu_pipeline(h, WFN="CCSD_T", DERTYPE="FIRST", OOC=ooc)
     assert abs(cc.eccsd + cc.et - run["e_ccsd"]) < ETOL
     no, nv = h.no, h.nv
     shapes = {"s1": (no, nv), "s2": (no, no, nv, nv), "DooT": (no, no), "DvvT": (nv, nv), "DovT": (no, nv),
@@ -160,11 +162,11 @@ def test_triples_gradient_vs_reference():
 def test_triples_gradient_vs_oracle_larger():
     """The same pieces at no=5, nv=24 (several tuple batches) against the oracle."""
     h = make_hamiltonian(5, 24, 31)
-    H, cc = gpu_pipeline(h, WFN="CCSD_T", DERTYPE="FIRST")
+    H, cc = gpu_pipeline(h, WFN="CCSD_T", DERTYPE="FIRST")  # OOC false: full Doo/Dvv
     Ho = O.Hamiltonian(h)
     co = O.CCWfn(Ho, r_convergence=1e-10)
     co.compute_energy()
-    tg = co.tgrad()
+    tg = co.tgrad(ooc=False)
     no, nv = h.no, h.nv
     pairs = {"s1": ("s1", (no, nv)), "s2": ("s2", (no, no, nv, nv)), "Doo": ("DooT", (no, no)),
              "Dvv": ("DvvT", (nv, nv)), "Dov": ("DovT", (no, nv)), "Goovv": ("GoovvT", (no, no, nv, nv)),

@@ -117,14 +117,16 @@ def test_not_converged_raises():
         cc.compute_energy()
 
 
-def test_triples_gradient_pieces_lambda_and_densities():
-    """WFN=CCSD_T, DERTYPE=FIRST: tgrad_ooc's s1, s2 and (T) density pieces
-    (ccwfn.cc:1150-1316), the Lambda equations with s1/s2 (cclambda.cc:181,243) and the
-    densities that start from the (T) pieces (ccdensity.cc:44-69)."""
+@pytest.mark.parametrize("tag,ooc", [("ccsd_t_first", True), ("ccsd_t_first_incore", False)])
+def test_triples_gradient_pieces_lambda_and_densities(tag, ooc):
+    """WFN=CCSD_T, DERTYPE=FIRST: the s1, s2 and (T) density pieces of tgrad_ooc
+    (ccwfn.cc:1150-1316, OOC=1) and of the in-core tgrad (:854-1142, OOC=0, full Doo/Dvv),
+    the Lambda equations with s1/s2 (cclambda.cc:181,243) and the densities that start
+    from the (T) pieces (ccdensity.cc:44-69)."""
     meta, arr = load("tgrad")
     h, perts, H, cc = _pipeline(meta)
-    tag, run = next(iter(meta["runs"].items()))
-    tg = cc.tgrad()
+    run = meta["runs"][tag]
+    tg = cc.tgrad(ooc=ooc)
     for k in ["s1", "s2", "Doo", "Dvv", "Dov", "Goovv", "Gooov", "Gvvvo"]:
         ref = arr[f"{tag}/{k}" if k in ("s1", "s2") else f"{tag}/{k}T"]
         np.testing.assert_allclose(tg[k], ref, atol=1e-16 + 1e-12 * np.abs(ref).max(), rtol=0, err_msg=k)

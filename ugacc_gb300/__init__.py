@@ -23,7 +23,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "ugacc_gb300.h")
 UCC_OK, UCC_NOT_CONVERGED = 0, 1
 STATUS = {0: "ok", 1: "not converged", 2: "nan detected", 3: "out of memory", 4: "bad arguments",
           5: "bad state", 6: "cuda error", 7: "device timeout", 8: "unsupported"}
-FP64, MIXED, MIXED_FINE = 0, 1, 2
+FP64, MIXED, MIXED_FINE, FP64_SLICED = 0, 1, 2, 3
 LEFT, RIGHT = 0, 1
 
 
@@ -40,7 +40,7 @@ class ConvergenceError(UccError):
 class _Options(ctypes.Structure):
     _fields_ = [("maxiter", ctypes.c_int), ("r_convergence", ctypes.c_double), ("diis", ctypes.c_int),
                 ("precision", ctypes.c_int), ("refine_sweeps", ctypes.c_int), ("print", ctypes.c_int),
-                ("mixed_switch", ctypes.c_double)]
+                ("mixed_switch", ctypes.c_double), ("ooc", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -54,7 +54,9 @@ class Stats(ctypes.Structure):
                 ("tc_gemm_launches", ctypes.c_int64), ("mixed_iterations", ctypes.c_int),
                 ("tc_gemm_ms", ctypes.c_double), ("tc_gemm_flops", ctypes.c_double),
                 ("anchored_iterations", ctypes.c_int), ("fp64_gemm_ms", ctypes.c_double),
-                ("fp64_gemm_flops", ctypes.c_double), ("fp64_gemm_launches", ctypes.c_int64)]
+                ("fp64_gemm_flops", ctypes.c_double), ("fp64_gemm_launches", ctypes.c_int64),
+                ("sliced_gemm_ms", ctypes.c_double), ("sliced_gemm_flops", ctypes.c_double),
+                ("sliced_gemm_launches", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -169,8 +171,8 @@ class Context:
         raise UccError(st, msg)
 
     def set_options(self, maxiter=100, r_convergence=1e-7, diis=True, precision=FP64, refine_sweeps=2, printing=0,
-                    mixed_switch=1e-5):
-        o = _Options(maxiter, r_convergence, int(diis), precision, refine_sweeps, printing, mixed_switch)
+                    mixed_switch=1e-5, ooc=False):
+        o = _Options(maxiter, r_convergence, int(diis), precision, refine_sweeps, printing, mixed_switch, int(bool(ooc)))
         self.check(self.lib.ucc_set_options(self.h, ctypes.byref(o)))
 
     def get(self, name: str, shape) -> np.ndarray:
@@ -218,7 +220,7 @@ class Context:
 # ------------------------------------------------------------------------------------
 DEFAULT_OPTIONS = {"WFN": "CCSD", "DERTYPE": "NONE", "MAXITER": 100, "R_CONVERGENCE": 1e-7, "DIIS": True,
                    "MYHAND": "RIGHT", "MY_OMEGA": 0.0, "PRECISION": "FP64", "REFINE_SWEEPS": 2, "PRINT": 0,
-                   "MIXED_SWITCH": 1e-5}
+                   "MIXED_SWITCH": 1e-5, "OOC": False}
 
 
 class Hamiltonian:
@@ -258,7 +260,7 @@ class CCWfn:
         self.ctx.set_options(maxiter=int(o["MAXITER"]), r_convergence=float(o["R_CONVERGENCE"]), diis=bool(o["DIIS"]),
                              precision=MIXED if str(o["PRECISION"]).upper() == "MIXED" else FP64,
                              refine_sweeps=int(o["REFINE_SWEEPS"]), printing=int(o["PRINT"]),
-                             mixed_switch=float(o["MIXED_SWITCH"]))
+                             mixed_switch=float(o["MIXED_SWITCH"]), ooc=bool(o["OOC"]))
         self.no, self.nv = H.no, H.nv
         self.eccsd = self.et = None
         self.iterations = 0
@@ -280,8 +282,8 @@ class CCWfn:
         return total
 
     def triples_gradient(self):
-        """ccwfn.cc:1150-1316 (tgrad_ooc): s1, s2 and the (T) density pieces, which the
-        following CCLambda and CCDensity include."""
+        """ccwfn.cc:854-1142 (tgrad, OOC false) or :1150-1316 (tgrad_ooc, OOC true): s1, s2 and
+        the (T) density pieces, which the following CCLambda and CCDensity include."""
         self.ctx.check(self.ctx.lib.ucc_triples_gradient(self.ctx.h))
 
     def triples(self) -> float:

@@ -6,6 +6,8 @@
 #include "pert.h"
 
 namespace ucc {
+bool sliced_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                     const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi, int S);
 void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                  const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi);
 void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
@@ -77,6 +79,7 @@ void ucc_options_default(ucc_options* o) {
   o->refine_sweeps = 2;
   o->print = 0;
   o->mixed_switch = 1e-5;
+  o->ooc = 0;
 }
 
 const char* ucc_status_string(ucc_status s) {
@@ -137,6 +140,7 @@ ucc_status ucc_set_options(ucc_ctx* ctx, const ucc_options* o) {
     UCC_REQUIRE(o->precision == UCC_FP64 || o->precision == UCC_MIXED, UCC_BAD_ARGS, "bad precision");
     UCC_REQUIRE(o->refine_sweeps >= 0, UCC_BAD_ARGS, "refine_sweeps must be >= 0");
     UCC_REQUIRE(o->mixed_switch > 0, UCC_BAD_ARGS, "mixed_switch must be > 0");
+    UCC_REQUIRE(o->ooc == 0 || o->ooc == 1, UCC_BAD_ARGS, "ooc must be 0 or 1");
     c.opt = *o;
   });
 }
@@ -303,8 +307,9 @@ ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t
                     double alpha, const double* A, const double* B, double beta, double* C) {
   return guard(ctx, [&](Ctx& c) {
     UCC_REQUIRE(A && B && C && M >= 1 && N >= 1 && K >= 1, UCC_BAD_ARGS, "ucc_gemm: bad arguments");
-    UCC_REQUIRE(precision == UCC_FP64 || precision == UCC_MIXED || precision == UCC_MIXED_FINE, UCC_BAD_ARGS,
-                "ucc_gemm: bad precision");
+    UCC_REQUIRE(precision == UCC_FP64 || precision == UCC_MIXED || precision == UCC_MIXED_FINE ||
+                    precision == UCC_FP64_SLICED,
+                UCC_BAD_ARGS, "ucc_gemm: bad precision");
     UCC_CUDA(cudaSetDevice(c.device));
     Scratch dA(c, sizeof(double) * M * K), dB(c, sizeof(double) * K * N), dC(c, sizeof(double) * M * N);
     UCC_CUDA(cudaMemcpyAsync(dA.p, A, sizeof(double) * M * K, cudaMemcpyHostToDevice, c.stream));
@@ -319,6 +324,10 @@ ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t
       tc_gemm_run(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi);
     else if (precision == UCC_MIXED_FINE)
       tc_gemm_run(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi, 3, 16);
+    else if (precision == UCC_FP64_SLICED)
+      UCC_REQUIRE(sliced_gemm_run(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi, 8),
+                  UCC_BAD_ARGS, "ucc_gemm: operands outside the sliced form's range (row maxima >= 2^498 or |alpha| "
+                                "outside [2^-20, 2^20])");
     else
       dgemm_strided(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi, 1, 0, 0, 0, nullptr);
     UCC_CUDA(cudaMemcpyAsync(C, dC.p, sizeof(double) * M * N, cudaMemcpyDeviceToHost, c.stream));

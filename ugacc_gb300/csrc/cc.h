@@ -87,6 +87,12 @@ void ccsd_alloc(Ctx& c);                                         // CCSD work ar
 void ccsd_residual(Ctx& c, const double* t_old, double* r);      // R(t_old), tau/ttau current
 double ccsd_energy(Ctx& c, const double* t);                     // E from t and the stored tau
 double run_triples(Ctx& c);
+// R2 += alpha sum_ef W_abef amp_ijef on packed pairs (cc_ground.cpp), W from block src by
+// mode (0: H_abef, 1: H_efab + H_feba, 2: H_abef + H_bafe)
+void packed_ladder(Ctx& c, double alpha, const Tensor& amp, const char* src, int mode, const char* vp_name,
+                   const char* vm_name, double* R2);
+// the packed form needs pairs on both sides and runs eagerly (it is not part of a recorded sweep)
+inline bool hbar_ladder_packed(Ctx& c) { return !recorder() && c.no > 1 && c.nv > 1; }
 void run_triples_gradient(Ctx& c);  // tgrad.cu
 void run_hbar(Ctx& c);
 CCSDResult run_lambda(Ctx& c);

@@ -18,6 +18,10 @@ using V4 = std::vector<int64_t>;
 void run_hbar(Ctx& c) {
   UCC_REQUIRE(c.have_ccsd, UCC_BAD_STATE, "HBAR needs converged CCSD amplitudes");
   Fp64Scope fp64(c);  // HBAR, Lambda, densities and response run in FP64
+  // the tensor-core operand caches key on block addresses, and the H blocks are rewritten
+  // in place
+  UCC_CUDA(cudaStreamSynchronize(c.stream));
+  c.tc_cache.reset();
   const int no = c.no, nv = c.nv;
   double* T = c.get("T").p;
   Tensor t1 = amp1(c, T), t2 = amp2(c, T), tau = c.get("tau");
@@ -44,6 +48,7 @@ void run_hbar(Ctx& c) {
   contract(c, "je,mnie->mnij", 2.0, t1, V(c, "ooov"), 1.0, Hoooo);
   contract(c, "ijef,mnef->mnij", 1.0, tau, V(c, "oovv"), 1.0, Hoooo);
 
+  for (const char* k : {"Hpp1", "Hmm1", "Hpp2", "Hmm2"}) c.drop(k);  // packed ladders of the previous HBAR
   Tensor Hvvvv = c.alloc("Hvvvv", {nv, nv, nv, nv}, false);  // :86-97
   copy_into(c, V(c, "vvvv"), Hvvvv);
   contract(c, "mb,amef->abef", -2.0, t1, V(c, "vovv"), 1.0, Hvvvv);
@@ -188,7 +193,10 @@ void lambda_l2(Ctx& c, const Tensor& l1, const Tensor& l2, const Tensor& Goo, co
   contract(c, "ijeb,ea->ijab", 1.0, l2, c.get("Hvv"), 1.0, Z);
   contract(c, "mjab,im->ijab", -1.0, l2, c.get("Hoo"), 1.0, Z);
   contract(c, "mnab,ijmn->ijab", 0.5, l2, c.get("Hoooo"), 1.0, Z);
-  contract(c, "ijef,efab->ijab", 0.5, l2, c.get("Hvvvv"), 1.0, Z);
+  // 0.5 sum_ef l2_ijef Hvvvv_efab: after the (ij,ab) + (ji,ba) symmetrisation below it is the packed
+  // ladder of W_abef = Hvvvv_efab + Hvvvv_feba on the symmetric l2
+  const bool packed = hbar_ladder_packed(c);
+  if (!packed) contract(c, "ijef,efab->ijab", 0.5, l2, c.get("Hvvvv"), 1.0, Z);
   contract(c, "ie,ejab->ijab", 1.0, l1, c.get("Hvovv_x"), 1.0, Z);
   contract(c, "mb,jima->ijab", -1.0, l1, c.get("Hooov_x"), 1.0, Z);
   contract(c, "ieam,mjeb->ijab", 1.0, c.get("Hovvo_x"), l2, 1.0, Z);
@@ -198,6 +206,7 @@ void lambda_l2(Ctx& c, const Tensor& l1, const Tensor& l2, const Tensor& Goo, co
   contract(c, "mi,mjab->ijab", -1.0, Goo, Loovv, 1.0, Z);
   copy_into(c, Z, R2);
   transpose_add(c, "jiba->ijab", 1.0, Z, 1.0, R2);
+  if (packed) packed_ladder(c, 0.5, l2, "Hvvvv", 1, "Hpp1", "Hmm1", R2.p);
 }
 }  // namespace
 

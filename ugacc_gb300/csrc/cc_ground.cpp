@@ -317,27 +317,41 @@ void build_t1(Ctx& c, const Tensor& t1, const Tensor& t2, Tensor R1) {
 // goes into a half residual Rh and R2 = <ij|ab> + Woooo.tau + ladder + Rh + Rh(ji,ba);
 // <ij|ab>, the hole ladder and the particle ladder are symmetric on their own.
 //
+}  // namespace
+
+// R2 += alpha sum_ef W_abef amp_ijef on packed pairs (kernels_fp64.cu): S = Tp Vp^T over
+// (i<=j, a<=b, e<=f), A = Tm Vm^T over strict pairs, a quarter of the multiply-adds of the
+// plain contraction; amp must be invariant under (i,j,e,f) -> (j,i,f,e).  The packed
+// operator (names vp_name / vm_name, constant blocks) is built from block `src` once.
+void packed_ladder(Ctx& c, double alpha, const Tensor& amp, const char* src, int mode, const char* vp_name,
+                   const char* vm_name, double* R2) {
+  const int no = c.no, nv = c.nv;
+  const int64_t op = (int64_t)no * (no + 1) / 2, om = (int64_t)no * (no - 1) / 2;
+  const int64_t vp = (int64_t)nv * (nv + 1) / 2, vm = (int64_t)nv * (nv - 1) / 2;
+  if (!c.has(vp_name)) {
+    Tensor Vp = c.alloc(vp_name, {vp, vp}, false), Vm = c.alloc(vm_name, {vm, vm}, false);
+    pack_vvvv(c, nv, mode, c.get(src).p, Vp.p, Vm.p);
+  }
+  UCC_REQUIRE(amp.dense(), UCC_BAD_ARGS, "packed ladder: dense amplitudes");
+  Temp Tp(c, {op, vp}), Tm(c, {om, vm}), S(c, {op, vp}), A(c, {om, vm});
+  pack_tau(c, no, nv, amp.p, Tp->p, Tm->p);
+  contract(c, "pe,qe->pq", 1.0, Tp, c.get(vp_name), 0.0, S);
+  contract(c, "pe,qe->pq", 1.0, Tm, c.get(vm_name), 0.0, A);
+  unpack_ladder(c, no, nv, alpha, S->p, A->p, R2);
+}
+
+namespace {
+
 // particle ladder sum_ef <ab|ef> tau_ijef, ccwfn.cc:508-510.  Outside a recorded batch it
 // runs on packed pairs: S = Tp Vp^T over (i<=j, a<=b, e<=f) and A = Tm Vm^T over strict
 // pairs, a quarter of the multiply-adds (the result is symmetric under the simultaneous
 // swap (i,j,a,b) -> (j,i,b,a) and the integrals under (a,b,e,f) -> (b,a,f,e))
 void ladder(Ctx& c, const Tensor& tau, const Tensor& R2) {
-  const int no = c.no, nv = c.nv;
-  if (recorder() || no < 2 || nv < 2) {
+  if (recorder() || c.no < 2 || c.nv < 2) {
     contract(c, "ijef,abef->ijab", 1.0, tau, V(c, "vvvv"), 1.0, R2);
     return;
   }
-  const int64_t op = (int64_t)no * (no + 1) / 2, om = (int64_t)no * (no - 1) / 2;
-  const int64_t vp = (int64_t)nv * (nv + 1) / 2, vm = (int64_t)nv * (nv - 1) / 2;
-  if (!c.has("Vpp")) {  // packed integrals, built once per Hamiltonian (constant blocks)
-    Tensor Vp = c.alloc("Vpp", {vp, vp}, false), Vm = c.alloc("Vmm", {vm, vm}, false);
-    pack_vvvv(c, nv, V(c, "vvvv").p, Vp.p, Vm.p);
-  }
-  Temp Tp(c, {op, vp}), Tm(c, {om, vm}), S(c, {op, vp}), A(c, {om, vm});
-  pack_tau(c, no, nv, tau.p, Tp->p, Tm->p);
-  contract(c, "pe,qe->pq", 1.0, Tp, c.get("Vpp"), 0.0, S);
-  contract(c, "pe,qe->pq", 1.0, Tm, c.get("Vmm"), 0.0, A);
-  unpack_ladder(c, no, nv, S->p, A->p, R2.p);
+  packed_ladder(c, 1.0, tau, "Vvvvv", 0, "Vpp", "Vmm", R2.p);
 }
 
 void build_t2(Ctx& c, const Tensor& t1, const Tensor& t2, const Tensor& tau, Tensor R2, std::vector<cudaEvent_t>* ev) {

@@ -93,12 +93,15 @@ void build_X(Ctx& c, Perturbation& p, const Tensor& X1o, const Tensor& X2o, Tens
   contract(c, "ijeb,ae->ijab", 1.0, X2o, c.get("Hvv"), 1.0, Q);
   contract(c, "mjab,mi->ijab", -1.0, X2o, c.get("Hoo"), 1.0, Q);
   contract(c, "mnab,mnij->ijab", 0.5, X2o, c.get("Hoooo"), 1.0, Q);
-  contract(c, "ijef,abef->ijab", 0.5, X2o, c.get("Hvvvv"), 1.0, Q);
+  // 0.5 sum_ef X2_ijef Hvvvv_abef, moved past the symmetrisation: W_abef = Hvvvv_abef + Hvvvv_bafe
+  const bool packed = hbar_ladder_packed(c);
+  if (!packed) contract(c, "ijef,abef->ijab", 0.5, X2o, c.get("Hvvvv"), 1.0, Q);
   contract(c, "imeb,maje->ijab", -1.0, X2o, c.get("Hovov"), 1.0, Q);
   contract(c, "imea,mbej->ijab", -1.0, X2o, c.get("Hovvo"), 1.0, Q);
   contract(c, "miea,mbej->ijab", 1.0, X2o, c.get("Hovvo_x"), 1.0, Q);  // 2 Hovvo[m,b,e,j] - Hovov[m,b,j,e]
   copy_into(c, Q, R2);
   transpose_add(c, "jiba->ijab", 1.0, Q, 1.0, R2);
+  if (packed) packed_ladder(c, 0.5, X2o, "Hvvvv", 2, "Hpp2", "Hmm2", R2.p);
 }
 
 // build_G / build_Y1 / build_Y2, ccpert.cc:500-881
@@ -244,7 +247,9 @@ void build_Y(Ctx& c, Perturbation& p, const Tensor& Y1o, const Tensor& Y2o, Tens
   contract(c, "ijeb,ea->ijab", 1.0, Y2o, Hvv, 1.0, Q);
   contract(c, "mjab,im->ijab", -1.0, Y2o, Hoo, 1.0, Q);
   contract(c, "mnab,ijmn->ijab", 0.5, Y2o, Hoooo, 1.0, Q);
-  contract(c, "ijef,efab->ijab", 0.5, Y2o, Hvvvv, 1.0, Q);
+  // 0.5 sum_ef Y2_ijef Hvvvv_efab, moved past the symmetrisation: W_abef = Hvvvv_efab + Hvvvv_feba
+  const bool packed = hbar_ladder_packed(c);
+  if (!packed) contract(c, "ijef,efab->ijab", 0.5, Y2o, Hvvvv, 1.0, Q);
   contract(c, "ie,ejab->ijab", 1.0, Y1o, Hvovv_x, 1.0, Q);
   contract(c, "mb,jima->ijab", -1.0, Y1o, Hooov_x, 1.0, Q);
   contract(c, "mjeb,ieam->ijab", 1.0, Y2o, Hovvo_x, 1.0, Q);
@@ -351,6 +356,7 @@ void build_Y(Ctx& c, Perturbation& p, const Tensor& Y1o, const Tensor& Y2o, Tens
   }
   copy_into(c, Q, R2);
   transpose_add(c, "jiba->ijab", 1.0, Q, 1.0, R2);
+  if (packed) packed_ladder(c, 0.5, Y2o, "Hvvvv", 1, "Hpp1", "Hmm1", R2.p);
 }
 
 double pseudoresponse(Ctx& c, Perturbation& p, double* amps) {  // ccpert.cc:233-253

@@ -289,14 +289,16 @@ void triples_energy(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, con
 void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, const double* t1,
                         const double* Voovv, const double* eps, double* d_partial);
 
-// Pair-symmetric particle ladder (sum_ef <ab|ef> tau_ijef = S + sign A over packed pairs):
-// Vp[a<=b][e<=f] = <ab|ef> + <ab|fe> (<ab|ee> on e == f), Vm[a<b][e<f] = <ab|ef> - <ab|fe>;
+// Pair-symmetric particle ladder (sum_ef W_abef tau_ijef = S + sign A over packed pairs,
+// W and tau invariant under the simultaneous pair swap):
+// Vp[a<=b][e<=f] = W_abef + W_abfe (W_abee on e == f), Vm[a<b][e<f] = W_abef - W_abfe, with
+// W from a stored block by `mode` (0: H_abef; 1: H_efab + H_feba; 2: H_abef + H_bafe);
 // Tp[i<=j][e<=f] = (tau_ijef + tau_ijfe)/2 (tau_ijee on e == f), Tm[i<j][e<f] = (tau_ijef - tau_ijfe)/2;
-// R2[ijab] += S[ij][ab] + sign A[ij][ab] over the sorted pairs.  Pairs p <= q are
+// R2[ijab] += alpha (S[ij][ab] + sign A[ij][ab]) over the sorted pairs.  Pairs p <= q are
 // numbered q(q+1)/2 + p, strict pairs q(q-1)/2 + p.
-void pack_vvvv(Ctx& c, int nv, const double* V, double* Vp, double* Vm);
+void pack_vvvv(Ctx& c, int nv, int mode, const double* H, double* Vp, double* Vm);
 void pack_tau(Ctx& c, int no, int nv, const double* tau, double* Tp, double* Tm);
-void unpack_ladder(Ctx& c, int no, int nv, const double* S, const double* A, double* R2);
+void unpack_ladder(Ctx& c, int no, int nv, double alpha, const double* S, const double* A, double* R2);
 
 int64_t launches();  // kernels launched by this library so far (all contexts)
 

@@ -706,24 +706,33 @@ __device__ __forceinline__ void pair_lt(int64_t Q, int& p, int& q) {
   p = (int)(Q - (int64_t)j * (j - 1) / 2);
 }
 
-// Vp[ab][ef] = <ab|ef> + <ab|fe> (e < f), <ab|ee> (e == f), a <= b;  Vm[ab][ef] = <ab|ef> - <ab|fe>, a < b, e < f
-__global__ void pack_vvvv_kernel(int nv, const double* __restrict__ V, double* Vp, double* Vm) {
+// the operator W_abef of a packed ladder, from a stored [nv]^4 block H:
+//   mode 0: H[a][b][e][f]                          (<ab|ef>, pair-symmetric itself)
+//   mode 1: H[e][f][a][b] + H[f][e][b][a]          (sum_ef Z_ijef H_efab of a Z + Z(ji,ba) residual)
+//   mode 2: H[a][b][e][f] + H[b][a][f][e]          (sum_ef Z_ijef H_abef of a Z + Z(ji,ba) residual)
+__device__ __forceinline__ double ladder_op(const double* H, int nv, int mode, int a, int b, int e, int f) {
+  auto at = [&](int p, int q, int r, int s) { return H[(((int64_t)p * nv + q) * nv + r) * nv + s]; };
+  if (mode == 1) return at(e, f, a, b) + at(f, e, b, a);
+  if (mode == 2) return at(a, b, e, f) + at(b, a, f, e);
+  return at(a, b, e, f);
+}
+
+// Vp[ab][ef] = W_abef + W_abfe (e < f), W_abee (e == f), a <= b;  Vm[ab][ef] = W_abef - W_abfe, a < b, e < f
+__global__ void pack_vvvv_kernel(int nv, int mode, const double* __restrict__ H, double* Vp, double* Vm) {
   const int64_t np = (int64_t)nv * (nv + 1) / 2, nm = (int64_t)nv * (nv - 1) / 2;
-  const int64_t nv2 = (int64_t)nv * nv;
   for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < np * np + nm * nm;
        x += (int64_t)gridDim.x * blockDim.x) {
     int a, b, e, f;
     if (x < np * np) {
       pair_le(x / np, a, b);
       pair_le(x % np, e, f);
-      const double* v = V + ((int64_t)a * nv + b) * nv2;
-      Vp[x] = e == f ? v[(int64_t)e * nv + e] : v[(int64_t)e * nv + f] + v[(int64_t)f * nv + e];
+      Vp[x] = e == f ? ladder_op(H, nv, mode, a, b, e, e)
+                     : ladder_op(H, nv, mode, a, b, e, f) + ladder_op(H, nv, mode, a, b, f, e);
     } else {
       const int64_t y = x - np * np;
       pair_lt(y / nm, a, b);
       pair_lt(y % nm, e, f);
-      const double* v = V + ((int64_t)a * nv + b) * nv2;
-      Vm[y] = v[(int64_t)e * nv + f] - v[(int64_t)f * nv + e];
+      Vm[y] = ladder_op(H, nv, mode, a, b, e, f) - ladder_op(H, nv, mode, a, b, f, e);
     }
   }
 }
@@ -753,8 +762,8 @@ __global__ void pack_tau_kernel(int no, int nv, const double* __restrict__ tau, 
 
 // R2[ijab] += S[(i,j) sorted][(a,b) sorted] + sign * A[...], sign = (-1)^[i>j] (-1)^[a>b],
 // A = 0 on i == j or a == b
-__global__ void unpack_ladder_kernel(int no, int nv, const double* __restrict__ S, const double* __restrict__ A,
-                                     double* R2) {
+__global__ void unpack_ladder_kernel(int no, int nv, double alpha, const double* __restrict__ S,
+                                     const double* __restrict__ A, double* R2) {
   const int64_t n = (int64_t)no * no * nv * nv;
   const int64_t vp = (int64_t)nv * (nv + 1) / 2, vm = (int64_t)nv * (nv - 1) / 2;
   for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
@@ -769,15 +778,15 @@ __global__ void unpack_ladder_kernel(int no, int nv, const double* __restrict__ 
       const double am = A[((int64_t)j0 * (j0 - 1) / 2 + i0) * vm + (int64_t)b0 * (b0 - 1) / 2 + a0];
       v += ((i > j) != (a > b)) ? -am : am;
     }
-    R2[x] += v;
+    R2[x] += alpha * v;
   }
 }
 }  // namespace
 
-void pack_vvvv(Ctx& c, int nv, const double* V, double* Vp, double* Vm) {
+void pack_vvvv(Ctx& c, int nv, int mode, const double* H, double* Vp, double* Vm) {
   UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
   const int64_t np = (int64_t)nv * (nv + 1) / 2, nm = (int64_t)nv * (nv - 1) / 2;
-  pack_vvvv_kernel<<<grid_for(np * np + nm * nm), 256, 0, c.stream>>>(nv, V, Vp, Vm);
+  pack_vvvv_kernel<<<grid_for(np * np + nm * nm), 256, 0, c.stream>>>(nv, mode, H, Vp, Vm);
   count_launch();
   check_launch("pack_vvvv");
 }
@@ -790,10 +799,10 @@ void pack_tau(Ctx& c, int no, int nv, const double* tau, double* Tp, double* Tm)
   check_launch("pack_tau");
 }
 
-void unpack_ladder(Ctx& c, int no, int nv, const double* S, const double* A, double* R2) {
+void unpack_ladder(Ctx& c, int no, int nv, double alpha, const double* S, const double* A, double* R2) {
   UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
   const int64_t n = (int64_t)no * no * nv * nv;
-  unpack_ladder_kernel<<<grid_for(n), 256, 0, c.stream>>>(no, nv, S, A, R2);
+  unpack_ladder_kernel<<<grid_for(n), 256, 0, c.stream>>>(no, nv, alpha, S, A, R2);
   count_launch();
   check_launch("unpack_ladder");
 }

@@ -150,6 +150,11 @@ __device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
       "l"(a), "l"(b), "r"(IDESC), "r"(acc));
 }
+__device__ __forceinline__ void mma_i(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
@@ -376,6 +381,334 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
+// ------------------------------------------------------------------------------------
+// FP64 GEMM from exact BF16 slices (the error-free splitting of Ozaki, Ogita, Oishi and
+// Rump, Numer. Algorithms 59 (2012) 95-118, with base-2^7 digits).
+//
+// Every operand row r is scaled by 2^-e_r (e_r = ilogb(max_k |x_rk|) + 2, so the scaled
+// row lies in (-1/2, 1/2)) and written as S balanced base-128 digits,
+//   x_rk = 2^e_r sum_{s<S} d_s(r,k) 2^-7(s+1),  |d_s| <= 64,
+// stored pre-scaled as bf16 slices d_s 2^-7(s+1) (exact: integers of 7 bits times a power
+// of two).  A product of an A slice s and a B slice t is an integer times 2^-7(s+t+2),
+// below 2^12 in magnitude, so any sum of up to 4096 such products with the same s+t is
+// exact in the FP32 tensor-memory accumulator.  The kernel therefore accumulates, per
+// output tile, "units": for each order g = s+t < gex, every pair (s, g-s) over a K range
+// of at most 4096 / (g+1) elements (exact), and one tail unit with all pairs of order
+// gex..S-1 over the whole K range (FP32, its terms are ~2^-7gex smaller than the leading
+// ones).  The epilogue adds each unit into the FP64 output as
+//   C[m][n] += alpha 2^(e_m + e_n) acc,
+// the first unit of a tile applying beta.  Pairs with s+t >= S are dropped (truncation
+// ~2^-7S relative to max|A_m.| max|B_.n|).
+// ------------------------------------------------------------------------------------
+struct SParams {
+  int M, N, kblocks, mtiles, ntiles;
+  int bn;              // N tile (a multiple of 32 up to 256): the MMA's N and the B box rows
+  int S, gex;          // slices per operand; orders below gex are accumulated exactly
+  int a_rows, b_rows;  // rows per slice in the slice arrays (slice s of row r at s * rows + r)
+  double alpha, beta;
+  double* C;
+  GemmEpilogue epi;
+  const int* ea;  // row exponents of A and B
+  const int* eb;
+  int* err;
+  int ksplit, kchunk;  // split-K into FP64 partials at C + z*M*N (alpha 1, beta 0)
+};
+
+struct SUnit {
+  int g0, g1, kb0, kb1;  // orders [g0, g1], K blocks [kb0, kb1)
+};
+
+// K blocks per exact unit of order g: (g+1) pairs x kc blocks x 64 <= 4096 products
+__device__ __forceinline__ int sunit_kc(int g) { return max(1, 64 / (g + 1)); }
+
+__device__ __forceinline__ int sunit_count(int S, int gex, int kn) {
+  int u = gex < S ? 1 : 0;
+  for (int g = 0; g < gex; g++) {
+    const int kc = sunit_kc(g);
+    u += (kn + kc - 1) / kc;
+  }
+  return u;
+}
+
+__device__ __forceinline__ SUnit sunit_at(int S, int gex, int k0, int kn, int u) {
+  for (int g = 0; g < gex; g++) {
+    const int kc = sunit_kc(g), nu = (kn + kc - 1) / kc;
+    if (u < nu) return SUnit{g, g, k0 + u * kc, k0 + min((u + 1) * kc, kn)};
+    u -= nu;
+  }
+  return SUnit{gex, S - 1, k0, k0 + kn};
+}
+
+__device__ __forceinline__ int sunit_items(const SUnit& U) {
+  int pairs = 0;
+  for (int g = U.g0; g <= U.g1; g++) pairs += g + 1;
+  return pairs * (U.kb1 - U.kb0);
+}
+
+__device__ __forceinline__ double pow2i(int e) {  // 2^e for -1022 <= e <= 1023
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    sliced_gemm_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, SParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + STAGES * A_BYTES;
+  uint64_t* full = (uint64_t*)(sB + STAGES * B_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* tfull = empty + STAGES;
+  uint64_t* tempty = tfull + 2;
+  uint32_t* tslot = (uint32_t*)(tempty + 2);
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int a = 0; a < 2; a++) {
+      mbar_init(&tfull[a], 1);
+      mbar_init(&tempty[a], 128);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tslot;
+  const int tiles_per = p.mtiles * p.ntiles;
+  const int ntile = tiles_per * (p.ksplit > 1 ? p.ksplit : 1);
+  // K range of a tile: the whole K, or chunk z of a split-K launch
+  auto krange = [&](int tile, int& k0, int& kn) {
+    k0 = 0;
+    kn = p.kblocks;
+    if (p.ksplit > 1) {
+      k0 = (tile / tiles_per) * p.kchunk;
+      kn = min(p.kblocks - k0, p.kchunk);
+    }
+  };
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int64_t issued = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+        const int tl = tile % tiles_per;
+        const int m0 = (tl % p.mtiles) * BM, n0 = (tl / p.mtiles) * p.bn;
+        int k0, kn;
+        krange(tile, k0, kn);
+        const int nu = sunit_count(p.S, p.gex, kn);
+        for (int u = 0; u < nu && ok; u++) {
+          const SUnit U = sunit_at(p.S, p.gex, k0, kn, u);
+          for (int g = U.g0; g <= U.g1 && ok; g++)
+            for (int s = 0; s <= g && ok; s++)
+              for (int kb = U.kb0; kb < U.kb1; kb++) {
+                if (!mbar_wait(&empty[stage], phase ^ 1u, p.err)) {
+                  ok = false;
+                  break;
+                }
+                mbar_expect_tx(&full[stage], (uint32_t)(A_BYTES + p.bn * BK * 2));
+                tma_load(sA + stage * A_BYTES, &mA, &full[stage], kb * BK, s * p.a_rows + m0);
+                tma_load(sB + stage * B_BYTES, &mB, &full[stage], kb * BK, (g - s) * p.b_rows + n0);
+                ++issued;
+                if (++stage == STAGES) {
+                  stage = 0;
+                  phase ^= 1u;
+                }
+              }
+        }
+      }
+      for (int64_t n = issued > STAGES ? issued - STAGES : 0; n < issued; n++)
+        mbar_wait_deadline(&full[n % STAGES], (uint32_t)((n / STAGES) & 1));
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int stage = 0, acc = 0;
+      uint32_t phase = 0, aphase = 0;
+      bool ok = true;
+      const uint32_t idesc =
+          (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(p.bn >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+      for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+        int k0, kn;
+        krange(tile, k0, kn);
+        const int nu = sunit_count(p.S, p.gex, kn);
+        for (int u = 0; u < nu && ok; u++) {
+          const int items = sunit_items(sunit_at(p.S, p.gex, k0, kn, u));
+          if (!mbar_wait(&tempty[acc], aphase ^ 1u, p.err)) {
+            ok = false;
+            break;
+          }
+          fence_after();
+          const uint32_t d = tmem + (uint32_t)(acc * BN);
+          for (int kb = 0; kb < items; kb++) {
+            if (!mbar_wait(&full[stage], phase, p.err)) {
+              ok = false;
+              break;
+            }
+            fence_after();
+            const uint64_t ad = sdesc(sA + stage * A_BYTES), bd = sdesc(sB + stage * B_BYTES);
+#pragma unroll
+            for (int k = 0; k < BK / 16; k++)
+              mma_i(d, ad + (uint64_t)(k * 2), bd + (uint64_t)(k * 2), idesc, (kb | k) != 0);
+            mma_commit(&empty[stage]);
+            if (++stage == STAGES) {
+              stage = 0;
+              phase ^= 1u;
+            }
+          }
+          mma_commit(&tfull[acc]);
+          if (++acc == 2) {
+            acc = 0;
+            aphase ^= 1u;
+          }
+        }
+      }
+    }
+  } else {
+    const int q = warp & 3;
+    int acc = 0;
+    uint32_t aphase = 0;
+    const GemmEpilogue ep = p.epi;
+    bool ok = true;
+    const int nch = p.bn / 32;
+    for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+      const int tl = tile % tiles_per;
+      const int mt = tl % p.mtiles, nt = tl / p.mtiles;
+      const int64_t coff = p.ksplit > 1 ? (int64_t)(tile / tiles_per) * p.M * p.N : 0;
+      int k0, kn;
+      krange(tile, k0, kn);
+      const int nu = sunit_count(p.S, p.gex, kn);
+      const int64_t m = (int64_t)mt * BM + q * 32 + lane;
+      const int64_t mo = ep.msplit ? (m / ep.msplit) * ep.s_mhi + (m % ep.msplit) * ep.s_mlo : m * ep.s_mhi;
+      // alpha 2^e_m; the column factor 2^e_n is added to its exponent field (|e| <= 500 and
+      // 2^-20 <= |alpha| <= 2^20 keep the result normal)
+      const long long sa = m < p.M ? __double_as_longlong(p.alpha * pow2i(p.ea[m])) : 0;
+      for (int u = 0; u < nu; u++) {
+        if (!mbar_wait(&tfull[acc], aphase, p.err)) {
+          ok = false;
+          break;
+        }
+        fence_after();
+        const bool first = u == 0;
+        for (int ch = 0; ch < nch; ch++) {
+          uint32_t r[32];
+          tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + ch * 32), r);
+          if (m < p.M) {
+            const int64_t n0 = (int64_t)nt * p.bn + ch * 32;
+            double* Cb = p.C + coff + mo;
+            double old[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+              old[j] = 0.0;
+              if (n0 + j < p.N && !(first && p.beta == 0.0)) {
+                old[j] = Cb[(n0 + j) * ep.s_n];
+                if (first) old[j] *= p.beta;
+              }
+            }
+#pragma unroll
+            for (int j = 0; j < 32; j++)
+              if (n0 + j < p.N) {
+                const double f = __longlong_as_double(sa + ((long long)p.eb[n0 + j] << 52));
+                Cb[(n0 + j) * ep.s_n] = fma((double)__uint_as_float(r[j]), f, old[j]);
+              }
+          }
+        }
+        fence_before();
+        mbar_arrive(&tempty[acc]);
+        if (++acc == 2) {
+          acc = 0;
+          aphase ^= 1u;
+        }
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+// row maxima |x| of a rows x cols FP64 view as bit patterns (positive doubles order like
+// their bits); 32 x 32 tiles, reads coalesced along whichever stride is 1
+__global__ void slice_absmax_kernel(int64_t rows, int64_t cols, const double* __restrict__ x, int64_t sr, int64_t sk,
+                                    unsigned long long* amax) {
+  __shared__ double t[32][33];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int i = ty; i < 32; i += 8) {
+    // sk == 1: lanes run along k; otherwise along r (transposed views)
+    const int64_t r = sk == 1 ? r0 + i : r0 + tx, k = sk == 1 ? k0 + tx : k0 + i;
+    const double v = (r < rows && k < cols) ? fabs(x[r * sr + k * sk]) : 0.0;
+    if (sk == 1)
+      t[i][tx] = v;
+    else
+      t[tx][i] = v;
+  }
+  __syncthreads();
+  // row i of the tile: warp ty reduces rows ty, ty+8, ...
+  for (int i = ty; i < 32; i += 8) {
+    double v = t[i][tx];
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (tx == 0 && r0 + i < rows && v > 0.0) atomicMax(amax + r0 + i, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
+// row exponent from the row maximum: e = ilogb(max) + 2 (max/2^e in [1/4, 1/2)), clamped
+// below at -500; a row maximum >= 2^498 sets *range (the caller falls back to FP64)
+__device__ __forceinline__ int slice_exponent(unsigned long long bits, int* range) {
+  const int be = (int)((bits >> 52) & 0x7FF);
+  if (be == 0) return -500;  // zero or subnormal row maximum
+  const int e = be - 1023 + 2;
+  if (e > 500) {
+    atomicExch(range, 1);
+    return 500;
+  }
+  return max(e, -500);
+}
+
+// digits: slices[s][r][k] = bf16(d_s 2^-7(s+1)) for r < rows_p (zero past rows), k < kp
+// (zero past cols); e[r] written by the blocks of the first K tile
+__global__ void slice_digits_kernel(int64_t rows, int64_t cols, int64_t rows_p, int64_t kp, const double* __restrict__ x,
+                                    int64_t sr, int64_t sk, const unsigned long long* __restrict__ amax, int S,
+                                    __nv_bfloat16* slices, int* e_out, int* range) {
+  __shared__ double t[32][33];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int i = ty; i < 32; i += 8) {
+    const int64_t r = sk == 1 ? r0 + i : r0 + tx, k = sk == 1 ? k0 + tx : k0 + i;
+    const double v = (r < rows && k < cols) ? x[r * sr + k * sk] : 0.0;
+    if (sk == 1)
+      t[i][tx] = v;
+    else
+      t[tx][i] = v;
+  }
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int64_t r = r0 + i, k = k0 + tx;
+    if (r >= rows_p || k >= kp) continue;
+    const int e = r < rows ? slice_exponent(amax[r], range) : 0;
+    if (k == 0 && r < rows) e_out[r] = e;
+    double v = r < rows ? t[i][tx] * pow2i(-e) : 0.0;  // in (-1/2, 1/2)
+    const size_t plane = (size_t)rows_p * kp;
+    for (int s = 0; s < S; s++) {
+      v *= 128.0;
+      const double d = rint(v);
+      v -= d;
+      slices[(size_t)s * plane + (size_t)r * kp + k] = __double2bfloat16(d * pow2i(-7 * (s + 1)));
+    }
+  }
+}
+
 // FP64 rows x cols view (strides sr, sk) -> bf16 hi/lo [rows][kp], zero padded to kp
 // (mid != null: three parts, x = hi + mid + lo, each the bf16 rounding of what remains)
 __global__ void split_kernel(int64_t rows, int64_t cols, int64_t kp, const double* x, int64_t sr, int64_t sk,
@@ -412,10 +745,30 @@ struct Split {
   }
 };
 
+// an operand as S exact bf16 slices [S][rows_p][kp] with row exponents (sliced FP64 GEMM)
+struct Sliced {
+  __nv_bfloat16* d = nullptr;
+  int* e = nullptr;
+  std::unique_ptr<Scratch> tmp;  // storage of a temporary (non-constant) operand
+  int64_t rows = 0, rows_p = 0, kp = 0;
+  int S = 0;
+  bool range_ok = true;
+  CUtensorMap map;
+  ~Sliced() {
+    if (!tmp) {
+      if (d) cudaFree(d);
+      if (e) cudaFree(e);
+    }
+  }
+};
+
 using Key = std::tuple<const double*, int64_t, int64_t, int64_t, int64_t, int, int>;
 struct Triples;
 struct Cache {
   std::map<Key, std::unique_ptr<Split>> ops;
+  std::map<Key, std::unique_ptr<Sliced>> sliced;
+  int* range = nullptr;
+  bool sattr_set = false;
   std::shared_ptr<Triples> triples;
   int* err = nullptr;
   int sms = 0;
@@ -423,6 +776,7 @@ struct Cache {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   ~Cache() {
     if (err) cudaFree(err);
+    if (range) cudaFree(range);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
   }
@@ -457,6 +811,8 @@ static Cache& cache(Ctx& c) {
     c.tc_cache = std::shared_ptr<void>(k, [](void* p) { delete static_cast<Cache*>(p); });
     UCC_CUDA(cudaMalloc(&k->err, sizeof(int)));
     UCC_CUDA(cudaMemset(k->err, 0, sizeof(int)));
+    UCC_CUDA(cudaMalloc(&k->range, sizeof(int)));
+    UCC_CUDA(cudaMemset(k->range, 0, sizeof(int)));
     UCC_CUDA(cudaDeviceGetAttribute(&k->sms, cudaDevAttrMultiProcessorCount, c.device));
     UCC_CUDA(cudaEventCreate(&k->ev0));
     UCC_CUDA(cudaEventCreate(&k->ev1));
@@ -496,7 +852,159 @@ static Split* prepare(Ctx& c, const double* x, int64_t rows, int64_t cols, int64
   return raw;
 }
 
+// slice (and cache when the source is a constant block and memory allows) a rows x cols
+// FP64 operand; the slice arrays are padded to whole tiles of box_rows rows so that no tile
+// reaches into the next slice.  nullptr when the slices do not fit in free memory.
+static Sliced* slice_prepare(Ctx& c, const double* x, int64_t rows, int64_t cols, int64_t sr, int64_t sk, int box_rows,
+                             int S, std::unique_ptr<Sliced>& temp) {
+  Cache& k = cache(c);
+  bool constant = c.is_constant(x);
+  Key key{x, rows, cols, sr, sk, box_rows, S};
+  if (constant) {
+    auto it = k.sliced.find(key);
+    if (it != k.sliced.end()) return it->second.get();
+  }
+  auto s = std::make_unique<Sliced>();
+  s->rows = rows;
+  s->rows_p = (rows + box_rows - 1) / box_rows * box_rows;
+  s->kp = (cols + BK - 1) / BK * BK;
+  s->S = S;
+  const size_t nel = (size_t)S * s->rows_p * s->kp;
+  size_t free_b = 0, total_b = 0;
+  UCC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const double need = 2.0 * nel + 4.0 * rows;
+  // a cached copy keeps a tenth of the memory free for the solver; a temporary 2 GB
+  if (constant && need > (double)free_b - 0.1 * (double)total_b) constant = false;
+  if (!constant && need > (double)free_b - 2e9) return nullptr;
+  if (constant) {
+    UCC_CUDA(cudaMalloc(&s->d, sizeof(__nv_bfloat16) * nel));
+    UCC_CUDA(cudaMalloc(&s->e, sizeof(int) * rows));
+  } else {
+    s->tmp = std::make_unique<Scratch>(c, sizeof(__nv_bfloat16) * nel + sizeof(int) * rows + 16);
+    s->d = static_cast<__nv_bfloat16*>(s->tmp->p);
+    s->e = reinterpret_cast<int*>(static_cast<char*>(s->tmp->p) + ((sizeof(__nv_bfloat16) * nel + 15) / 16) * 16);
+  }
+  Scratch amax(c, sizeof(unsigned long long) * rows);
+  UCC_CUDA(cudaMemsetAsync(amax.p, 0, sizeof(unsigned long long) * rows, c.stream));
+  UCC_CUDA(cudaMemsetAsync(k.range, 0, sizeof(int), c.stream));
+  const dim3 blk(32, 8);
+  slice_absmax_kernel<<<dim3((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32)), blk, 0, c.stream>>>(
+      rows, cols, x, sr, sk, static_cast<unsigned long long*>(amax.p));
+  count_kernel_launch();
+  slice_digits_kernel<<<dim3((unsigned)(s->kp / 32), (unsigned)(s->rows_p / 32)), blk, 0, c.stream>>>(
+      rows, cols, s->rows_p, s->kp, x, sr, sk, static_cast<const unsigned long long*>(amax.p), S, s->d, s->e,
+      k.range);
+  count_kernel_launch();
+  UCC_CUDA(cudaGetLastError());
+  int hrange = 0;
+  UCC_CUDA(cudaMemcpyAsync(&hrange, k.range, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  UCC_CUDA(cudaStreamSynchronize(c.stream));
+  s->range_ok = hrange == 0;
+  make_map(&s->map, s->d, (int64_t)S * s->rows_p, s->kp, box_rows);
+  Sliced* raw = s.get();
+  if (constant)
+    k.sliced[key] = std::move(s);
+  else
+    temp = std::move(s);
+  return raw;
+}
+
 }  // namespace tc
+
+// slices per operand of the sliced FP64 GEMM (56 bits) and the smallest GEMM it takes
+constexpr int kSlices = 8;
+constexpr double kSlicedMinWork = 2e8;
+
+bool sliced_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                     const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi,
+                     int S) {
+  using namespace tc;
+  UCC_REQUIRE(S >= 2 && S <= 8, UCC_BAD_ARGS, "sliced GEMM: 2 to 8 slices");
+  const double aa = std::fabs(alpha);
+  if (!(aa >= 0x1p-20 && aa <= 0x1p20) || M > INT32_MAX || N > INT32_MAX) return false;
+  // N tile: a short N is padded to a multiple of 32 only
+  const int bn = N >= BN ? BN : (int)((N + 31) / 32 * 32);
+  if ((double)S * (double)((M + BM - 1) / BM * BM) >= 2e9 || (double)S * (double)((N + bn - 1) / bn * bn) >= 2e9)
+    return false;
+  if ((N + bn - 1) / bn * bn / 32 > 65535 || (M + BM - 1) / BM * BM / 32 > 65535) return false;  // slicing grid.y
+  Cache& k = cache(c);
+  UCC_CUDA(cudaEventRecord(k.ev0, c.stream));  // the time includes the slicing of non-cached operands
+  std::unique_ptr<Sliced> ta, tb;
+  Sliced* a = slice_prepare(c, A, M, K, sAm, sAk, BM, S, ta);
+  Sliced* b = a ? slice_prepare(c, B, N, K, sBn, sBk, bn, S, tb) : nullptr;
+  if (!a || !b || !a->range_ok || !b->range_ok) return false;
+  if (!k.sattr_set) {
+    UCC_CUDA(cudaFuncSetAttribute(sliced_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+    k.sattr_set = true;
+  }
+  SParams p;
+  p.M = (int)M;
+  p.N = (int)N;
+  p.bn = bn;
+  p.kblocks = (int)(a->kp / BK);
+  p.mtiles = (int)((M + BM - 1) / BM);
+  p.ntiles = (int)((N + bn - 1) / bn);
+  p.S = S;
+  p.gex = std::max(1, S - 2);
+  p.a_rows = (int)a->rows_p;
+  p.b_rows = (int)b->rows_p;
+  p.alpha = alpha;
+  p.beta = beta;
+  p.C = C;
+  p.epi = epi;
+  p.ea = a->e;
+  p.eb = b->e;
+  p.err = k.err;
+  p.ksplit = 1;
+  p.kchunk = p.kblocks;
+  const int tiles = p.mtiles * p.ntiles;
+  std::unique_ptr<Scratch> part;
+  // split K when the tiles fill the SMs poorly: the split (up to 8, chunks of >= 8 K blocks)
+  // with the fewest idle SM slots in the last wave; fixed-order FP64 reduce
+  int ks = 1;
+  {
+    double best = 1.0 - (double)tiles / ((double)((tiles + k.sms - 1) / k.sms) * k.sms);
+    for (int z = 2; z <= 8 && p.kblocks / z >= 8 && tiles < 2 * k.sms && 8.0 * M * N * z <= 2e9; z++) {
+      const double waste = 1.0 - (double)(tiles * z) / ((double)((tiles * z + k.sms - 1) / k.sms) * k.sms);
+      if (waste < best - 0.05) {
+        best = waste;
+        ks = z;
+      }
+    }
+  }
+  {
+    if (ks > 1) {
+      p.kchunk = (p.kblocks + ks - 1) / ks;
+      p.ksplit = (p.kblocks + p.kchunk - 1) / p.kchunk;
+      part = std::make_unique<Scratch>(c, sizeof(double) * M * N * p.ksplit);
+      p.C = part->d();
+      p.alpha = 1.0;
+      p.beta = 0.0;
+      p.epi.msplit = 0;
+      p.epi.s_mhi = N;
+      p.epi.s_n = 1;
+    }
+  }
+  const int grid = std::min(tiles * p.ksplit, k.sms);
+  sliced_gemm_kernel<<<grid, THREADS, SMEM_BYTES, c.stream>>>(a->map, b->map, p);
+  count_kernel_launch();
+  c.stats.sliced_gemm_launches++;
+  UCC_CUDA(cudaGetLastError());
+  if (part) splitk_reduce(c, M, N, p.ksplit, part->d(), alpha, beta, C, epi);
+  UCC_CUDA(cudaEventRecord(k.ev1, c.stream));
+  int herr = 0;
+  UCC_CUDA(cudaMemcpyAsync(&herr, k.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  UCC_CUDA(cudaStreamSynchronize(c.stream));  // keeps the temporary slices alive until the GEMM is done
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, k.ev0, k.ev1);
+  c.stats.sliced_gemm_ms += ms;
+  c.stats.sliced_gemm_flops += 2.0 * (double)M * (double)N * (double)K;
+  if (herr) {
+    cudaMemsetAsync(k.err, 0, sizeof(int), c.stream);
+    throw Error(UCC_DEVICE_TIMEOUT, "sliced FP64 GEMM: a pipeline wait timed out");
+  }
+  return true;
+}
 
 void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                  const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi, int parts,
@@ -597,6 +1105,23 @@ void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, con
     epi.s_n = sCn;
     tc_gemm_run(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, parts, kc);
   }
+}
+
+// FP64-accurate GEMM on the tensor cores (sliced operands) for the FP64 work of the MIXED
+// form; false when the problem is too small for it or outside its exponent range
+bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn) {
+  if (!tc_eligible(M, N, K) || (double)M * N * K < kSlicedMinWork) return false;
+  GemmEpilogue epi;
+  epi.msplit = 0;
+  if (M <= 256 && N > M) {  // the short side becomes the (narrow) N tile
+    epi.s_mhi = sCn;
+    epi.s_n = sCm;
+    return sliced_gemm_run(c, N, M, K, alpha, B, sBn, sBk, A, sAk, sAm, beta, C, epi, kSlices);
+  }
+  epi.s_mhi = sCm;
+  epi.s_n = sCn;
+  return sliced_gemm_run(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, kSlices);
 }
 
 bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,

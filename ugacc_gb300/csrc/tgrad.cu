@@ -1,4 +1,5 @@
-// (T) contributions to CCSD(T) first derivatives: tgrad_ooc of ccwfn.cc:1150-1316.
+// (T) contributions to CCSD(T) first derivatives: tgrad_ooc of ccwfn.cc:1150-1316 (OOC=1)
+// and tgrad of ccwfn.cc:854-1142 (OOC=0, the plugin's default).
 //
 // For every ordered occupied triple (i,j,k) the connected and disconnected triples
 //   M3(abc) = W3_ijk(abc) / D3,   N3(abc) = [<ij|ab> t1_kc + <ik|ac> t1_jb + <jk|bc> t1_ia
@@ -16,6 +17,14 @@
 // indexed by the occupied triple; because M3 and N3 are invariant under a simultaneous
 // permutation of (i,j,k) and (a,b,c), its occupied-permutation X3/Y3 equal the virtual
 // ones here, so Doo[i][i] -= 1/2 sum_{jk,abc} M3 (X3+Y3) reuses the Dvv partial sums.
+//
+// The in-core tgrad stores T3 and L3 and gives the same s1, s2, Dov, Goovv, Gooov and
+// Gvvvo, and full matrices (ccwfn.cc:998-1021)
+//   Doo[i][j] = -1/2 sum_{lm,def} t3_ilm^def l3_jlm^def,  Dvv[a][b] = 1/2 sum_{lmn,de} t3_lmn^bde l3_lmn^ade
+// whose diagonals are the ones above: its t3 is M3 and its l3 contracts like P3 = X3 + Y3.
+// With the same permutation invariance Doo[i][j] = -1/2 sum_{lm} M3_lmi . P3_lmj, so a
+// batch (fixed l, a range of m, every k) adds -1/2 sum_m M3_lmk1 . P3_lmk2 to Doo[k1][k2],
+// and 1/2 sum_{t,de} M3_t(bde) P3_t(ade) to Dvv[a][b]: two more engine contractions.
 //
 // Tuples are processed in batches (fixed i, a range of j, every k); W3 comes from the
 // FP64 tuple GEMMs of the (T) energy, the element-wise work from the kernels below, and
@@ -87,8 +96,8 @@ __device__ double block_sum(double v) {
 // Dvv diagonal, Dov and s1 terms
 __global__ void tg_reduce_kernel(int no, int nv, const int* __restrict__ tuples, const double* __restrict__ M,
                                  const double* __restrict__ N, const double* __restrict__ t2,
-                                 const double* __restrict__ Voovv, double* Q, double* Z, double* pdvv, double* pdov,
-                                 double* ps1) {
+                                 const double* __restrict__ Voovv, double* Q, double* Z, double* P, double* pdvv,
+                                 double* pdov, double* ps1) {
   const int a = blockIdx.x, t = blockIdx.y;
   const int j = tuples[3 * t + 1], k = tuples[3 * t + 2];
   const int64_t nv2 = (int64_t)nv * nv, nv3 = nv2 * nv;
@@ -109,6 +118,7 @@ __global__ void tg_reduce_kernel(int no, int nv, const int* __restrict__ tuples,
                       2.0 * at(n, c, a, b) + 2.0 * at(n, b, c, a);
     q[e] = 2.0 * X3 + Y3;
     z[e] = 2.0 * (mabc - macb) - (mbac - mbca);
+    if (P) P[(int64_t)t * nv3 + (int64_t)a * nv2 + e] = X3 + Y3;
     sdvv += 0.5 * mabc * (X3 + Y3);
     sdov += (mabc - mcba) * (4.0 * t2jk[(int64_t)b * nv + c] - 2.0 * t2jk[(int64_t)c * nv + b]);
     ss1 += (4.0 * mabc - 4.0 * mbac - 2.0 * macb + 2.0 * mcab) * vjk[(int64_t)b * nv + c];
@@ -176,13 +186,15 @@ void run_triples_gradient(Ctx& c) {
   // MIXED: W3 from the tensor-core tuple GEMMs (FP32 W3) and split contractions; the
   // element-wise algebra and every accumulation stay FP64
   const bool mixed = c.opt.precision == UCC_MIXED && !c.force_fp64;
+  const bool full = c.opt.ooc == 0;  // in-core tgrad: full Doo and Dvv
 
   // batch = (fixed i, nj values of j, every k): M3, N3, Q3, Z3 of each tuple plus the
   // engine's gathered copies of Q3 / Z3
   size_t free_b = 0, total_b = 0;
   UCC_CUDA(cudaMemGetInfo(&free_b, &total_b));
   const double budget = std::min<double>(24.0e9, 0.3 * (double)free_b);
-  const int nj = (int)std::max<int64_t>(1, std::min<int64_t>(no, (int64_t)(budget / (6.0 * 8.0 * nv3 * no))));
+  const double nbuf = full ? 8.0 : 6.0;  // + P3 and a gathered copy for the full Doo/Dvv
+  const int nj = (int)std::max<int64_t>(1, std::min<int64_t>(no, (int64_t)(budget / (nbuf * 8.0 * nv3 * no))));
   const int ntmax = nj * no;
   Tensor Acat, Bcat;
   const bool tc = mixed && mixed_triples_prepare(c, ntmax);
@@ -191,6 +203,15 @@ void run_triples_gradient(Ctx& c) {
   if (tc) W32 = std::make_unique<Scratch>(c, sizeof(float) * nv3 * ntmax);
   Scratch Mb(c, sizeof(double) * nv3 * ntmax), Nb(c, sizeof(double) * nv3 * ntmax);
   Scratch Qb(c, sizeof(double) * nv3 * ntmax), Zb(c, sizeof(double) * nv3 * ntmax);
+  std::unique_ptr<Scratch> Pb, diag;
+  if (full) {
+    Pb = std::make_unique<Scratch>(c, sizeof(double) * nv3 * ntmax);
+    diag = std::make_unique<Scratch>(c, sizeof(double) * ((size_t)no * no + (size_t)nv * nv));
+    UCC_CUDA(cudaMemsetAsync(diag->p, 0, sizeof(double) * ((size_t)no * no + (size_t)nv * nv), c.stream));
+  }
+  // the diagonal sums go to TDoo/TDvv, or to a scratch copy when the full matrices are formed
+  double* doo_diag = full ? diag->d() : Doo.p;
+  double* dvv_diag = full ? diag->d() + (size_t)no * no : Dvv.p;
   Scratch part(c, sizeof(double) * 3 * (size_t)ntmax * nv);
   Scratch dtup(c, sizeof(int) * 3 * ntmax);
   Scratch dptr(c, sizeof(GemmPtrs) * 6 * ntmax);
@@ -228,9 +249,10 @@ void run_triples_gradient(Ctx& c) {
       count_kernel_launch();
       UCC_REQUIRE(nt <= 65535, UCC_BAD_ARGS, "(T) gradient: too many tuples per batch");
       tg_reduce_kernel<<<dim3((unsigned)nv, (unsigned)nt), 256, 0, c.stream>>>(
-          no, nv, static_cast<int*>(dtup.p), Mb.d(), Nb.d(), t2.p, Voovv, Qb.d(), Zb.d(), pdvv, pdov, ps1);
+          no, nv, static_cast<int*>(dtup.p), Mb.d(), Nb.d(), t2.p, Voovv, Qb.d(), Zb.d(), full ? Pb->d() : nullptr,
+          pdvv, pdov, ps1);
       count_kernel_launch();
-      tg_accumulate_kernel<<<1, 256, 0, c.stream>>>(no, nv, nt, i, pdvv, pdov, ps1, Dvv.p, Dov.p, S1.p, Doo.p);
+      tg_accumulate_kernel<<<1, 256, 0, c.stream>>>(no, nv, nt, i, pdvv, pdov, ps1, dvv_diag, Dov.p, S1.p, doo_diag);
       count_kernel_launch();
       UCC_CUDA(cudaGetLastError());
       const Tensor Q = make_view(Qb.d(), {nb, no, nv, nv, nv}), Z = make_view(Zb.d(), {nb, no, nv, nv, nv});
@@ -244,6 +266,13 @@ void run_triples_gradient(Ctx& c) {
       contract(c, "jkabc,dkbc->jad", 1.0, Q, Vvovv, 1.0, narrow(X2.slice0(i), 0, j0, nb));
       // Gvvvo[a][b][d][j] += sum_kc Q3 t2[k][i][c][d]
       contract(c, "jkabc,kcd->abdj", 1.0, Q, select(t2, 1, i), 1.0, narrow(Gvvvo, 3, j0, nb));
+      if (full) {
+        // Dvv[a][b] += 1/2 sum_{t,de} M3_t(bde) P3_t(ade);  Doo[k1][k2] -= 1/2 sum_{j,abc} M3_ijk1 P3_ijk2
+        const Tensor M4 = make_view(Mb.d(), {nt, nv, nv, nv}), P4 = make_view(Pb->d(), {nt, nv, nv, nv});
+        contract(c, "tbde,tade->ab", 0.5, M4, P4, 1.0, Dvv);
+        const Tensor M3 = make_view(Mb.d(), {nb, no, nv3}), P3 = make_view(Pb->d(), {nb, no, nv3});
+        contract(c, "jkx,jlx->kl", -0.5, M3, P3, 1.0, Doo);
+      }
     }
   }
   // s2 = X2 + X2(ji,ba)

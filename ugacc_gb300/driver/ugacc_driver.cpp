@@ -4,7 +4,7 @@
 //
 // usage: ugacc_driver <input.bin> [WFN=CCSD|CCSD_T] [DERTYPE=NONE|FIRST|SECOND]
 //        [MAXITER=100] [R_CONVERGENCE=1e-7] [DIIS=1] [MY_OMEGA=0] [MYHAND=RIGHT|LEFT]
-//        [PRECISION=FP64|MIXED] [REFINE_SWEEPS=2] [PRINT=0]
+//        [PRECISION=FP64|MIXED] [REFINE_SWEEPS=2] [PRINT=0] [OOC=0|1]
 // Prints one JSON object with the energies (and polarizabilities for DERTYPE=SECOND).
 #include <cstdint>
 #include <cstdio>
@@ -80,6 +80,7 @@ int main(int argc, char** argv) {
     o.r_convergence = std::atof(get("R_CONVERGENCE", "1e-7").c_str());
     o.my_omega = std::atof(get("MY_OMEGA", "0").c_str());
     o.diis = get("DIIS", "1") == "1";
+    o.ooc = get("OOC", "0") == "1";
 
     auto H = std::make_shared<Hamiltonian>(in.no, in.nv, in.naux, fock.data(), in.B.data());
     auto cc = std::make_shared<CCWfn>(H, o);

@@ -24,7 +24,8 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--iters", type=int, default=1)
     ap.add_argument("--triples", action="store_true")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "sliced"],
+                    help="sliced: with --gemm only, the FP64-accurate sliced tensor-core GEMM")
     ap.add_argument("--gemm", type=int, nargs=3, metavar=("M", "N", "K"))
     ap.add_argument("--print", type=int, nargs="?", const=1, default=0,
                     help="print the iteration tables (2: also the residual error of every mixed sweep)")
@@ -46,8 +47,18 @@ def main(argv=None):
         rng = np.random.default_rng(0)
         ctx = U.Context()
         A, B = rng.standard_normal((M, K)), rng.standard_normal((K, N))
-        ctx.gemm(A, B, precision=U.MIXED if a.precision == "mixed" else U.FP64)
-        print(json.dumps({"gemm": [M, N, K], "precision": a.precision}))
+        prec = {"mixed": U.MIXED, "sliced": U.FP64_SLICED}.get(a.precision, U.FP64)
+        for rep in range(3):
+            ctx.reset_stats()
+            C = ctx.gemm(A, B, precision=prec)
+            st = ctx.stats()
+        ms = {U.MIXED: st["tc_gemm_ms"], U.FP64_SLICED: st["sliced_gemm_ms"]}.get(prec, st["fp64_gemm_ms"])
+        err = None
+        if M * N * K <= 2e10:
+            ref = A @ B
+            err = float(np.abs(C - ref).max() / np.abs(ref).max())
+        print(json.dumps({"gemm": [M, N, K], "precision": a.precision, "ms": ms,
+                          "tflops": 2.0 * M * N * K / (ms * 1e-3) / 1e12 if ms else None, "max_rel_err": err}))
         return 0
     h = make_hamiltonian(a.no, a.nv, a.seed)
     H = U.Hamiltonian.from_synthetic(h)
