@@ -130,3 +130,38 @@ def test_fine_split_gemm_matches_fp64():
         got = ctx.gemm(A, B, C0, alpha=0.5, beta=0.25, precision=U.MIXED_FINE)
         scale = 0.5 * np.abs(A) @ np.abs(B)
         assert np.all(np.abs(got - ref) <= SPLIT_RTOL * scale + 1e-12)
+
+
+@pytest.mark.parametrize("M,N,K,ta,tb", [(128, 256, 64, 0, 0), (300, 520, 777, 0, 1), (257, 129, 1000, 1, 0),
+                                          (40, 3000, 5000, 0, 1), (1000, 300, 96, 1, 1), (640, 768, 20000, 0, 0)])
+def test_sliced_fp64_gemm(M, N, K, ta, tb):
+    """UCC_FP64_SLICED: 8 exact bf16 slices per operand on the tensor cores, FP64-accurate
+    (error of the order of FP64 rounding, relative to the row / column maxima)."""
+    rng = np.random.default_rng(M * 7 + N + K)
+    A = rng.standard_normal((K, M) if ta else (M, K)) * np.exp(2.0 * rng.standard_normal((K, M) if ta else (M, K)))
+    B = rng.standard_normal((N, K) if tb else (K, N))
+    A[..., 3] = 0.0  # zero rows / columns and tiny entries
+    B[..., 5] *= 1e-30
+    C0 = rng.standard_normal((M, N))
+    ctx = U.Context()
+    Am, Bm = (A.T if ta else A), (B.T if tb else B)
+    ref = 0.7 * Am @ Bm - 0.3 * C0
+    got = ctx.gemm(A, B, C0, alpha=0.7, beta=-0.3, transa=ta, transb=tb, precision=U.FP64_SLICED)
+    scale = 0.7 * np.abs(Am).max(axis=1)[:, None] * np.abs(Bm).max(axis=0)[None, :]
+    err = np.abs(got - ref)
+    assert np.all(err <= 1e-14 * np.sqrt(K) * scale + 1e-15 * np.abs(ref) + 1e-300), (err / scale).max()
+    st = ctx.stats()
+    assert st["sliced_gemm_launches"] == 1
+
+
+def test_mixed_record_sweeps_use_the_sliced_gemm():
+    """The FP64 work of a MIXED solve (record sweeps, HBAR) runs on the sliced tensor-core
+    GEMM and keeps the FP64 answer."""
+    h = make_hamiltonian(12, 96, 9)
+    H = U.Hamiltonian.from_synthetic(h)
+    e64 = U.CCWfn(H, {"R_CONVERGENCE": 1e-10}).compute_energy()
+    H.ctx.reset_stats()
+    emx = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": "MIXED"}).compute_energy()
+    st = H.ctx.stats()
+    assert st["sliced_gemm_launches"] > 0 and st["fp64_iterations"] >= 2
+    assert abs(emx - e64) < 1e-9

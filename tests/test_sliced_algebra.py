@@ -10,16 +10,19 @@ import numpy as np
 
 
 def _slices(X, S):
+    """Digits as slice_digits_kernel forms them: x 2^(7S-e) rounded to an integer, then
+    balanced base-128 digits from the least significant one up."""
     amax = np.abs(X).max(axis=1)
-    e = np.where(amax > 0, np.floor(np.log2(np.where(amax > 0, amax, 1.0))).astype(int) + 2, -500)
+    e = np.where(amax > 0, np.frexp(np.where(amax > 0, amax, 1.0))[1] + 1, -500)  # ilogb + 2
     v = X * np.ldexp(1.0, -e)[:, None]
     assert np.all(np.abs(v) < 0.5)
-    out = []
-    for s in range(S):
-        v = v * 128.0
-        d = np.rint(v)
-        v = v - d
-        out.append(d)
+    Xi = np.rint(np.ldexp(v, 7 * S)).astype(np.int64)  # exact: |v 2^(7S)| < 2^55
+    out = [None] * S
+    for s in range(S - 1, 0, -1):
+        d = ((Xi + 64) & 127) - 64
+        Xi = (Xi - d) >> 7
+        out[s] = d.astype(np.float64)
+    out[0] = Xi.astype(np.float64)
     return np.array(out), e
 
 

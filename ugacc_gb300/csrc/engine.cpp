@@ -10,6 +10,8 @@ namespace ucc {
 bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn);
 bool tc_eligible(int64_t M, int64_t N, int64_t K);
+bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn);
 void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
                       int64_t sAk, const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm,
                       int64_t sCn, int parts, int kc);
@@ -242,10 +244,12 @@ void anchored_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const 
       permute_add(c, bv, 1.0, 0.0, make_view(t.b0->p, {K, N}));
     }
     t.p0 = std::make_unique<DeviceBuffer>((size_t)(M * N));
-    GemmEpilogue epi;
-    epi.s_mhi = N;
-    epi.s_n = 1;
-    dgemm_strided(c, M, N, K, 1.0, A, sAm, sAk, B, sBk, sBn, 0.0, t.p0->p, epi, 1, 0, 0, 0, nullptr);
+    if (!sliced_gemm(c, M, N, K, 1.0, A, sAm, sAk, B, sBk, sBn, 0.0, t.p0->p, N, 1)) {
+      GemmEpilogue epi;
+      epi.s_mhi = N;
+      epi.s_n = 1;
+      dgemm_strided(c, M, N, K, 1.0, A, sAm, sAk, B, sBk, sBn, 0.0, t.p0->p, epi, 1, 0, 0, 0, nullptr);
+    }
     permute_add(c, make_view(t.p0->p, {M, N}), alpha, beta, cv);
     an.terms.push_back(std::move(t));
     an.next++;
@@ -499,6 +503,10 @@ void contract(Ctx& c, const std::string& spec, double alpha, const Tensor& A, co
   }
   if (!done && c.opt.precision == UCC_MIXED && !c.force_fp64)
     done = mixed_gemm(c, M, N, K, ga, a.p, sAm, sAk, b.p, sBk, sBn, gb, ct.p, sCm, sCn);
+  // the FP64 work of the MIXED form (refinement sweeps, one-shot builds): sliced operands
+  // on the tensor cores, FP64-accurate
+  if (!done && c.opt.precision == UCC_MIXED && !recorder())
+    done = sliced_gemm(c, M, N, K, ga, a.p, sAm, sAk, b.p, sBk, sBn, gb, ct.p, sCm, sCn);
   if (!done) {
     GemmEpilogue epi;
     epi.msplit = 0;

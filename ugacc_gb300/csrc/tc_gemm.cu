@@ -449,6 +449,20 @@ __device__ __forceinline__ double pow2i(int e) {  // 2^e for -1022 <= e <= 1023
   return __longlong_as_double((long long)(e + 1023) << 52);
 }
 
+// FP32 -> FP64 by moving the bit fields (integer pipe); exact for zero and normal values,
+// which are all an accumulator of slice products can hold (multiples of 2^-63)
+__device__ __forceinline__ double f32_bits_to_f64(uint32_t fb) {
+  if ((fb & 0x7FFFFFFFu) == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)(fb >> 31) << 63;
+  const unsigned long long ex = (unsigned long long)(((fb >> 23) & 0xFFu) + 896u) << 52;
+  const unsigned long long mt = (unsigned long long)(fb & 0x7FFFFFu) << 29;
+  return __longlong_as_double((long long)(sgn | ex | mt));
+}
+
+// shared memory of the sliced kernel: the operand ring, barriers, and a 32 x 33 FP32
+// transpose buffer per epilogue warp
+constexpr size_t SLICED_SMEM_BYTES = SMEM_BYTES + 4 * 32 * 33 * sizeof(float);
+
 __global__ void __launch_bounds__(THREADS, 1)
     sliced_gemm_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, SParams p) {
   extern __shared__ uint8_t smem_raw[];
@@ -586,11 +600,19 @@ __global__ void __launch_bounds__(THREADS, 1)
       int k0, kn;
       krange(tile, k0, kn);
       const int nu = sunit_count(p.S, p.gex, kn);
-      const int64_t m = (int64_t)mt * BM + q * 32 + lane;
-      const int64_t mo = ep.msplit ? (m / ep.msplit) * ep.s_mhi + (m % ep.msplit) * ep.s_mlo : m * ep.s_mhi;
+      const int64_t mw = (int64_t)mt * BM + q * 32;  // first row of this warp
+      const int64_t m = mw + lane;
+      auto moff = [&](int64_t mm) {
+        return ep.msplit ? (mm / ep.msplit) * ep.s_mhi + (mm % ep.msplit) * ep.s_mlo : mm * ep.s_mhi;
+      };
+      const int64_t mo = moff(m);
       // alpha 2^e_m; the column factor 2^e_n is added to its exponent field (|e| <= 500 and
       // 2^-20 <= |alpha| <= 2^20 keep the result normal)
       const long long sa = m < p.M ? __double_as_longlong(p.alpha * pow2i(p.ea[m])) : 0;
+      // lanes run along the rows when those are contiguous in C; otherwise the 32 x 32 block
+      // is transposed through shared memory so that lanes run along the columns
+      const bool rows_contiguous = ep.msplit == 0 && ep.s_mhi == 1;
+      float* tsm = reinterpret_cast<float*>(smem + STAGES * (A_BYTES + B_BYTES) + 256) + (warp - 2) * 32 * 33;
       for (int u = 0; u < nu; u++) {
         if (!mbar_wait(&tfull[acc], aphase, p.err)) {
           ok = false;
@@ -598,27 +620,61 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         fence_after();
         const bool first = u == 0;
+        const bool load_old = !(first && p.beta == 0.0);
         for (int ch = 0; ch < nch; ch++) {
           uint32_t r[32];
           tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + ch * 32), r);
-          if (m < p.M) {
-            const int64_t n0 = (int64_t)nt * p.bn + ch * 32;
-            double* Cb = p.C + coff + mo;
-            double old[32];
+          const int64_t n0 = (int64_t)nt * p.bn + ch * 32;
+          if (rows_contiguous) {
+            if (m < p.M) {
+              double* Cb = p.C + coff + mo;
 #pragma unroll
-            for (int j = 0; j < 32; j++) {
-              old[j] = 0.0;
-              if (n0 + j < p.N && !(first && p.beta == 0.0)) {
-                old[j] = Cb[(n0 + j) * ep.s_n];
-                if (first) old[j] *= p.beta;
+              for (int h = 0; h < 32; h += 16) {  // 16 columns at a time: loads in flight together
+                double old[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                  old[j] = 0.0;
+                  if (n0 + h + j < p.N && load_old) {
+                    old[j] = Cb[(n0 + h + j) * ep.s_n];
+                    if (first) old[j] *= p.beta;
+                  }
+                }
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                  if (n0 + h + j < p.N) {
+                    const double f = __longlong_as_double(sa + ((long long)p.eb[n0 + h + j] << 52));
+                    Cb[(n0 + h + j) * ep.s_n] = fma(f32_bits_to_f64(r[h + j]), f, old[j]);
+                  }
               }
             }
+          } else {
 #pragma unroll
-            for (int j = 0; j < 32; j++)
-              if (n0 + j < p.N) {
-                const double f = __longlong_as_double(sa + ((long long)p.eb[n0 + j] << 52));
-                Cb[(n0 + j) * ep.s_n] = fma((double)__uint_as_float(r[j]), f, old[j]);
+            for (int j = 0; j < 32; j++) tsm[lane * 33 + j] = __uint_as_float(r[j]);
+            __syncwarp();
+            const int64_t n = n0 + lane;  // this lane's column
+            const bool nok = n < p.N;
+            const long long ebs = nok ? (long long)p.eb[n] << 52 : 0;
+            double* Cn = p.C + coff + n * ep.s_n;
+#pragma unroll
+            for (int h = 0; h < 32; h += 16) {
+              double old[16];
+#pragma unroll
+              for (int i = 0; i < 16; i++) {
+                old[i] = 0.0;
+                if (nok && mw + h + i < p.M && load_old) {
+                  old[i] = Cn[moff(mw + h + i)];
+                  if (first) old[i] *= p.beta;
+                }
               }
+#pragma unroll
+              for (int i = 0; i < 16; i++) {
+                const long long sai = __shfl_sync(0xffffffffu, sa, h + i);
+                if (nok && mw + h + i < p.M)
+                  Cn[moff(mw + h + i)] = fma(f32_bits_to_f64(__float_as_uint(tsm[(h + i) * 33 + lane])),
+                                             __longlong_as_double(sai + ebs), old[i]);
+              }
+            }
+            __syncwarp();
           }
         }
         fence_before();
@@ -638,28 +694,37 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
-// row maxima |x| of a rows x cols FP64 view as bit patterns (positive doubles order like
-// their bits); 32 x 32 tiles, reads coalesced along whichever stride is 1
+// row maxima |x| of a rows x cols FP64 view as bit patterns (non-negative doubles order
+// like their bits, so the maximum is an integer one); a block covers 32 rows and all of K,
+// with lanes along k (sk == 1) or along the rows (transposed views)
 __global__ void slice_absmax_kernel(int64_t rows, int64_t cols, const double* __restrict__ x, int64_t sr, int64_t sk,
                                     unsigned long long* amax) {
-  __shared__ double t[32][33];
-  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
+  __shared__ unsigned long long t[8][32];
+  const int64_t r0 = (int64_t)blockIdx.x * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  for (int i = ty; i < 32; i += 8) {
-    // sk == 1: lanes run along k; otherwise along r (transposed views)
-    const int64_t r = sk == 1 ? r0 + i : r0 + tx, k = sk == 1 ? k0 + tx : k0 + i;
-    const double v = (r < rows && k < cols) ? fabs(x[r * sr + k * sk]) : 0.0;
-    if (sk == 1)
-      t[i][tx] = v;
-    else
-      t[tx][i] = v;
-  }
-  __syncthreads();
-  // row i of the tile: warp ty reduces rows ty, ty+8, ...
-  for (int i = ty; i < 32; i += 8) {
-    double v = t[i][tx];
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (tx == 0 && r0 + i < rows && v > 0.0) atomicMax(amax + r0 + i, (unsigned long long)__double_as_longlong(v));
+  const unsigned long long absmask = 0x7FFFFFFFFFFFFFFFull;
+  if (sk == 1) {
+    for (int i = ty; i < 32; i += 8) {
+      const int64_t r = r0 + i;
+      unsigned long long mm = 0;
+      if (r < rows)
+        for (int64_t k = tx; k < cols; k += 32)
+          mm = max(mm, (unsigned long long)__double_as_longlong(x[r * sr + k]) & absmask);
+      for (int o = 16; o > 0; o >>= 1) mm = max(mm, __shfl_xor_sync(0xffffffffu, mm, o));
+      if (tx == 0 && r < rows) amax[r] = mm;
+    }
+  } else {
+    const int64_t r = r0 + tx;
+    unsigned long long mm = 0;
+    if (r < rows)
+      for (int64_t k = ty; k < cols; k += 8)
+        mm = max(mm, (unsigned long long)__double_as_longlong(x[r * sr + k * sk]) & absmask);
+    t[ty][tx] = mm;
+    __syncthreads();
+    if (ty == 0 && r < rows) {
+      for (int i = 1; i < 8; i++) mm = max(mm, t[i][tx]);
+      amax[r] = mm;
+    }
   }
 }
 
@@ -676,8 +741,27 @@ __device__ __forceinline__ int slice_exponent(unsigned long long bits, int* rang
   return max(e, -500);
 }
 
+// x 2^(bits-e) rounded to an integer (|result| < 2^(bits-1) since |x| < 2^(e-1); bits <= 56),
+// from the bit fields of x with integer operations only
+__device__ __forceinline__ long long slice_fixed(double x, int e, int bits) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)((b >> 52) & 0x7FF);
+  const long long mant = (long long)(b & 0xFFFFFFFFFFFFFull) | (E ? (1ll << 52) : 0ll);
+  const int shift = max(E, 1) - 1075 + bits - e;  // x = mant 2^(max(E,1) - 1075)
+  long long v;
+  if (shift >= 0)
+    v = mant << shift;
+  else if (shift > -63)
+    v = (mant + (1ll << (-shift - 1))) >> (-shift);
+  else
+    v = 0;
+  return (b >> 63) ? -v : v;
+}
+
 // digits: slices[s][r][k] = bf16(d_s 2^-7(s+1)) for r < rows_p (zero past rows), k < kp
-// (zero past cols); e[r] written by the blocks of the first K tile
+// (zero past cols), the balanced base-128 digits of x 2^(7S-e) (least significant s = S-1);
+// e[r] written by the blocks of the first K tile.  32 x 32 tiles through shared memory:
+// reads coalesced along whichever stride is 1, writes along k.
 __global__ void slice_digits_kernel(int64_t rows, int64_t cols, int64_t rows_p, int64_t kp, const double* __restrict__ x,
                                     int64_t sr, int64_t sk, const unsigned long long* __restrict__ amax, int S,
                                     __nv_bfloat16* slices, int* e_out, int* range) {
@@ -693,18 +777,23 @@ __global__ void slice_digits_kernel(int64_t rows, int64_t cols, int64_t rows_p, 
       t[tx][i] = v;
   }
   __syncthreads();
+  const size_t plane = (size_t)rows_p * kp;
   for (int i = ty; i < 32; i += 8) {
     const int64_t r = r0 + i, k = k0 + tx;
     if (r >= rows_p || k >= kp) continue;
     const int e = r < rows ? slice_exponent(amax[r], range) : 0;
     if (k == 0 && r < rows) e_out[r] = e;
-    double v = r < rows ? t[i][tx] * pow2i(-e) : 0.0;  // in (-1/2, 1/2)
-    const size_t plane = (size_t)rows_p * kp;
-    for (int s = 0; s < S; s++) {
-      v *= 128.0;
-      const double d = rint(v);
-      v -= d;
-      slices[(size_t)s * plane + (size_t)r * kp + k] = __double2bfloat16(d * pow2i(-7 * (s + 1)));
+    long long X = r < rows ? slice_fixed(t[i][tx], e, 7 * S) : 0;
+    __nv_bfloat16* dst = slices + (size_t)r * kp + k;
+    for (int s = S - 1; s >= 0; s--) {
+      long long d;
+      if (s > 0) {
+        d = ((X + 64) & 127) - 64;  // balanced digit in [-64, 63]
+        X = (X - d) >> 7;
+      } else {
+        d = X;  // what remains: |d| <= 64
+      }
+      dst[(size_t)s * plane] = __float2bfloat16_rn((float)d * __int_as_float((127 - 7 * (s + 1)) << 23));
     }
   }
 }
@@ -885,10 +974,9 @@ static Sliced* slice_prepare(Ctx& c, const double* x, int64_t rows, int64_t cols
     s->e = reinterpret_cast<int*>(static_cast<char*>(s->tmp->p) + ((sizeof(__nv_bfloat16) * nel + 15) / 16) * 16);
   }
   Scratch amax(c, sizeof(unsigned long long) * rows);
-  UCC_CUDA(cudaMemsetAsync(amax.p, 0, sizeof(unsigned long long) * rows, c.stream));
   UCC_CUDA(cudaMemsetAsync(k.range, 0, sizeof(int), c.stream));
   const dim3 blk(32, 8);
-  slice_absmax_kernel<<<dim3((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32)), blk, 0, c.stream>>>(
+  slice_absmax_kernel<<<(unsigned)((rows + 31) / 32), blk, 0, c.stream>>>(
       rows, cols, x, sr, sk, static_cast<unsigned long long*>(amax.p));
   count_kernel_launch();
   slice_digits_kernel<<<dim3((unsigned)(s->kp / 32), (unsigned)(s->rows_p / 32)), blk, 0, c.stream>>>(
@@ -934,7 +1022,8 @@ bool sliced_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, cons
   Sliced* b = a ? slice_prepare(c, B, N, K, sBn, sBk, bn, S, tb) : nullptr;
   if (!a || !b || !a->range_ok || !b->range_ok) return false;
   if (!k.sattr_set) {
-    UCC_CUDA(cudaFuncSetAttribute(sliced_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+    UCC_CUDA(cudaFuncSetAttribute(sliced_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)SLICED_SMEM_BYTES));
     k.sattr_set = true;
   }
   SParams p;
@@ -986,7 +1075,7 @@ bool sliced_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, cons
     }
   }
   const int grid = std::min(tiles * p.ksplit, k.sms);
-  sliced_gemm_kernel<<<grid, THREADS, SMEM_BYTES, c.stream>>>(a->map, b->map, p);
+  sliced_gemm_kernel<<<grid, THREADS, SLICED_SMEM_BYTES, c.stream>>>(a->map, b->map, p);
   count_kernel_launch();
   c.stats.sliced_gemm_launches++;
   UCC_CUDA(cudaGetLastError());
