@@ -272,7 +272,7 @@ def main():
     barrier()
     t1 = time.perf_counter()
     for _ in range(e2e_steps):
-        H2 = U.Hamiltonian(NO, NV, Fp.numpy(), B=Bp.numpy(), context=ctx2)
+        H2 = U.Hamiltonian(NO, NV, Fp.numpy(), B=Bp.numpy(), context=ctx2, precision=args.precision.upper())
         c2 = U.CCWfn(H2, opts)
         c2.compute_energy()
     barrier()

@@ -230,9 +230,12 @@ class Hamiltonian:
     density-fitting factors ``B`` ([naux][nact][nact]) are accepted."""
 
     def __init__(self, no: int, nv: int, fock: np.ndarray, ints: np.ndarray | None = None,
-                 B: np.ndarray | None = None, device: int = 0, context: Context | None = None):
+                 B: np.ndarray | None = None, device: int = 0, context: Context | None = None,
+                 precision: str | None = None):
         self.no, self.nv = no, nv
         self.ctx = context or Context(device)
+        if precision is not None:  # "MIXED": the blocks are built by the sliced tensor-core GEMM
+            self.ctx.set_options(precision=MIXED if precision.upper() == "MIXED" else FP64)
         f = np.ascontiguousarray(fock, dtype=np.float64)
         if ints is not None:
             x = np.ascontiguousarray(ints, dtype=np.float64)

@@ -286,6 +286,7 @@ void triples_energy(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, con
                     const double* t1, const double* Voovv, const double* eps, double* d_partial);
 // The same from an FP32 W3 (mixed form): per-element arithmetic in FP32, the energy sum
 // in FP64 (compensated).
+int64_t triples_f32_partials(int nv);  // partial sums per tuple written by triples_energy_f32
 void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, const double* t1,
                         const double* Voovv, const double* eps, double* d_partial);
 

@@ -632,59 +632,93 @@ __global__ void triples_energy_kernel(int no, int nv, const int* tuples, const d
   if (threadIdx.x == 0) partial[(int64_t)t * nv + a] = tot;
 }
 
-// FP32 W3 (mixed form): the per-element V3/X3/Y3/Z3 algebra in FP32, the sum in FP64
-__global__ void triples_energy_f32_kernel(int no, int nv, const int* tuples, const float* W3, const double* t1,
-                                          const double* Voovv, const double* eps, double* partial) {
-  extern __shared__ float sh[];  // t1 rows i, j, k and the orbital energies of the virtuals
-  const int t = blockIdx.y;
-  const int a = blockIdx.x;
+// FP32 W3 (mixed form): the per-element V3/X3/Y3/Z3 algebra in FP32, the sums in FP64.
+// Block (r, t) takes the sorted tile triple r (tiles
+// A >= B >= C of edge ET along the virtual axis) of tuple t and stages the six permutation
+// tiles W[A][B][C], W[A][C][B], ..., W[C][B][A] in shared memory with coalesced loads, so
+// every W3 element is read from memory once; the Voovv blocks and t1 / eps pieces of the
+// three tile ranges are staged too.  Roles 0, 1, 2 are the index ranges of a, b, c.
+constexpr int ET = 8;
+__global__ void __launch_bounds__(128) triples_energy_f32_tiled_kernel(int no, int nv, const int* __restrict__ tuples,
+                                                                      const int* __restrict__ tri, int ntri,
+                                                                      const float* __restrict__ W3,
+                                                                      const double* __restrict__ t1,
+                                                                      const double* __restrict__ Voovv,
+                                                                      const double* __restrict__ eps, double* partial) {
+  __shared__ float Ws[6][ET][ET][ET + 1];
+  __shared__ float Vs[3][6][ET][ET + 1];  // Vij, Vik, Vjk on the 6 ordered role pairs
+  __shared__ float s1[3][3][ET];          // t1 rows i, j, k on the 3 role ranges
+  __shared__ float ev[3][ET];
+  const int r = blockIdx.x, t = blockIdx.y;
+  const int code = tri[r];
+  const int R0[3] = {(code & 1023) * ET, ((code >> 10) & 1023) * ET, (code >> 20) * ET};
   const int i = tuples[3 * t], j = tuples[3 * t + 1], k = tuples[3 * t + 2];
   const int64_t nv2 = (int64_t)nv * nv;
-  float* s1i = sh;
-  float* s1j = sh + nv;
-  float* s1k = sh + 2 * nv;
-  float* sev = sh + 3 * nv;
-  for (int x = threadIdx.x; x < nv; x += blockDim.x) {
-    s1i[x] = (float)t1[(int64_t)i * nv + x];
-    s1j[x] = (float)t1[(int64_t)j * nv + x];
-    s1k[x] = (float)t1[(int64_t)k * nv + x];
-    sev[x] = (float)eps[no + x];
+  const float* W = W3 + (int64_t)t * nv2 * nv;
+  // role order of each permutation tile p: W[x in role P[p][0]][y in P[p][1]][z in P[p][2]]
+  const int P[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  for (int e = threadIdx.x; e < 6 * ET * ET * ET; e += blockDim.x) {
+    const int p = e / (ET * ET * ET), rem = e - p * (ET * ET * ET);
+    const int x = rem / (ET * ET), y = (rem / ET) % ET, z = rem % ET;
+    const int gx = R0[P[p][0]] + x, gy = R0[P[p][1]] + y, gz = R0[P[p][2]] + z;
+    Ws[p][x][y][z] = (gx < nv && gy < nv && gz < nv) ? W[(int64_t)gx * nv2 + (int64_t)gy * nv + gz] : 0.f;
+  }
+  const double* Vm[3] = {Voovv + ((int64_t)i * no + j) * nv2, Voovv + ((int64_t)i * no + k) * nv2,
+                         Voovv + ((int64_t)j * no + k) * nv2};
+  for (int e = threadIdx.x; e < 3 * 6 * ET * ET; e += blockDim.x) {
+    const int m = e / (6 * ET * ET), rem = e - m * (6 * ET * ET);
+    const int pid = rem / (ET * ET), x = (rem / ET) % ET, y = rem % ET;
+    const int u = pid / 2, v0 = pid % 2, v = v0 < u ? v0 : v0 + 1;  // ordered role pair (u, v), u != v
+    const int gx = R0[u] + x, gy = R0[v] + y;
+    Vs[m][pid][x][y] = (gx < nv && gy < nv) ? (float)Vm[m][(int64_t)gx * nv + gy] : 0.f;
+  }
+  if (threadIdx.x < 3 * 3 * ET) {
+    const int m = threadIdx.x / (3 * ET), role = (threadIdx.x / ET) % 3, l = threadIdx.x % ET;
+    const int row = m == 0 ? i : (m == 1 ? j : k), g = R0[role] + l;
+    s1[m][role][l] = g < nv ? (float)t1[(int64_t)row * nv + g] : 0.f;
+  }
+  if (threadIdx.x < 3 * ET) {
+    const int role = threadIdx.x / ET, l = threadIdx.x % ET, g = R0[role] + l;
+    ev[role][l] = g < nv ? (float)eps[no + g] : 0.f;
   }
   __syncthreads();
-  const float* W = W3 + (int64_t)t * nv2 * nv;
-  const double* Vij = Voovv + ((int64_t)i * no + j) * nv2;
-  const double* Vik = Voovv + ((int64_t)i * no + k) * nv2;
-  const double* Vjk = Voovv + ((int64_t)j * no + k) * nv2;
   const float eijk = (float)(eps[i] + eps[j] + eps[k]);
   const float fac = 2.0f - (float)((i == j) + (i == k) + (j == k));
-  const float inv[4] = {1.0f, 0.5f, 0.25f, 0.25f};  // 1 / (1 + #equal index pairs): 0, 1 or 3 pairs
-  double s = 0.0, cc = 0.0;
-  const int npair = (a + 1) * (a + 1);
-  for (int q = threadIdx.x; q < npair; q += blockDim.x) {
-    const int b = q / (a + 1), c = q % (a + 1);
-    if (c > b) continue;
-    auto Wv = [&](int x, int y, int z) { return W[(int64_t)x * nv2 + (int64_t)y * nv + z]; };
-    auto Vv = [&](int x, int y, int z) {
-      const float num = Wv(x, y, z) + (float)Vij[(int64_t)x * nv + y] * s1k[z] +
-                        (float)Vik[(int64_t)x * nv + z] * s1j[y] + (float)Vjk[(int64_t)y * nv + z] * s1i[x];
-      return num * inv[(x == y) + (x == z) + (y == z)];
-    };
-    const float wabc = Wv(a, b, c), wacb = Wv(a, c, b), wbac = Wv(b, a, c);
-    const float wbca = Wv(b, c, a), wcab = Wv(c, a, b), wcba = Wv(c, b, a);
-    const float vabc = Vv(a, b, c), vacb = Vv(a, c, b), vbac = Vv(b, a, c);
-    const float vbca = Vv(b, c, a), vcab = Vv(c, a, b), vcba = Vv(c, b, a);
+  const float inv[4] = {1.0f, 0.5f, 0.25f, 0.25f};
+  auto pid = [](int u, int v) { return u * 2 + (v > u ? v - 1 : v); };
+  // V at one permutation: roles (r0, r1, r2) with local indices (l0, l1, l2), global (g0, g1, g2)
+  auto Vp = [&](float w, int r0, int l0, int r1, int l1, int r2, int l2, int g0, int g1, int g2) {
+    const float num = w + Vs[0][pid(r0, r1)][l0][l1] * s1[2][r2][l2] + Vs[1][pid(r0, r2)][l0][l2] * s1[1][r1][l1] +
+                      Vs[2][pid(r1, r2)][l1][l2] * s1[0][r0][l0];
+    return num * inv[(g0 == g1) + (g0 == g2) + (g1 == g2)];
+  };
+  double s = 0.0;
+  for (int q = threadIdx.x; q < ET * ET * ET; q += blockDim.x) {
+    const int la = q / (ET * ET), lb = (q / ET) % ET, lc = q % ET;
+    const int a = R0[0] + la, b = R0[1] + lb, c = R0[2] + lc;
+    if (a >= nv || b > a || c > b) continue;
+    const float wabc = Ws[0][la][lb][lc], wacb = Ws[1][la][lc][lb], wbac = Ws[2][lb][la][lc];
+    const float wbca = Ws[3][lb][lc][la], wcab = Ws[4][lc][la][lb], wcba = Ws[5][lc][lb][la];
+    const float vabc = Vp(wabc, 0, la, 1, lb, 2, lc, a, b, c), vacb = Vp(wacb, 0, la, 2, lc, 1, lb, a, c, b);
+    const float vbac = Vp(wbac, 1, lb, 0, la, 2, lc, b, a, c), vbca = Vp(wbca, 1, lb, 2, lc, 0, la, b, c, a);
+    const float vcab = Vp(wcab, 2, lc, 0, la, 1, lb, c, a, b), vcba = Vp(wcba, 2, lc, 1, lb, 0, la, c, b, a);
     const float X3 = wabc * vabc + wacb * vacb + wbac * vbac + wbca * vbca + wcab * vcab + wcba * vcba;
     const float Y3 = vabc + vbca + vcab;
     const float Z3 = vacb + vbac + vcba;
-    const float denom = eijk - (sev[a] + sev[b] + sev[c]);
+    const float denom = eijk - (ev[0][la] + ev[1][lb] + ev[2][lc]);
     const float e = ((Y3 - 2.0f * Z3) * (wabc + wbca + wcab) + (Z3 - 2.0f * Y3) * (wacb + wbac + wcba) + 3.0f * X3) *
                     fac / denom;
-    neumaier(s, cc, (double)e);
+    s += (double)e;
   }
-  const double tot = block_sum(s + cc);
-  if (threadIdx.x == 0) partial[(int64_t)t * nv + a] = tot;
+  const double tot = block_sum(s);
+  if (threadIdx.x == 0) partial[(int64_t)t * ntri + r] = tot;
 }
 }  // namespace
+
+int64_t triples_f32_partials(int nv) {
+  const int64_t T = (nv + ET - 1) / ET;
+  return T * (T + 1) * (T + 2) / 6;
+}
 
 // ------------------------------------------------------------------------------------
 // Pair-symmetric particle ladder.  Pairs p <= q are numbered q(q+1)/2 + p, strict pairs
@@ -810,11 +844,20 @@ void unpack_ladder(Ctx& c, int no, int nv, double alpha, const double* S, const 
 void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, const double* t1,
                         const double* Voovv, const double* eps, double* d_partial) {
   UCC_REQUIRE(ntuple <= 65535, UCC_BAD_ARGS, "triples_energy: too many tuples per batch");
-  dim3 grid((unsigned)nv, (unsigned)ntuple);
-  triples_energy_f32_kernel<<<grid, 256, sizeof(float) * 4 * nv, c.stream>>>(no, nv, d_tuples, W3, t1, Voovv, eps,
-                                                                             d_partial);
+  const int T = (nv + ET - 1) / ET;
+  UCC_REQUIRE(T <= 1024, UCC_BAD_ARGS, "triples_energy: too many virtual tiles");
+  std::vector<int> tri;
+  for (int A = 0; A < T; A++)
+    for (int B = 0; B <= A; B++)
+      for (int C = 0; C <= B; C++) tri.push_back(A | (B << 10) | (C << 20));
+  Scratch dtri(c, sizeof(int) * tri.size());
+  UCC_CUDA(cudaMemcpyAsync(dtri.p, tri.data(), sizeof(int) * tri.size(), cudaMemcpyHostToDevice, c.stream));
+  dim3 grid((unsigned)tri.size(), (unsigned)ntuple);
+  triples_energy_f32_tiled_kernel<<<grid, 128, 0, c.stream>>>(no, nv, d_tuples, static_cast<const int*>(dtri.p),
+                                                             (int)tri.size(), W3, t1, Voovv, eps, d_partial);
   count_launch();
   check_launch("triples_energy_f32");
+  UCC_CUDA(cudaStreamSynchronize(c.stream));  // the tile list is freed on return
 }
 
 void triples_energy(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const double* W3, const double* t1,

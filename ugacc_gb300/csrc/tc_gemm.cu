@@ -695,12 +695,14 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 // row maxima |x| of a rows x cols FP64 view as bit patterns (non-negative doubles order
-// like their bits, so the maximum is an integer one); a block covers 32 rows and all of K,
-// with lanes along k (sk == 1) or along the rows (transposed views)
-__global__ void slice_absmax_kernel(int64_t rows, int64_t cols, const double* __restrict__ x, int64_t sr, int64_t sk,
-                                    unsigned long long* amax) {
+// like their bits, so the maximum is an integer one); block (x, y) covers 32 rows and the
+// K range [x kchunk, (x+1) kchunk), lanes along k (sk == 1) or along the rows (transposed
+// views), and merges into amax (zeroed by the caller) with one atomicMax per row
+__global__ void slice_absmax_kernel(int64_t rows, int64_t cols, int64_t kchunk, const double* __restrict__ x,
+                                    int64_t sr, int64_t sk, unsigned long long* amax) {
   __shared__ unsigned long long t[8][32];
-  const int64_t r0 = (int64_t)blockIdx.x * 32;
+  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * kchunk;
+  const int64_t k1 = min(cols, k0 + kchunk);
   const int tx = threadIdx.x, ty = threadIdx.y;
   const unsigned long long absmask = 0x7FFFFFFFFFFFFFFFull;
   if (sk == 1) {
@@ -708,22 +710,22 @@ __global__ void slice_absmax_kernel(int64_t rows, int64_t cols, const double* __
       const int64_t r = r0 + i;
       unsigned long long mm = 0;
       if (r < rows)
-        for (int64_t k = tx; k < cols; k += 32)
+        for (int64_t k = k0 + tx; k < k1; k += 32)
           mm = max(mm, (unsigned long long)__double_as_longlong(x[r * sr + k]) & absmask);
       for (int o = 16; o > 0; o >>= 1) mm = max(mm, __shfl_xor_sync(0xffffffffu, mm, o));
-      if (tx == 0 && r < rows) amax[r] = mm;
+      if (tx == 0 && r < rows && mm) atomicMax(amax + r, mm);
     }
   } else {
     const int64_t r = r0 + tx;
     unsigned long long mm = 0;
     if (r < rows)
-      for (int64_t k = ty; k < cols; k += 8)
+      for (int64_t k = k0 + ty; k < k1; k += 8)
         mm = max(mm, (unsigned long long)__double_as_longlong(x[r * sr + k * sk]) & absmask);
     t[ty][tx] = mm;
     __syncthreads();
     if (ty == 0 && r < rows) {
       for (int i = 1; i < 8; i++) mm = max(mm, t[i][tx]);
-      amax[r] = mm;
+      if (mm) atomicMax(amax + r, mm);
     }
   }
 }
@@ -974,10 +976,15 @@ static Sliced* slice_prepare(Ctx& c, const double* x, int64_t rows, int64_t cols
     s->e = reinterpret_cast<int*>(static_cast<char*>(s->tmp->p) + ((sizeof(__nv_bfloat16) * nel + 15) / 16) * 16);
   }
   Scratch amax(c, sizeof(unsigned long long) * rows);
+  UCC_CUDA(cudaMemsetAsync(amax.p, 0, sizeof(unsigned long long) * rows, c.stream));
+  // K chunks of >= 1024 elements, enough blocks to cover the SMs a few times
+  const int64_t rblocks = (rows + 31) / 32;
+  const int64_t want = std::max<int64_t>(1, (int64_t)k.sms * 8 / rblocks);
+  const int64_t kchunk = std::max<int64_t>(1024, (cols + want - 1) / want);
   UCC_CUDA(cudaMemsetAsync(k.range, 0, sizeof(int), c.stream));
   const dim3 blk(32, 8);
-  slice_absmax_kernel<<<(unsigned)((rows + 31) / 32), blk, 0, c.stream>>>(
-      rows, cols, x, sr, sk, static_cast<unsigned long long*>(amax.p));
+  slice_absmax_kernel<<<dim3((unsigned)((cols + kchunk - 1) / kchunk), (unsigned)rblocks), blk, 0, c.stream>>>(
+      rows, cols, kchunk, x, sr, sk, static_cast<unsigned long long*>(amax.p));
   count_kernel_launch();
   slice_digits_kernel<<<dim3((unsigned)(s->kp / 32), (unsigned)(s->rows_p / 32)), blk, 0, c.stream>>>(
       rows, cols, s->rows_p, s->kp, x, sr, sk, static_cast<const unsigned long long*>(amax.p), S, s->d, s->e,
@@ -1001,7 +1008,7 @@ static Sliced* slice_prepare(Ctx& c, const double* x, int64_t rows, int64_t cols
 
 // slices per operand of the sliced FP64 GEMM (56 bits) and the smallest GEMM it takes
 constexpr int kSlices = 8;
-constexpr double kSlicedMinWork = 2e8;
+constexpr double kSlicedMinWork = 3e7;
 
 bool sliced_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                      const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi,
@@ -1048,15 +1055,18 @@ bool sliced_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, cons
   p.kchunk = p.kblocks;
   const int tiles = p.mtiles * p.ntiles;
   std::unique_ptr<Scratch> part;
-  // split K when the tiles fill the SMs poorly: the split (up to 8, chunks of >= 8 K blocks)
-  // with the fewest idle SM slots in the last wave; fixed-order FP64 reduce
+  // split K when the tiles fill the SMs poorly: the split z (chunks of >= 8 K blocks, FP64
+  // partials of at most 2 GB) with the shortest time in waves, ceil(tiles z / SMs) / z,
+  // a larger z only for a 5 % gain; fixed-order FP64 reduce
   int ks = 1;
   {
-    double best = 1.0 - (double)tiles / ((double)((tiles + k.sms - 1) / k.sms) * k.sms);
-    for (int z = 2; z <= 8 && p.kblocks / z >= 8 && tiles < 2 * k.sms && 8.0 * M * N * z <= 2e9; z++) {
-      const double waste = 1.0 - (double)(tiles * z) / ((double)((tiles * z + k.sms - 1) / k.sms) * k.sms);
-      if (waste < best - 0.05) {
-        best = waste;
+    const int zmax = (int)std::min<int64_t>(std::min<int64_t>(p.kblocks / 8, 256),
+                                            std::max<int64_t>(1, 8LL * k.sms / tiles));
+    double best = (double)((tiles + k.sms - 1) / k.sms);
+    for (int z = 2; z <= zmax && 8.0 * M * N * z <= 2e9; z++) {
+      const double t = (double)((tiles * z + k.sms - 1) / k.sms) / z;
+      if (t < 0.95 * best) {
+        best = t;
         ks = z;
       }
     }
@@ -1200,7 +1210,10 @@ void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, con
 // form; false when the problem is too small for it or outside its exponent range
 bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                  const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn) {
-  if (!tc_eligible(M, N, K) || (double)M * N * K < kSlicedMinWork) return false;
+  if (K < 16 || (double)M * N * K < kSlicedMinWork || M > INT32_MAX || N > INT32_MAX) return false;
+  // the output must fill at least 1/16 of its 128 x (N rounded to 32) tiles
+  const int64_t lo = std::min(M, N), hi = std::max(M, N);
+  if (16.0 * (double)lo * hi < (double)((hi + 127) / 128 * 128) * (double)((lo + 31) / 32 * 32)) return false;
   GemmEpilogue epi;
   epi.msplit = 0;
   if (M <= 256 && N > M) {  // the short side becomes the (narrow) N tile

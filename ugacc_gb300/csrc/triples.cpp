@@ -94,9 +94,11 @@ double run_triples(Ctx& c) {
   Scratch dtup(c, sizeof(int) * tuples.size());
   UCC_CUDA(cudaMemcpyAsync(dtup.p, tuples.data(), sizeof(int) * tuples.size(), cudaMemcpyHostToDevice, c.stream));
   Scratch W3(c, sizeof(double) * nv3 * batch);
-  Scratch partial(c, sizeof(double) * (size_t)ntup * nv);
-
   const bool mixed = c.opt.precision == UCC_MIXED && !c.force_fp64 && mixed_triples_prepare(c, batch);
+  // per-tuple partial sums: one per virtual index a (FP64 kernel) or per virtual tile triple (FP32)
+  const int64_t pstride = mixed ? triples_f32_partials(nv) : nv;
+  Scratch partial(c, sizeof(double) * (size_t)ntup * pstride);
+
   // FP64 path: concatenated operands A_x and B_yz
   Tensor Acat, Bcat;
   if (!mixed) triples_operands_fp64(c, Acat, Bcat);
@@ -110,13 +112,13 @@ double run_triples(Ctx& c) {
       triples_w3_fp64(c, Acat, Bcat, tuples.data() + 3 * t0, nb, W3.d(), dp);
     if (mixed)
       triples_energy_f32(c, no, nv, nb, static_cast<int*>(dtup.p) + 3 * t0, static_cast<const float*>(W3.p), t1.p,
-                         c.get("Voovv").p, c.get("eps").p, partial.d() + (int64_t)t0 * nv);
+                         c.get("Voovv").p, c.get("eps").p, partial.d() + (int64_t)t0 * pstride);
     else
       triples_energy(c, no, nv, nb, static_cast<int*>(dtup.p) + 3 * t0, W3.d(), t1.p, c.get("Voovv").p,
                      c.get("eps").p, partial.d() + (int64_t)t0 * nv);
   }
   Scratch et(c, sizeof(double));
-  dot_async(c, (int64_t)ntup * nv, partial.d(), nullptr, et.d());
+  dot_async(c, (int64_t)ntup * pstride, partial.d(), nullptr, et.d());
   double e = 0.0;
   UCC_CUDA(cudaMemcpyAsync(&e, et.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
   UCC_CUDA(cudaStreamSynchronize(c.stream));
