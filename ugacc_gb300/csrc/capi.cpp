@@ -325,7 +325,7 @@ ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t
     else if (precision == UCC_MIXED_FINE)
       tc_gemm_run(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi, 3, 16);
     else if (precision == UCC_FP64_SLICED)
-      UCC_REQUIRE(sliced_gemm_run(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi, 8),
+      UCC_REQUIRE(sliced_gemm_run(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi, 9),
                   UCC_BAD_ARGS, "ucc_gemm: operands outside the sliced form's range (row maxima >= 2^498 or |alpha| "
                                 "outside [2^-20, 2^20])");
     else

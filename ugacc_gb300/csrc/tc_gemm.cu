@@ -46,6 +46,7 @@ constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s per wait
 
 struct Params {
   int M, N, kblocks, mtiles, ntiles;
+  int bn;  // N tile: the MMA's N and the B box rows (a multiple of 32 up to 256)
   double alpha, beta;
   double* C;
   GemmEpilogue epi;
@@ -225,8 +226,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
         const int pb = tile / tiles_per, tl = tile - pb * tiles_per;
         const int mt = tl % p.mtiles, nt = tl / p.mtiles;
-        const int ar0 = (p.nprob ? p.a_row0[pb] : 0) + mt * BM, br0 = (p.nprob ? p.b_row0[pb] : 0) + nt * BN;
-        const int ar1 = p.nterms > 1 ? p.a_row1[pb] + mt * BM : 0, br1 = p.nterms > 1 ? p.b_row1[pb] + nt * BN : 0;
+        const int ar0 = (p.nprob ? p.a_row0[pb] : 0) + mt * BM, br0 = (p.nprob ? p.b_row0[pb] : 0) + nt * p.bn;
+        const int ar1 = p.nterms > 1 ? p.a_row1[pb] + mt * BM : 0, br1 = p.nterms > 1 ? p.b_row1[pb] + nt * p.bn : 0;
         for (int ch = 0; ch < nch && ok; ch++) {
           int k0 = 0, kn = p.kblocks;
           if (p.ksplit > 1) {
@@ -248,7 +249,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const CUtensorMap* ma = term == 0 ? (pa == 0 ? &mAhi : (pa == 1 && p.nparts == 3) ? &mAmid : &mAlo)
                                               : (pa == 0 ? &mA2hi : &mA2lo);
             const CUtensorMap* mb = pbp == 0 ? &mBhi : (pbp == 1 && p.nparts == 3) ? &mBmid : &mBlo;
-            mbar_expect_tx(&full[stage], A_BYTES + B_BYTES);
+            mbar_expect_tx(&full[stage], (uint32_t)(A_BYTES + p.bn * BK * 2));
             tma_load(sA + stage * A_BYTES, ma, &full[stage], kk, term == 0 ? ar0 : ar1);
             tma_load(sB + stage * B_BYTES, mb, &full[stage], kk, term == 0 ? br0 : br1);
             ++issued;
@@ -269,6 +270,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       int stage = 0, acc = 0;
       uint32_t phase = 0, aphase = 0;
       bool ok = true;
+      const uint32_t idesc =
+          (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(p.bn >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
       for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
         for (int ch = 0; ch < nch && ok; ch++) {
           int kn = p.kblocks;
@@ -291,7 +294,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const uint64_t ad = sdesc(sA + stage * A_BYTES), bd = sdesc(sB + stage * B_BYTES);
 #pragma unroll
             for (int k = 0; k < BK / 16; k++)  // +32 bytes along K per 16-element step
-              mma(d, ad + (uint64_t)(k * 2), bd + (uint64_t)(k * 2), (kb | k) != 0);
+              mma_i(d, ad + (uint64_t)(k * 2), bd + (uint64_t)(k * 2), idesc, (kb | k) != 0);
             mma_commit(&empty[stage]);
             if (++stage == STAGES) {
               stage = 0;
@@ -326,11 +329,11 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int64_t mo = ep.msplit ? (m / ep.msplit) * ep.s_mhi + (m % ep.msplit) * ep.s_mlo : m * ep.s_mhi;
       // later K chunks of a tile add onto the earlier ones
       const double alpha = p.alpha, beta = kch == 0 ? p.beta : 1.0;
-      for (int ch = 0; ch < BN / 32; ch++) {
+      for (int ch = 0; ch < p.bn / 32; ch++) {
         uint32_t r[32];
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + ch * 32), r);
         if (m < p.M) {
-          const int64_t n0 = (int64_t)nt * BN + ch * 32;
+          const int64_t n0 = (int64_t)nt * p.bn + ch * 32;
           // with beta != 0 all 32 old values are loaded before the first store, so the
           // loads are in flight together instead of each waiting behind a store that
           // might alias it
@@ -383,22 +386,24 @@ __global__ void __launch_bounds__(THREADS, 1)
 
 // ------------------------------------------------------------------------------------
 // FP64 GEMM from exact BF16 slices (the error-free splitting of Ozaki, Ogita, Oishi and
-// Rump, Numer. Algorithms 59 (2012) 95-118, with base-2^7 digits).
+// Rump, Numer. Algorithms 59 (2012) 95-118, with base-2^SB digits, SB = 6).
 //
 // Every operand row r is scaled by 2^-e_r (e_r = ilogb(max_k |x_rk|) + 2, so the scaled
-// row lies in (-1/2, 1/2)) and written as S balanced base-128 digits,
-//   x_rk = 2^e_r sum_{s<S} d_s(r,k) 2^-7(s+1),  |d_s| <= 64,
-// stored pre-scaled as bf16 slices d_s 2^-7(s+1) (exact: integers of 7 bits times a power
-// of two).  A product of an A slice s and a B slice t is an integer times 2^-7(s+t+2),
-// below 2^12 in magnitude, so any sum of up to 4096 such products with the same s+t is
-// exact in the FP32 tensor-memory accumulator.  The kernel therefore accumulates, per
-// output tile, "units": for each order g = s+t < gex, every pair (s, g-s) over a K range
-// of at most 4096 / (g+1) elements (exact), and one tail unit with all pairs of order
-// gex..S-1 over the whole K range (FP32, its terms are ~2^-7gex smaller than the leading
-// ones).  The epilogue adds each unit into the FP64 output as
+// row lies in (-1/2, 1/2)) and written as S balanced base-2^SB digits,
+//   x_rk = 2^e_r sum_{s<S} d_s(r,k) 2^-SB(s+1),  |d_s| <= 2^(SB-1) = 32,
+// stored pre-scaled as bf16 slices d_s 2^-SB(s+1) (exact: small integers times a power of
+// two).  A product of an A slice s and a B slice t is an integer times 2^-SB(s+t+2), at most
+// 2^10 in magnitude, so any sum of up to 2^14 such products with the same s+t is exact in
+// the FP32 tensor-memory accumulator.  The kernel therefore accumulates, per output tile,
+// "units": for each order g = s+t < gex, every pair (s, g-s) over a K range of at most
+// 2^14 / (g+1) elements (exact), and one tail unit with all pairs of order gex..S-1 over the
+// whole K range (FP32, its terms are ~2^-SB gex smaller than the leading ones).  The
+// epilogue adds each unit into the FP64 output as
 //   C[m][n] += alpha 2^(e_m + e_n) acc,
 // the first unit of a tile applying beta.  Pairs with s+t >= S are dropped (truncation
-// ~2^-7S relative to max|A_m.| max|B_.n|).
+// ~2^-SB S relative to max|A_m.| max|B_.n|).  Fewer, wider digits (SB = 7) would need 20 %
+// fewer products but 4x more units, and the global read-modify-write of every unit's
+// epilogue is what limits this kernel.
 // ------------------------------------------------------------------------------------
 struct SParams {
   int M, N, kblocks, mtiles, ntiles;
@@ -418,8 +423,11 @@ struct SUnit {
   int g0, g1, kb0, kb1;  // orders [g0, g1], K blocks [kb0, kb1)
 };
 
-// K blocks per exact unit of order g: (g+1) pairs x kc blocks x 64 <= 4096 products
-__device__ __forceinline__ int sunit_kc(int g) { return max(1, 64 / (g + 1)); }
+constexpr int SB = 6;                                           // bits per digit
+constexpr int SEXACT_KB = (1 << (24 - 2 * (SB - 1))) / BK;     // K blocks of one pair per exact unit
+
+// K blocks per exact unit of order g: (g+1) pairs x kc blocks x 64 <= 2^(24 - 2(SB-1)) products
+__device__ __forceinline__ int sunit_kc(int g) { return max(1, SEXACT_KB / (g + 1)); }
 
 __device__ __forceinline__ int sunit_count(int S, int gex, int kn) {
   int u = gex < S ? 1 : 0;
@@ -760,8 +768,8 @@ __device__ __forceinline__ long long slice_fixed(double x, int e, int bits) {
   return (b >> 63) ? -v : v;
 }
 
-// digits: slices[s][r][k] = bf16(d_s 2^-7(s+1)) for r < rows_p (zero past rows), k < kp
-// (zero past cols), the balanced base-128 digits of x 2^(7S-e) (least significant s = S-1);
+// digits: slices[s][r][k] = bf16(d_s 2^-SB(s+1)) for r < rows_p (zero past rows), k < kp
+// (zero past cols), the balanced base-2^SB digits of x 2^(SB S - e) (least significant s = S-1);
 // e[r] written by the blocks of the first K tile.  32 x 32 tiles through shared memory:
 // reads coalesced along whichever stride is 1, writes along k.
 __global__ void slice_digits_kernel(int64_t rows, int64_t cols, int64_t rows_p, int64_t kp, const double* __restrict__ x,
@@ -785,17 +793,18 @@ __global__ void slice_digits_kernel(int64_t rows, int64_t cols, int64_t rows_p, 
     if (r >= rows_p || k >= kp) continue;
     const int e = r < rows ? slice_exponent(amax[r], range) : 0;
     if (k == 0 && r < rows) e_out[r] = e;
-    long long X = r < rows ? slice_fixed(t[i][tx], e, 7 * S) : 0;
+    long long X = r < rows ? slice_fixed(t[i][tx], e, SB * S) : 0;
     __nv_bfloat16* dst = slices + (size_t)r * kp + k;
     for (int s = S - 1; s >= 0; s--) {
       long long d;
       if (s > 0) {
-        d = ((X + 64) & 127) - 64;  // balanced digit in [-64, 63]
-        X = (X - d) >> 7;
+        constexpr long long H = 1ll << (SB - 1);
+        d = ((X + H) & (2 * H - 1)) - H;  // balanced digit in [-H, H)
+        X = (X - d) >> SB;
       } else {
-        d = X;  // what remains: |d| <= 64
+        d = X;  // what remains: |d| <= H
       }
-      dst[(size_t)s * plane] = __float2bfloat16_rn((float)d * __int_as_float((127 - 7 * (s + 1)) << 23));
+      dst[(size_t)s * plane] = __float2bfloat16_rn((float)d * __int_as_float((127 - SB * (s + 1)) << 23));
     }
   }
 }
@@ -947,9 +956,9 @@ static Split* prepare(Ctx& c, const double* x, int64_t rows, int64_t cols, int64
 // FP64 operand; the slice arrays are padded to whole tiles of box_rows rows so that no tile
 // reaches into the next slice.  nullptr when the slices do not fit in free memory.
 static Sliced* slice_prepare(Ctx& c, const double* x, int64_t rows, int64_t cols, int64_t sr, int64_t sk, int box_rows,
-                             int S, std::unique_ptr<Sliced>& temp) {
+                             int S, std::unique_ptr<Sliced>& temp, bool allow_cache) {
   Cache& k = cache(c);
-  bool constant = c.is_constant(x);
+  bool constant = allow_cache && c.is_constant(x);
   Key key{x, rows, cols, sr, sk, box_rows, S};
   if (constant) {
     auto it = k.sliced.find(key);
@@ -1006,28 +1015,75 @@ static Sliced* slice_prepare(Ctx& c, const double* x, int64_t rows, int64_t cols
 
 }  // namespace tc
 
-// slices per operand of the sliced FP64 GEMM (56 bits) and the smallest GEMM it takes
-constexpr int kSlices = 8;
+// slices per operand of the sliced FP64 GEMM (9 x 6 = 54 bits) and the smallest GEMM it takes
+constexpr int kSlices = 9;
 constexpr double kSlicedMinWork = 3e7;
+
+static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
+                             int64_t sAk, const double* B, int64_t sBk, int64_t sBn, double beta, double* C,
+                             const GemmEpilogue& epi, int S, bool allow_cache, bool& wrote);
 
 bool sliced_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                      const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi,
                      int S) {
+  bool wrote = false;
+  const bool ok = sliced_gemm_part(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, S, true, wrote);
+  // a false return lets the caller redo the whole product in FP64, so no chunk may have been
+  // written by then
+  UCC_REQUIRE(ok || !wrote, UCC_BAD_ARGS, "sliced GEMM: operand outside the sliced range after partial output");
+  return ok;
+}
+
+// one sliced product, or the longer of M and N in halves when the slices exceed one launch's
+// limits or the free memory (chunks are sliced as temporaries)
+static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
+                             int64_t sAk, const double* B, int64_t sBk, int64_t sBn, double beta, double* C,
+                             const GemmEpilogue& epi, int S, bool allow_cache, bool& wrote) {
   using namespace tc;
-  UCC_REQUIRE(S >= 2 && S <= 8, UCC_BAD_ARGS, "sliced GEMM: 2 to 8 slices");
+  UCC_REQUIRE(S >= 2 && SB * S <= 56, UCC_BAD_ARGS, "sliced GEMM: 2 to 9 slices");
   const double aa = std::fabs(alpha);
   if (!(aa >= 0x1p-20 && aa <= 0x1p20) || M > INT32_MAX || N > INT32_MAX) return false;
   // N tile: a short N is padded to a multiple of 32 only
   const int bn = N >= BN ? BN : (int)((N + 31) / 32 * 32);
-  if ((double)S * (double)((M + BM - 1) / BM * BM) >= 2e9 || (double)S * (double)((N + bn - 1) / bn * bn) >= 2e9)
-    return false;
-  if ((N + bn - 1) / bn * bn / 32 > 65535 || (M + BM - 1) / BM * BM / 32 > 65535) return false;  // slicing grid.y
   Cache& k = cache(c);
+  {
+    const int64_t Mp = (M + BM - 1) / BM * BM, Np = (N + bn - 1) / bn * bn, kp = (K + BK - 1) / BK * BK;
+    auto cached = [&](const double* x, int64_t rows, int64_t sr, int64_t sk, int box) {
+      return allow_cache && k.sliced.count(Key{x, rows, K, sr, sk, box, S}) != 0;
+    };
+    const double needA = cached(A, M, sAm, sAk, BM) ? 0.0 : 2.0 * S * (double)Mp * kp;
+    const double needB = cached(B, N, sBn, sBk, bn) ? 0.0 : 2.0 * S * (double)Np * kp;
+    size_t free_b = 0, total_b = 0;
+    UCC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const bool too_big = (double)S * Mp >= 2e9 || (double)S * Np >= 2e9 || Np / 32 > 65535 || Mp / 32 > 65535 ||
+                         needA + needB > (double)free_b - 4e9;
+    if (too_big) {
+      if (needB >= needA && N > bn) {
+        const int64_t n1 = ((N + 1) / 2 + bn - 1) / bn * bn;
+        GemmEpilogue e2 = epi;
+        return sliced_gemm_part(c, M, n1, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, S, false, wrote) &&
+               sliced_gemm_part(c, M, N - n1, K, alpha, A, sAm, sAk, B + n1 * sBn, sBk, sBn, beta, C + n1 * epi.s_n,
+                                e2, S, false, wrote);
+      }
+      const int64_t unit = epi.msplit ? (int64_t)BM * epi.msplit : BM;  // row chunks keep the row split whole
+      if (M > unit) {
+        const int64_t m1 = ((M + 1) / 2 + unit - 1) / unit * unit;
+        if (m1 < M) {
+          const int64_t off = epi.msplit ? (m1 / epi.msplit) * epi.s_mhi : m1 * epi.s_mhi;
+          return sliced_gemm_part(c, m1, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, S, false, wrote) &&
+                 sliced_gemm_part(c, M - m1, N, K, alpha, A + m1 * sAm, sAm, sAk, B, sBk, sBn, beta, C + off, epi, S,
+                                  false, wrote);
+        }
+      }
+      return false;
+    }
+  }
   UCC_CUDA(cudaEventRecord(k.ev0, c.stream));  // the time includes the slicing of non-cached operands
   std::unique_ptr<Sliced> ta, tb;
-  Sliced* a = slice_prepare(c, A, M, K, sAm, sAk, BM, S, ta);
-  Sliced* b = a ? slice_prepare(c, B, N, K, sBn, sBk, bn, S, tb) : nullptr;
+  Sliced* a = slice_prepare(c, A, M, K, sAm, sAk, BM, S, ta, allow_cache);
+  Sliced* b = a ? slice_prepare(c, B, N, K, sBn, sBk, bn, S, tb, allow_cache) : nullptr;
   if (!a || !b || !a->range_ok || !b->range_ok) return false;
+  wrote = true;
   if (!k.sattr_set) {
     UCC_CUDA(cudaFuncSetAttribute(sliced_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)SLICED_SMEM_BYTES));
@@ -1112,8 +1168,9 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
   UCC_REQUIRE(parts == 2 || parts == 3, UCC_BAD_ARGS, "tensor-core GEMM: 2 or 3 split parts");
   Cache& k = cache(c);
   std::unique_ptr<Split> ta, tb;
+  const int bn = N >= BN ? BN : (int)((N + 31) / 32 * 32);  // a short N is padded to a multiple of 32 only
   Split* a = prepare(c, A, M, K, sAm, sAk, BM, ta, parts);
-  Split* b = prepare(c, B, N, K, sBn, sBk, BN, tb, parts);
+  Split* b = prepare(c, B, N, K, sBn, sBk, bn, tb, parts);
   if (!k.attr_set) {
     UCC_CUDA(cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     k.attr_set = true;
@@ -1123,7 +1180,8 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
   p.N = (int)N;
   p.kblocks = (int)(a->kp / BK);
   p.mtiles = (int)((M + BM - 1) / BM);
-  p.ntiles = (int)((N + BN - 1) / BN);
+  p.bn = bn;
+  p.ntiles = (int)((N + bn - 1) / bn);
   p.alpha = alpha;
   p.beta = beta;
   p.C = C;
@@ -1135,11 +1193,23 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
   p.ksplit = 1;
   p.kchunk = p.kblocks;
   const int tiles = p.mtiles * p.ntiles;
-  // too few output tiles for the SMs and a long K: split K, FP64 partials, fixed-order reduce
+  // tiles that fill the SMs poorly and a long K: split K (chunks of >= 4 K blocks, FP64
+  // partials of at most 2 GB) for the shortest time in waves, ceil(tiles z / SMs) / z, a
+  // larger z only for a 5 % gain; fixed-order reduce
   std::unique_ptr<Scratch> part;
   p.kc = kc > 0 && kc < p.kblocks ? kc : 0;
-  if (p.kc == 0 && tiles * 2 <= k.sms && p.kblocks >= 8) {
-    int ks = std::min(k.sms / tiles, p.kblocks / 4);
+  if (p.kc == 0 && p.kblocks >= 8) {
+    int ks = 1;
+    const int zmax = (int)std::min<int64_t>(std::min<int64_t>(p.kblocks / 4, 256),
+                                            std::max<int64_t>(1, 8LL * k.sms / tiles));
+    double best = (double)((tiles + k.sms - 1) / k.sms);
+    for (int z = 2; z <= zmax && 8.0 * M * N * z <= 2e9; z++) {
+      const double t = (double)((tiles * z + k.sms - 1) / k.sms) / z;
+      if (t < 0.95 * best) {
+        best = t;
+        ks = z;
+      }
+    }
     if (ks > 1) {
       p.kchunk = (p.kblocks + ks - 1) / ks;
       p.ksplit = (p.kblocks + p.kchunk - 1) / p.kchunk;
@@ -1194,8 +1264,9 @@ void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, con
                       int64_t sCn, int parts, int kc) {
   GemmEpilogue epi;
   epi.msplit = 0;
-  if (M < 128 && N > M) {
-    // short M: compute C^T = B^T A^T so that the long side fills the 128-row MMA tile
+  if (M <= 256 && N > M) {
+    // short M: compute C^T = B^T A^T so that the long side fills the 128-row MMA tile and
+    // the short one a narrow N tile
     epi.s_mhi = sCn;
     epi.s_n = sCm;
     tc_gemm_run(c, N, M, K, alpha, B, sBn, sBk, A, sAk, sAm, beta, C, epi, parts, kc);
@@ -1268,6 +1339,7 @@ __global__ void split_into_kernel(int64_t rows, int64_t cols, const double* src,
 
 struct Triples {
   Split A, A2, B;  // A2: A with its (a,b) row pairs in (b,a) order
+  int bn = BN;     // N tile: the virtual index c, padded to a multiple of 32
   int* d_arow = nullptr;
   int* d_brow = nullptr;
   int64_t* d_coff = nullptr;
@@ -1326,8 +1398,9 @@ bool mixed_triples_prepare(Ctx& c, int max_batch) {
   make_map(&T->A.mlo, T->A.lo, T->A.rows, kp, BM);
   make_map(&T->A2.mhi, T->A2.hi, T->A2.rows, kp, BM);
   make_map(&T->A2.mlo, T->A2.lo, T->A2.rows, kp, BM);
-  make_map(&T->B.mhi, T->B.hi, T->B.rows, kp, BN);
-  make_map(&T->B.mlo, T->B.lo, T->B.rows, kp, BN);
+  T->bn = nv >= BN ? BN : (int)((nv + 31) / 32 * 32);
+  make_map(&T->B.mhi, T->B.hi, T->B.rows, kp, T->bn);
+  make_map(&T->B.mlo, T->B.lo, T->B.rows, kp, T->bn);
   UCC_CUDA(cudaMalloc(&T->d_arow, sizeof(int) * 2 * max_batch));
   UCC_CUDA(cudaMalloc(&T->d_brow, sizeof(int) * 2 * max_batch));
   UCC_CUDA(cudaMalloc(&T->d_coff, sizeof(int64_t) * max_batch));
@@ -1377,7 +1450,8 @@ bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, float* W3) {
     p.N = (int)nv;
     p.kblocks = (int)(T.A.kp / BK);
     p.mtiles = (int)((nv2 + BM - 1) / BM);
-    p.ntiles = (int)((nv + BN - 1) / BN);
+    p.bn = T.bn;
+    p.ntiles = (int)((nv + T.bn - 1) / T.bn);
     p.alpha = 1.0;
     p.beta = pq == 0 ? 0.0 : 1.0;
     p.C = nullptr;

@@ -61,7 +61,7 @@ def main(argv=None):
                           "tflops": 2.0 * M * N * K / (ms * 1e-3) / 1e12 if ms else None, "max_rel_err": err}))
         return 0
     h = make_hamiltonian(a.no, a.nv, a.seed)
-    H = U.Hamiltonian.from_synthetic(h)
+    H = U.Hamiltonian.from_synthetic(h, precision=a.precision.upper() if a.precision != "sliced" else None)
     prec = a.precision.upper()
     if a.iters > 0:
         cc = U.CCWfn(H, {"MAXITER": a.iters, "R_CONVERGENCE": 1e-10, "PRECISION": prec, "PRINT": int(a.print),
