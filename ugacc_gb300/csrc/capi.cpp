@@ -31,6 +31,7 @@ Ctx::~Ctx() {
     cudaEventDestroy(t.b);
   }
   for (auto e : event_pool) cudaEventDestroy(e);
+  anchors.clear();  // pool buffers are freed on the stream
   tc_cache.reset();
   perts.clear();
   store.clear();

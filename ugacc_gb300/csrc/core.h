@@ -63,6 +63,21 @@ struct Error : std::runtime_error {
     if (!(cond)) throw ::ucc::Error(status, msg); \
   } while (0)
 
+// FP64 buffer from the stream-ordered pool, freed in stream order (no device
+// synchronisation): per-sweep state such as the refinement anchors.
+struct PoolBuffer {
+  double* p = nullptr;
+  cudaStream_t stream = nullptr;
+  PoolBuffer(cudaStream_t s, size_t count) : stream(s) {
+    if (count) UCC_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p), count * sizeof(double), s));
+  }
+  ~PoolBuffer() {
+    if (p) cudaFreeAsync(p, stream);
+  }
+  PoolBuffer(const PoolBuffer&) = delete;
+  PoolBuffer& operator=(const PoolBuffer&) = delete;
+};
+
 // Owned device buffer (cudaMalloc; freed on destruction).
 struct DeviceBuffer {
   double* p = nullptr;
@@ -147,7 +162,7 @@ struct Ctx {
   struct AnchorTerm {
     int64_t M = 0, N = 0, K = 0;
     bool a_const = false, b_const = false;
-    std::unique_ptr<DeviceBuffer> a0, b0, p0;  // dense [M][K], [K][N], [M][N]
+    std::unique_ptr<PoolBuffer> a0, b0, p0;  // dense [M][K], [K][N], [M][N]
   };
   struct Anchors {
     int mode = 0;  // 0 off, 1 record, 2 delta

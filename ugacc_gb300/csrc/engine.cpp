@@ -236,14 +236,14 @@ void anchored_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const 
     t.a_const = a_const;
     t.b_const = b_const;
     if (!a_const) {
-      t.a0 = std::make_unique<DeviceBuffer>((size_t)(M * K));
+      t.a0 = std::make_unique<PoolBuffer>(c.stream, (size_t)(M * K));
       permute_add(c, av, 1.0, 0.0, make_view(t.a0->p, {M, K}));
     }
     if (!b_const) {
-      t.b0 = std::make_unique<DeviceBuffer>((size_t)(K * N));
+      t.b0 = std::make_unique<PoolBuffer>(c.stream, (size_t)(K * N));
       permute_add(c, bv, 1.0, 0.0, make_view(t.b0->p, {K, N}));
     }
-    t.p0 = std::make_unique<DeviceBuffer>((size_t)(M * N));
+    t.p0 = std::make_unique<PoolBuffer>(c.stream, (size_t)(M * N));
     if (!sliced_gemm(c, M, N, K, 1.0, A, sAm, sAk, B, sBk, sBn, 0.0, t.p0->p, N, 1)) {
       GemmEpilogue epi;
       epi.s_mhi = N;

@@ -811,21 +811,45 @@ __global__ void slice_digits_kernel(int64_t rows, int64_t cols, int64_t rows_p, 
 
 // FP64 rows x cols view (strides sr, sk) -> bf16 hi/lo [rows][kp], zero padded to kp
 // (mid != null: three parts, x = hi + mid + lo, each the bf16 rounding of what remains)
-__global__ void split_kernel(int64_t rows, int64_t cols, int64_t kp, const double* x, int64_t sr, int64_t sk,
-                             __nv_bfloat16* hi, __nv_bfloat16* lo, __nv_bfloat16* mid) {
-  const int64_t n = rows * kp;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = i / kp, k = i - r * kp;
-    const double v = k < cols ? x[r * sr + k * sk] : 0.0;
-    const __nv_bfloat16 h = __double2bfloat16(v);
-    hi[i] = h;
-    double rest = v - (double)__bfloat162float(h);
+// 32 x 32 tiles through shared memory: reads coalesced along whichever stride is 1 (sk == 1:
+// along k, otherwise along the rows), writes along k.  Two parts are formed in FP32 (x
+// rounded to FP32 first: 2^-24, far below the lo part's 2^-17), three parts in FP64.
+__global__ void split_kernel(int64_t rows, int64_t cols, int64_t kp, const double* __restrict__ x, int64_t sr,
+                             int64_t sk, __nv_bfloat16* hi, __nv_bfloat16* lo, __nv_bfloat16* mid) {
+  __shared__ double t[32][33];
+  const int64_t k0 = (int64_t)blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int64_t r0 = (int64_t)blockIdx.y * 32; r0 < rows; r0 += (int64_t)gridDim.y * 32) {  // row tiles
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int64_t r = sk == 1 ? r0 + i : r0 + tx, k = sk == 1 ? k0 + tx : k0 + i;
+    const double v = (r < rows && k < cols) ? x[r * sr + k * sk] : 0.0;
+    if (sk == 1)
+      t[i][tx] = v;
+    else
+      t[tx][i] = v;
+  }
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int64_t r = r0 + i, k = k0 + tx;
+    if (r >= rows || k >= kp) continue;
+    const int64_t o = r * kp + k;
+    const double v = t[i][tx];
     if (mid) {
+      const __nv_bfloat16 h = __double2bfloat16(v);
+      double rest = v - (double)__bfloat162float(h);
       const __nv_bfloat16 m = __double2bfloat16(rest);
-      mid[i] = m;
       rest -= (double)__bfloat162float(m);
+      hi[o] = h;
+      mid[o] = m;
+      lo[o] = __double2bfloat16(rest);
+    } else {
+      const float f = (float)v;
+      const __nv_bfloat16 h = __float2bfloat16_rn(f);
+      hi[o] = h;
+      lo[o] = __float2bfloat16_rn(f - __bfloat162float(h));
     }
-    lo[i] = __double2bfloat16(rest);
+  }
   }
 }
 
@@ -836,9 +860,11 @@ struct Split {
   __nv_bfloat16* hi = nullptr;
   __nv_bfloat16* lo = nullptr;
   __nv_bfloat16* mid = nullptr;  // three-part splits only
+  std::unique_ptr<Scratch> tmp;  // storage of a temporary (non-constant) operand
   int64_t rows = 0, kp = 0;
   CUtensorMap mhi, mlo, mmid;
   ~Split() {
+    if (tmp) return;
     if (hi) cudaFree(hi);
     if (lo) cudaFree(lo);
     if (mid) cudaFree(mid);
@@ -933,12 +959,19 @@ static Split* prepare(Ctx& c, const double* x, int64_t rows, int64_t cols, int64
   auto s = std::make_unique<Split>();
   s->rows = rows;
   s->kp = (cols + BK - 1) / BK * BK;
-  UCC_CUDA(cudaMalloc(&s->hi, sizeof(__nv_bfloat16) * rows * s->kp));
-  UCC_CUDA(cudaMalloc(&s->lo, sizeof(__nv_bfloat16) * rows * s->kp));
-  if (parts == 3) UCC_CUDA(cudaMalloc(&s->mid, sizeof(__nv_bfloat16) * rows * s->kp));
-  const int64_t n = rows * s->kp;
-  const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)k.sms * 16);
-  split_kernel<<<blocks, 256, 0, c.stream>>>(rows, cols, s->kp, x, sr, sk, s->hi, s->lo, s->mid);
+  const size_t plane = sizeof(__nv_bfloat16) * rows * s->kp;  // a multiple of 128 bytes
+  if (constant) {
+    UCC_CUDA(cudaMalloc(&s->hi, plane));
+    UCC_CUDA(cudaMalloc(&s->lo, plane));
+    if (parts == 3) UCC_CUDA(cudaMalloc(&s->mid, plane));
+  } else {  // stream-ordered pool: no device synchronisation per temporary
+    s->tmp = std::make_unique<Scratch>(c, plane * (parts == 3 ? 3 : 2));
+    s->hi = static_cast<__nv_bfloat16*>(s->tmp->p);
+    s->lo = reinterpret_cast<__nv_bfloat16*>(static_cast<char*>(s->tmp->p) + plane);
+    if (parts == 3) s->mid = reinterpret_cast<__nv_bfloat16*>(static_cast<char*>(s->tmp->p) + 2 * plane);
+  }
+  split_kernel<<<dim3((unsigned)(s->kp / 32), (unsigned)std::min<int64_t>((rows + 31) / 32, 65535)), dim3(32, 8), 0,
+                 c.stream>>>(rows, cols, s->kp, x, sr, sk, s->hi, s->lo, s->mid);
   count_kernel_launch();
   UCC_CUDA(cudaGetLastError());
   make_map(&s->mhi, s->hi, rows, s->kp, box_rows);
