@@ -512,6 +512,9 @@ void contract(Ctx& c, const std::string& spec, double alpha, const Tensor& A, co
     epi.msplit = 0;
     epi.s_mhi = sCm;
     epi.s_n = sCn;
+    // PRINT >= 3 in the MIXED form: the FP64 (DFMA) GEMMs that remain, with their shapes
+    if (c.opt.print >= 3 && c.opt.precision == UCC_MIXED && 2.0 * M * N * K >= 1e9)
+      std::printf("\tFP64 GEMM %s  M=%lld N=%lld K=%lld\n", spec.c_str(), (long long)M, (long long)N, (long long)K);
     dgemm_strided(c, M, N, K, ga, a.p, sAm, sAk, b.p, sBk, sBn, gb, ct.p, epi, 1, 0, 0, 0, nullptr);
   }
   if (!cdirect) {
