@@ -1099,7 +1099,7 @@ static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alp
                                 e2, S, false, wrote);
       }
       const int64_t unit = epi.msplit ? (int64_t)BM * epi.msplit : BM;  // row chunks keep the row split whole
-      if (M > unit) {
+      if (M > unit && needA >= needB) {
         const int64_t m1 = ((M + 1) / 2 + unit - 1) / unit * unit;
         if (m1 < M) {
           const int64_t off = epi.msplit ? (m1 / epi.msplit) * epi.s_mhi : m1 * epi.s_mhi;
@@ -1107,6 +1107,14 @@ static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alp
                  sliced_gemm_part(c, M - m1, N, K, alpha, A + m1 * sAm, sAm, sAk, B, sBk, sBn, beta, C + off, epi, S,
                                   false, wrote);
         }
+      }
+      // both operands short and K long (or little memory left): K in halves, the second
+      // accumulating onto the first
+      if (K >= 2 * 4096) {
+        const int64_t k1 = ((K + 1) / 2 + BK - 1) / BK * BK;
+        return sliced_gemm_part(c, M, N, k1, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, S, false, wrote) &&
+               sliced_gemm_part(c, M, N, K - k1, alpha, A + k1 * sAk, sAm, sAk, B + k1 * sBk, sBk, sBn, 1.0, C, epi, S,
+                                false, wrote);
       }
       return false;
     }
