@@ -261,6 +261,11 @@ void dgemm(Ctx& c, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alp
            int64_t sA = 0, int64_t sB = 0, int64_t sC = 0, const GemmPtrs* ptrs = nullptr);
 
 // Same with arbitrary operand strides: op(A)[m][k] = A[m*sAm + k*sAk], op(B)[k][n] = B[k*sBk + n*sBn].
+// FP64 GEMM for a small output (M, N <= 256, M N <= 4096) and a long K (>= 8192): K chunks
+// per block and a fixed-order reduce.  False when the shape does not qualify.
+bool dgemm_small_output(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
+                        int64_t sAk, const double* B, int64_t sBk, int64_t sBn, double beta, double* C,
+                        const GemmEpilogue& epi);
 void dgemm_strided(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                    const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi,
                    int batch, int64_t bA, int64_t bB, int64_t bC, const GemmPtrs* ptrs);

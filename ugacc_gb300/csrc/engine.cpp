@@ -244,7 +244,12 @@ void anchored_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const 
       permute_add(c, bv, 1.0, 0.0, make_view(t.b0->p, {K, N}));
     }
     t.p0 = std::make_unique<PoolBuffer>(c.stream, (size_t)(M * N));
-    if (!sliced_gemm(c, M, N, K, 1.0, A, sAm, sAk, B, sBk, sBn, 0.0, t.p0->p, N, 1)) {
+    const double t0 = c.stats.sliced_gemm_ms;
+    const bool sliced = sliced_gemm(c, M, N, K, 1.0, A, sAm, sAk, B, sBk, sBn, 0.0, t.p0->p, N, 1);
+    if (sliced && c.opt.print >= 3)
+      std::printf("\tsliced GEMM (anchor)  M=%lld N=%lld K=%lld  %.3f ms\n", (long long)M, (long long)N, (long long)K,
+                  c.stats.sliced_gemm_ms - t0);
+    if (!sliced) {
       GemmEpilogue epi;
       epi.s_mhi = N;
       epi.s_n = 1;
@@ -503,10 +508,22 @@ void contract(Ctx& c, const std::string& spec, double alpha, const Tensor& A, co
   }
   if (!done && c.opt.precision == UCC_MIXED && !c.force_fp64)
     done = mixed_gemm(c, M, N, K, ga, a.p, sAm, sAk, b.p, sBk, sBn, gb, ct.p, sCm, sCn);
+  if (!done) {  // small output, long K: a reduction rather than a GEMM (every precision)
+    GemmEpilogue epi;
+    epi.msplit = 0;
+    epi.s_mhi = sCm;
+    epi.s_n = sCn;
+    done = dgemm_small_output(c, M, N, K, ga, a.p, sAm, sAk, b.p, sBk, sBn, gb, ct.p, epi);
+  }
   // the FP64 work of the MIXED form (refinement sweeps, one-shot builds): sliced operands
   // on the tensor cores, FP64-accurate
-  if (!done && c.opt.precision == UCC_MIXED && !recorder())
+  if (!done && c.opt.precision == UCC_MIXED && !recorder()) {
+    const double t0 = c.stats.sliced_gemm_ms;
     done = sliced_gemm(c, M, N, K, ga, a.p, sAm, sAk, b.p, sBk, sBn, gb, ct.p, sCm, sCn);
+    if (done && c.opt.print >= 3)  // PRINT >= 3: every sliced FP64 GEMM with its shape and time
+      std::printf("\tsliced GEMM %s  M=%lld N=%lld K=%lld  %.3f ms\n", spec.c_str(), (long long)M, (long long)N,
+                  (long long)K, c.stats.sliced_gemm_ms - t0);
+  }
   if (!done) {
     GemmEpilogue epi;
     epi.msplit = 0;

@@ -219,6 +219,79 @@ void splitk_reduce(Ctx& c, int64_t M, int64_t N, int nsplit, const double* P, do
   check_launch("split-K reduce");
 }
 
+// ------------------------------------------------------------------------------------
+// GEMM with a small output (M, N <= 256, M N <= 4096) and a long K (reductions such as
+// sum_nef t_inef L_mnef): block z sums the K chunk [z kc, (z+1) kc) for every output into
+// P[z][m][n]; splitk_reduce adds the chunks in a fixed order.  A 64 x 64 tile would leave
+// most of its multiply-adds idle on such shapes.
+// ------------------------------------------------------------------------------------
+namespace {
+constexpr int SMT = 256, SMK = 16;  // threads, K rows staged per step
+__global__ void __launch_bounds__(SMT) dgemm_smallmn_kernel(int M, int N, int64_t K, int64_t kc,
+                                                           const double* __restrict__ A, int64_t sAm, int64_t sAk,
+                                                           const double* __restrict__ B, int64_t sBk, int64_t sBn,
+                                                           double* P) {
+  extern __shared__ double sm[];
+  double* As = sm;                   // [SMK][M]
+  double* Bs = sm + (size_t)SMK * M;  // [SMK][N]
+  const int MN = M * N, t = threadIdx.x;
+  const int64_t k0 = (int64_t)blockIdx.x * kc, k1 = min(K, k0 + kc);
+  double acc[16];
+#pragma unroll
+  for (int j = 0; j < 16; j++) acc[j] = 0.0;
+  for (int64_t kb = k0; kb < k1; kb += SMK) {
+    const int kn = (int)(k1 - kb < SMK ? k1 - kb : SMK);
+    __syncthreads();
+    for (int e = t; e < SMK * M; e += SMT) {  // A tile, k fastest when A is K-contiguous
+      const int kk = sAk == 1 ? e % SMK : e / M, m = sAk == 1 ? e / SMK : e % M;
+      As[kk * M + m] = kk < kn ? A[(int64_t)m * sAm + (kb + kk) * sAk] : 0.0;
+    }
+    for (int e = t; e < SMK * N; e += SMT) {
+      const int kk = sBk == 1 ? e % SMK : e / N, n = sBk == 1 ? e / SMK : e % N;
+      Bs[kk * N + n] = kk < kn ? B[(kb + kk) * sBk + (int64_t)n * sBn] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const int o = t + j * SMT;
+      if (o < MN) {
+        const int m = o / N, n = o - m * N;
+        double s = acc[j];
+#pragma unroll
+        for (int kk = 0; kk < SMK; kk++) s = fma(As[kk * M + m], Bs[kk * N + n], s);
+        acc[j] = s;
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 16; j++) {
+    const int o = t + j * SMT;
+    if (o < MN) P[(int64_t)blockIdx.x * MN + o] = acc[j];
+  }
+}
+}  // namespace
+
+bool dgemm_small_output(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
+                        int64_t sAk, const double* B, int64_t sBk, int64_t sBn, double beta, double* C,
+                        const GemmEpilogue& epi) {
+  if (recorder() || M > 256 || N > 256 || M * N > 16 * SMT || K < 8192) return false;
+  int64_t nblk = std::min<int64_t>((K + 511) / 512, 4 * 152);
+  const int64_t kc = ((K + nblk - 1) / nblk + SMK - 1) / SMK * SMK;
+  nblk = (K + kc - 1) / kc;
+  Scratch part(c, sizeof(double) * M * N * nblk);
+  cudaEvent_t ev0 = c.take_event(), ev1 = c.take_event();
+  cudaEventRecord(ev0, c.stream);
+  dgemm_smallmn_kernel<<<(unsigned)nblk, SMT, sizeof(double) * SMK * (M + N), c.stream>>>(
+      (int)M, (int)N, K, kc, A, sAm, sAk, B, sBk, sBn, part.d());
+  count_launch();
+  check_launch("dgemm_smallmn");
+  splitk_reduce(c, M, N, (int)nblk, part.d(), alpha, beta, C, epi);
+  cudaEventRecord(ev1, c.stream);
+  c.gemm_timers.push_back({ev0, ev1, 2.0 * (double)M * N * K});
+  if (c.gemm_timers.size() >= 4096) c.resolve_timers();
+  return true;
+}
+
 void dgemm(Ctx& c, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
            const double* B, int64_t ldb, double beta, double* C, const GemmEpilogue& epi, int batch, int64_t sA,
            int64_t sB, int64_t sC, const GemmPtrs* ptrs) {

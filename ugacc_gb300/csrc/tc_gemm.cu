@@ -1322,7 +1322,8 @@ void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, con
 // form; false when the problem is too small for it or outside its exponent range
 bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                  const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn) {
-  if (K < 16 || (double)M * N * K < kSlicedMinWork || M > INT32_MAX || N > INT32_MAX) return false;
+  // a short K (a few occupied indices) leaves too little work per slice and output
+  if (K < 48 || (double)M * N * K < kSlicedMinWork || M > INT32_MAX || N > INT32_MAX) return false;
   // the output must fill at least 1/16 of its 128 x (N rounded to 32) tiles
   const int64_t lo = std::min(M, N), hi = std::max(M, N);
   if (16.0 * (double)lo * hi < (double)((hi + 127) / 128 * 128) * (double)((lo + 31) / 32 * 32)) return false;
