@@ -724,34 +724,39 @@ __global__ void __launch_bounds__(128) triples_energy_f32_tiled_kernel(int no, i
   __shared__ float ev[3][ET];
   const int r = blockIdx.x, t = blockIdx.y;
   const int code = tri[r];
-  const int R0[3] = {(code & 1023) * ET, ((code >> 10) & 1023) * ET, (code >> 20) * ET};
+  const int Ra = (code & 1023) * ET, Rb = ((code >> 10) & 1023) * ET, Rc = (code >> 20) * ET;
+  auto R0 = [&](int role) { return role == 0 ? Ra : (role == 1 ? Rb : Rc); };  // range start of a role
   const int i = tuples[3 * t], j = tuples[3 * t + 1], k = tuples[3 * t + 2];
   const int64_t nv2 = (int64_t)nv * nv;
   const float* W = W3 + (int64_t)t * nv2 * nv;
-  // role order of each permutation tile p: W[x in role P[p][0]][y in P[p][1]][z in P[p][2]]
-  const int P[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  // role order of each permutation tile p, two bits per role: W[x in role 0][y in 1][z in 2]
+  // for (0,1,2), (0,2,1), (1,0,2), (1,2,0), (2,0,1), (2,1,0)
+  constexpr uint64_t kPerm = 0x24ull | (0x18ull << 6) | (0x21ull << 12) | (0x09ull << 18) | (0x12ull << 24) |
+                             (0x06ull << 30);
   for (int e = threadIdx.x; e < 6 * ET * ET * ET; e += blockDim.x) {
     const int p = e / (ET * ET * ET), rem = e - p * (ET * ET * ET);
     const int x = rem / (ET * ET), y = (rem / ET) % ET, z = rem % ET;
-    const int gx = R0[P[p][0]] + x, gy = R0[P[p][1]] + y, gz = R0[P[p][2]] + z;
+    const uint64_t code6 = kPerm >> (6 * p);
+    const int gx = R0((int)(code6 & 3)) + x, gy = R0((int)((code6 >> 2) & 3)) + y, gz = R0((int)((code6 >> 4) & 3)) + z;
     Ws[p][x][y][z] = (gx < nv && gy < nv && gz < nv) ? W[(int64_t)gx * nv2 + (int64_t)gy * nv + gz] : 0.f;
   }
-  const double* Vm[3] = {Voovv + ((int64_t)i * no + j) * nv2, Voovv + ((int64_t)i * no + k) * nv2,
-                         Voovv + ((int64_t)j * no + k) * nv2};
+  auto Vm = [&](int m) {  // Vij, Vik, Vjk
+    return Voovv + ((m == 2 ? (int64_t)j : (int64_t)i) * no + (m == 0 ? j : k)) * nv2;
+  };
   for (int e = threadIdx.x; e < 3 * 6 * ET * ET; e += blockDim.x) {
     const int m = e / (6 * ET * ET), rem = e - m * (6 * ET * ET);
     const int pid = rem / (ET * ET), x = (rem / ET) % ET, y = rem % ET;
     const int u = pid / 2, v0 = pid % 2, v = v0 < u ? v0 : v0 + 1;  // ordered role pair (u, v), u != v
-    const int gx = R0[u] + x, gy = R0[v] + y;
-    Vs[m][pid][x][y] = (gx < nv && gy < nv) ? (float)Vm[m][(int64_t)gx * nv + gy] : 0.f;
+    const int gx = R0(u) + x, gy = R0(v) + y;
+    Vs[m][pid][x][y] = (gx < nv && gy < nv) ? (float)Vm(m)[(int64_t)gx * nv + gy] : 0.f;
   }
   if (threadIdx.x < 3 * 3 * ET) {
     const int m = threadIdx.x / (3 * ET), role = (threadIdx.x / ET) % 3, l = threadIdx.x % ET;
-    const int row = m == 0 ? i : (m == 1 ? j : k), g = R0[role] + l;
+    const int row = m == 0 ? i : (m == 1 ? j : k), g = R0(role) + l;
     s1[m][role][l] = g < nv ? (float)t1[(int64_t)row * nv + g] : 0.f;
   }
   if (threadIdx.x < 3 * ET) {
-    const int role = threadIdx.x / ET, l = threadIdx.x % ET, g = R0[role] + l;
+    const int role = threadIdx.x / ET, l = threadIdx.x % ET, g = R0(role) + l;
     ev[role][l] = g < nv ? (float)eps[no + g] : 0.f;
   }
   __syncthreads();
@@ -768,7 +773,7 @@ __global__ void __launch_bounds__(128) triples_energy_f32_tiled_kernel(int no, i
   double s = 0.0;
   for (int q = threadIdx.x; q < ET * ET * ET; q += blockDim.x) {
     const int la = q / (ET * ET), lb = (q / ET) % ET, lc = q % ET;
-    const int a = R0[0] + la, b = R0[1] + lb, c = R0[2] + lc;
+    const int a = Ra + la, b = Rb + lb, c = Rc + lc;
     if (a >= nv || b > a || c > b) continue;
     const float wabc = Ws[0][la][lb][lc], wacb = Ws[1][la][lc][lb], wbac = Ws[2][lb][la][lc];
     const float wbca = Ws[3][lb][lc][la], wcab = Ws[4][lc][la][lb], wcba = Ws[5][lc][lb][la];
