@@ -63,6 +63,44 @@ struct Error : std::runtime_error {
     if (!(cond)) throw ::ucc::Error(status, msg); \
   } while (0)
 
+// An operand matrix whose row and column indices are index groups of a tensor made of up
+// to two strided runs each: element (r, k) sits at p + off(r) + off(k) with
+// off(r) = rsplit ? (r / rsplit) rs_hi + (r % rsplit) rs_lo : r rs_hi (columns likewise).
+// The tensor-core operand readers take it directly, so such operands need no gather.
+struct MatView {
+  const double* p = nullptr;
+  int64_t rows = 0, cols = 0;
+  int64_t rsplit = 0, rs_hi = 0, rs_lo = 0;
+  int64_t ksplit = 0, ks_hi = 0, ks_lo = 0;
+  static MatView strided(const double* p, int64_t rows, int64_t cols, int64_t sr, int64_t sk) {
+    MatView v;
+    v.p = p;
+    v.rows = rows;
+    v.cols = cols;
+    v.rs_hi = sr;
+    v.ks_hi = sk;
+    return v;
+  }
+  int64_t roff(int64_t r) const { return rsplit ? (r / rsplit) * rs_hi + (r % rsplit) * rs_lo : r * rs_hi; }
+  int64_t koff(int64_t k) const { return ksplit ? (k / ksplit) * ks_hi + (k % ksplit) * ks_lo : k * ks_hi; }
+  // the rows [r0, r0 + n) (columns [k0, k0 + n)) as a view; false when r0 splits a run
+  bool sub_rows(int64_t r0, int64_t n, MatView& out) const {
+    if (rsplit && r0 % rsplit) return false;
+    out = *this;
+    out.p = p + roff(r0);
+    out.rows = n;
+    return true;
+  }
+  bool sub_cols(int64_t k0, int64_t n, MatView& out) const {
+    if (ksplit && k0 % ksplit) return false;
+    out = *this;
+    out.p = p + koff(k0);
+    out.cols = n;
+    return true;
+  }
+  bool k_contiguous() const { return (ksplit ? ks_lo : ks_hi) == 1; }  // unit stride along the columns
+};
+
 // FP64 buffer from the stream-ordered pool, freed in stream order (no device
 // synchronisation): per-sweep state such as the refinement anchors.
 struct PoolBuffer {

@@ -10,6 +10,10 @@ namespace ucc {
 bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn);
 bool tc_eligible(int64_t M, int64_t N, int64_t K);
+bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const MatView& A, const MatView& B, double beta,
+                double* C, int64_t sCm, int64_t sCn);
+bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const MatView& A, const MatView& B,
+                 double beta, double* C, int64_t sCm, int64_t sCn);
 bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                  const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn);
 void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
@@ -334,6 +338,36 @@ int64_t extent(const Tensor& T, const std::string& str, const std::string& grp) 
   return e;
 }
 
+// index group grp of T as at most two strided runs, an outer one (the leading labels) and an
+// inner one: offset(x) = split ? (x / split) s_hi + (x % split) s_lo : x s_hi
+bool fusable2(const Tensor& T, const std::string& str, const std::string& grp, int64_t& split, int64_t& s_hi,
+              int64_t& s_lo) {
+  split = 0;
+  s_lo = 0;
+  if (fusable(T, str, grp, s_hi)) return true;
+  for (size_t cut = 1; cut < grp.size(); cut++) {
+    int64_t so, si;
+    const std::string outer = grp.substr(0, cut), inner = grp.substr(cut);
+    if (fusable(T, str, outer, so) && fusable(T, str, inner, si)) {
+      split = extent(T, str, inner);
+      s_hi = so;
+      s_lo = si;
+      return true;
+    }
+  }
+  return false;
+}
+
+// rows (group rg) x columns (group kg) of T as a two-stride operand view
+bool view2(const Tensor& T, const std::string& str, const std::string& rg, const std::string& kg, MatView& v) {
+  if (!fusable2(T, str, rg, v.rsplit, v.rs_hi, v.rs_lo) || !fusable2(T, str, kg, v.ksplit, v.ks_hi, v.ks_lo))
+    return false;
+  v.p = T.p;
+  v.rows = extent(T, str, rg);
+  v.cols = extent(T, str, kg);
+  return true;
+}
+
 std::string ordered(const std::string& src, const std::string& set) {
   std::string r;
   for (char ch : src)
@@ -457,21 +491,7 @@ void contract(Ctx& c, const std::string& spec, double alpha, const Tensor& A, co
     }
   }
   std::unique_ptr<Scratch> hA, hB, hC;
-  Tensor a = A, b = B;
-  std::string sa = p.a, sb = p.b;
-  int64_t sAm, sAk, sBk, sBn, sCm, sCn;
-  if (!(fusable(a, sa, bm, sAm) && fusable(a, sa, bk, sAk))) {
-    a = gather(c, A, p.a, bm + bk, hA);
-    sa = bm + bk;
-    fusable(a, sa, bm, sAm);
-    fusable(a, sa, bk, sAk);
-  }
-  if (!(fusable(b, sb, bk, sBk) && fusable(b, sb, bn, sBn))) {
-    b = gather(c, B, p.b, bk + bn, hB);
-    sb = bk + bn;
-    fusable(b, sb, bk, sBk);
-    fusable(b, sb, bn, sBn);
-  }
+  int64_t sCm, sCn;
   const bool cdirect = fusable(C, p.c, bm, sCm) && fusable(C, p.c, bn, sCn);
   Tensor ct = C;
   if (!cdirect) {
@@ -484,24 +504,58 @@ void contract(Ctx& c, const std::string& spec, double alpha, const Tensor& A, co
     sCm = N;
     sCn = 1;
   }
-  // empty groups: any stride works
-  if (sAm == 0) sAm = 1;
-  if (sAk == 0) sAk = 1;
-  if (sBk == 0) sBk = 1;
-  if (sBn == 0) sBn = 1;
-  if (sCm == 0) sCm = 1;
+  if (sCm == 0) sCm = 1;  // empty groups: any stride works
   if (sCn == 0) sCn = 1;
   const double ga = cdirect ? alpha : 1.0, gb = cdirect ? beta : 0.0;
   bool done = false;
-  if (M == 1) {  // row vector times matrix
+  const bool mixed = c.opt.precision == UCC_MIXED;
+  const bool anchored = c.anchors.mode != 0 && mixed && (double)M * N * K >= kAnchorMinWork && tc_eligible(M, N, K);
+  const bool small_out = M <= 256 && N <= 256 && M * N <= 4096 && K >= 8192;
+  // the tensor-core paths read operands whose index groups are two strided runs directly:
+  // no gather
+  if (M > 1 && N > 1 && mixed && !recorder() && !anchored && !small_out) {
+    MatView av, bv;
+    if (view2(A, p.a, bm, bk, av) && view2(B, p.b, bn, bk, bv)) {
+      if (!c.force_fp64) done = mixed_gemm(c, M, N, K, ga, av, bv, gb, ct.p, sCm, sCn);
+      if (!done) {
+        const double t0 = c.stats.sliced_gemm_ms;
+        done = sliced_gemm(c, M, N, K, ga, av, bv, gb, ct.p, sCm, sCn);
+        if (done && c.opt.print >= 3)  // PRINT >= 3: every sliced FP64 GEMM with its shape and time
+          std::printf("\tsliced GEMM %s  M=%lld N=%lld K=%lld  %.3f ms\n", spec.c_str(), (long long)M, (long long)N,
+                      (long long)K, c.stats.sliced_gemm_ms - t0);
+      }
+    }
+  }
+  Tensor a = A, b = B;
+  int64_t sAm = 1, sAk = 1, sBk = 1, sBn = 1;
+  if (!done) {  // single-stride operands for the other paths: gather where needed
+    std::string sa = p.a, sb = p.b;
+    if (!(fusable(a, sa, bm, sAm) && fusable(a, sa, bk, sAk))) {
+      a = gather(c, A, p.a, bm + bk, hA);
+      sa = bm + bk;
+      fusable(a, sa, bm, sAm);
+      fusable(a, sa, bk, sAk);
+    }
+    if (!(fusable(b, sb, bk, sBk) && fusable(b, sb, bn, sBn))) {
+      b = gather(c, B, p.b, bk + bn, hB);
+      sb = bk + bn;
+      fusable(b, sb, bk, sBk);
+      fusable(b, sb, bn, sBn);
+    }
+    // empty groups: any stride works
+    if (sAm == 0) sAm = 1;
+    if (sAk == 0) sAk = 1;
+    if (sBk == 0) sBk = 1;
+    if (sBn == 0) sBn = 1;
+  }
+  if (!done && M == 1) {  // row vector times matrix
     dgemv_strided(c, N, K, ga, a.p, sAk, b.p, sBk, sBn, gb, ct.p, sCn);
     done = true;
-  } else if (N == 1) {  // matrix times column vector
+  } else if (!done && N == 1) {  // matrix times column vector
     dgemv_strided(c, M, K, ga, b.p, sBk, a.p, sAk, sAm, gb, ct.p, sCm);
     done = true;
   }
-  if (!done && c.anchors.mode != 0 && c.opt.precision == UCC_MIXED && (double)M * N * K >= kAnchorMinWork &&
-      tc_eligible(M, N, K)) {
+  if (!done && anchored) {
     anchored_gemm(c, M, N, K, ga, a.p, sAm, sAk, c.is_constant(A.p), b.p, sBk, sBn, c.is_constant(B.p), gb, ct.p,
                   sCm, sCn);
     done = true;

@@ -702,24 +702,39 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
+// element (r, k) of a two-stride operand view (r, k and the splits below 2^32: 32-bit division)
+__device__ __forceinline__ const double& mv_at(const MatView& v, int64_t r, int64_t k) {
+  int64_t ro = r * v.rs_hi, ko = k * v.ks_hi;
+  if (v.rsplit) {
+    const uint32_t q = (uint32_t)r / (uint32_t)v.rsplit;
+    ro = (int64_t)q * v.rs_hi + ((int64_t)r - (int64_t)q * v.rsplit) * v.rs_lo;
+  }
+  if (v.ksplit) {
+    const uint32_t q = (uint32_t)k / (uint32_t)v.ksplit;
+    ko = (int64_t)q * v.ks_hi + ((int64_t)k - (int64_t)q * v.ksplit) * v.ks_lo;
+  }
+  return v.p[ro + ko];
+}
+__device__ __forceinline__ bool mv_kcontig(const MatView& v) { return (v.ksplit ? v.ks_lo : v.ks_hi) == 1; }
+
 // row maxima |x| of a rows x cols FP64 view as bit patterns (non-negative doubles order
 // like their bits, so the maximum is an integer one); block (x, y) covers 32 rows and the
 // K range [x kchunk, (x+1) kchunk), lanes along k (sk == 1) or along the rows (transposed
 // views), and merges into amax (zeroed by the caller) with one atomicMax per row
-__global__ void slice_absmax_kernel(int64_t rows, int64_t cols, int64_t kchunk, const double* __restrict__ x,
-                                    int64_t sr, int64_t sk, unsigned long long* amax) {
+__global__ void slice_absmax_kernel(MatView x, int64_t kchunk, unsigned long long* amax) {
   __shared__ unsigned long long t[8][32];
+  const int64_t rows = x.rows, cols = x.cols;
   const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * kchunk;
   const int64_t k1 = min(cols, k0 + kchunk);
   const int tx = threadIdx.x, ty = threadIdx.y;
   const unsigned long long absmask = 0x7FFFFFFFFFFFFFFFull;
-  if (sk == 1) {
+  if (mv_kcontig(x)) {
     for (int i = ty; i < 32; i += 8) {
       const int64_t r = r0 + i;
       unsigned long long mm = 0;
       if (r < rows)
         for (int64_t k = k0 + tx; k < k1; k += 32)
-          mm = max(mm, (unsigned long long)__double_as_longlong(x[r * sr + k]) & absmask);
+          mm = max(mm, (unsigned long long)__double_as_longlong(mv_at(x, r, k)) & absmask);
       for (int o = 16; o > 0; o >>= 1) mm = max(mm, __shfl_xor_sync(0xffffffffu, mm, o));
       if (tx == 0 && r < rows && mm) atomicMax(amax + r, mm);
     }
@@ -728,7 +743,7 @@ __global__ void slice_absmax_kernel(int64_t rows, int64_t cols, int64_t kchunk, 
     unsigned long long mm = 0;
     if (r < rows)
       for (int64_t k = k0 + ty; k < k1; k += 8)
-        mm = max(mm, (unsigned long long)__double_as_longlong(x[r * sr + k * sk]) & absmask);
+        mm = max(mm, (unsigned long long)__double_as_longlong(mv_at(x, r, k)) & absmask);
     t[ty][tx] = mm;
     __syncthreads();
     if (ty == 0 && r < rows) {
@@ -772,16 +787,17 @@ __device__ __forceinline__ long long slice_fixed(double x, int e, int bits) {
 // (zero past cols), the balanced base-2^SB digits of x 2^(SB S - e) (least significant s = S-1);
 // e[r] written by the blocks of the first K tile.  32 x 32 tiles through shared memory:
 // reads coalesced along whichever stride is 1, writes along k.
-__global__ void slice_digits_kernel(int64_t rows, int64_t cols, int64_t rows_p, int64_t kp, const double* __restrict__ x,
-                                    int64_t sr, int64_t sk, const unsigned long long* __restrict__ amax, int S,
-                                    __nv_bfloat16* slices, int* e_out, int* range) {
+__global__ void slice_digits_kernel(MatView x, int64_t rows_p, int64_t kp, const unsigned long long* __restrict__ amax,
+                                    int S, __nv_bfloat16* slices, int* e_out, int* range) {
   __shared__ double t[32][33];
+  const int64_t rows = x.rows, cols = x.cols;
   const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
+  const bool kc = mv_kcontig(x);
   for (int i = ty; i < 32; i += 8) {
-    const int64_t r = sk == 1 ? r0 + i : r0 + tx, k = sk == 1 ? k0 + tx : k0 + i;
-    const double v = (r < rows && k < cols) ? x[r * sr + k * sk] : 0.0;
-    if (sk == 1)
+    const int64_t r = kc ? r0 + i : r0 + tx, k = kc ? k0 + tx : k0 + i;
+    const double v = (r < rows && k < cols) ? mv_at(x, r, k) : 0.0;
+    if (kc)
       t[i][tx] = v;
     else
       t[tx][i] = v;
@@ -814,17 +830,18 @@ __global__ void slice_digits_kernel(int64_t rows, int64_t cols, int64_t rows_p, 
 // 32 x 32 tiles through shared memory: reads coalesced along whichever stride is 1 (sk == 1:
 // along k, otherwise along the rows), writes along k.  Two parts are formed in FP32 (x
 // rounded to FP32 first: 2^-24, far below the lo part's 2^-17), three parts in FP64.
-__global__ void split_kernel(int64_t rows, int64_t cols, int64_t kp, const double* __restrict__ x, int64_t sr,
-                             int64_t sk, __nv_bfloat16* hi, __nv_bfloat16* lo, __nv_bfloat16* mid) {
+__global__ void split_kernel(MatView x, int64_t kp, __nv_bfloat16* hi, __nv_bfloat16* lo, __nv_bfloat16* mid) {
   __shared__ double t[32][33];
+  const int64_t rows = x.rows, cols = x.cols;
   const int64_t k0 = (int64_t)blockIdx.x * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
+  const bool kc = mv_kcontig(x);
   for (int64_t r0 = (int64_t)blockIdx.y * 32; r0 < rows; r0 += (int64_t)gridDim.y * 32) {  // row tiles
   __syncthreads();
   for (int i = ty; i < 32; i += 8) {
-    const int64_t r = sk == 1 ? r0 + i : r0 + tx, k = sk == 1 ? k0 + tx : k0 + i;
-    const double v = (r < rows && k < cols) ? x[r * sr + k * sk] : 0.0;
-    if (sk == 1)
+    const int64_t r = kc ? r0 + i : r0 + tx, k = kc ? k0 + tx : k0 + i;
+    const double v = (r < rows && k < cols) ? mv_at(x, r, k) : 0.0;
+    if (kc)
       t[i][tx] = v;
     else
       t[tx][i] = v;
@@ -888,7 +905,11 @@ struct Sliced {
   }
 };
 
-using Key = std::tuple<const double*, int64_t, int64_t, int64_t, int64_t, int, int>;
+// an operand of the caches: the view (pointer, shape, strides), the box rows and the parts
+using Key = std::tuple<const double*, int64_t, int64_t, int64_t, int64_t, int64_t, int64_t, int64_t, int64_t, int, int>;
+static Key make_key(const MatView& v, int box_rows, int parts) {
+  return Key{v.p, v.rows, v.cols, v.rsplit, v.rs_hi, v.rs_lo, v.ksplit, v.ks_hi, v.ks_lo, box_rows, parts};
+}
 struct Triples;
 struct Cache {
   std::map<Key, std::unique_ptr<Split>> ops;
@@ -947,11 +968,12 @@ static Cache& cache(Ctx& c) {
 }
 
 // split (and cache when the source is a constant block) a rows x cols FP64 operand
-static Split* prepare(Ctx& c, const double* x, int64_t rows, int64_t cols, int64_t sr, int64_t sk, int box_rows,
-                      std::unique_ptr<Split>& temp, int parts = 2) {
+static Split* prepare(Ctx& c, const MatView& x, int box_rows, std::unique_ptr<Split>& temp, int parts = 2) {
   Cache& k = cache(c);
-  const bool constant = c.is_constant(x);
-  Key key{x, rows, cols, sr, sk, box_rows, parts};
+  const bool constant = c.is_constant(x.p);
+  const int64_t rows = x.rows, cols = x.cols;
+  UCC_REQUIRE(rows < INT32_MAX && cols < INT32_MAX, UCC_BAD_ARGS, "tensor-core GEMM: operand too large");
+  const Key key = make_key(x, box_rows, parts);
   if (constant) {
     auto it = k.ops.find(key);
     if (it != k.ops.end()) return it->second.get();
@@ -971,7 +993,7 @@ static Split* prepare(Ctx& c, const double* x, int64_t rows, int64_t cols, int64
     if (parts == 3) s->mid = reinterpret_cast<__nv_bfloat16*>(static_cast<char*>(s->tmp->p) + 2 * plane);
   }
   split_kernel<<<dim3((unsigned)(s->kp / 32), (unsigned)std::min<int64_t>((rows + 31) / 32, 65535)), dim3(32, 8), 0,
-                 c.stream>>>(rows, cols, s->kp, x, sr, sk, s->hi, s->lo, s->mid);
+                 c.stream>>>(x, s->kp, s->hi, s->lo, s->mid);
   count_kernel_launch();
   UCC_CUDA(cudaGetLastError());
   make_map(&s->mhi, s->hi, rows, s->kp, box_rows);
@@ -988,11 +1010,13 @@ static Split* prepare(Ctx& c, const double* x, int64_t rows, int64_t cols, int64
 // slice (and cache when the source is a constant block and memory allows) a rows x cols
 // FP64 operand; the slice arrays are padded to whole tiles of box_rows rows so that no tile
 // reaches into the next slice.  nullptr when the slices do not fit in free memory.
-static Sliced* slice_prepare(Ctx& c, const double* x, int64_t rows, int64_t cols, int64_t sr, int64_t sk, int box_rows,
-                             int S, std::unique_ptr<Sliced>& temp, bool allow_cache) {
+static Sliced* slice_prepare(Ctx& c, const MatView& x, int box_rows, int S, std::unique_ptr<Sliced>& temp,
+                             bool allow_cache) {
   Cache& k = cache(c);
-  bool constant = allow_cache && c.is_constant(x);
-  Key key{x, rows, cols, sr, sk, box_rows, S};
+  bool constant = allow_cache && c.is_constant(x.p);
+  const int64_t rows = x.rows, cols = x.cols;
+  UCC_REQUIRE(rows < INT32_MAX && cols < INT32_MAX, UCC_BAD_ARGS, "sliced GEMM: operand too large");
+  const Key key = make_key(x, box_rows, S);
   if (constant) {
     auto it = k.sliced.find(key);
     if (it != k.sliced.end()) return it->second.get();
@@ -1026,11 +1050,10 @@ static Sliced* slice_prepare(Ctx& c, const double* x, int64_t rows, int64_t cols
   UCC_CUDA(cudaMemsetAsync(k.range, 0, sizeof(int), c.stream));
   const dim3 blk(32, 8);
   slice_absmax_kernel<<<dim3((unsigned)((cols + kchunk - 1) / kchunk), (unsigned)rblocks), blk, 0, c.stream>>>(
-      rows, cols, kchunk, x, sr, sk, static_cast<unsigned long long*>(amax.p));
+      x, kchunk, static_cast<unsigned long long*>(amax.p));
   count_kernel_launch();
   slice_digits_kernel<<<dim3((unsigned)(s->kp / 32), (unsigned)(s->rows_p / 32)), blk, 0, c.stream>>>(
-      rows, cols, s->rows_p, s->kp, x, sr, sk, static_cast<const unsigned long long*>(amax.p), S, s->d, s->e,
-      k.range);
+      x, s->rows_p, s->kp, static_cast<const unsigned long long*>(amax.p), S, s->d, s->e, k.range);
   count_kernel_launch();
   UCC_CUDA(cudaGetLastError());
   int hrange = 0;
@@ -1052,26 +1075,34 @@ static Sliced* slice_prepare(Ctx& c, const double* x, int64_t rows, int64_t cols
 constexpr int kSlices = 9;
 constexpr double kSlicedMinWork = 3e7;
 
-static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
-                             int64_t sAk, const double* B, int64_t sBk, int64_t sBn, double beta, double* C,
-                             const GemmEpilogue& epi, int S, bool allow_cache, bool& wrote);
+static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const MatView& A,
+                             const MatView& B, double beta, double* C, const GemmEpilogue& epi, int S, bool allow_cache,
+                             bool& wrote);
 
-bool sliced_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
-                     const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi,
-                     int S) {
+// A: M x K, B: N x K (rows = the output's columns)
+bool sliced_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const MatView& A, const MatView& B,
+                     double beta, double* C, const GemmEpilogue& epi, int S) {
   bool wrote = false;
-  const bool ok = sliced_gemm_part(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, S, true, wrote);
+  const bool ok = sliced_gemm_part(c, M, N, K, alpha, A, B, beta, C, epi, S, true, wrote);
   // a false return lets the caller redo the whole product in FP64, so no chunk may have been
   // written by then
   UCC_REQUIRE(ok || !wrote, UCC_BAD_ARGS, "sliced GEMM: operand outside the sliced range after partial output");
   return ok;
 }
 
-// one sliced product, or the longer of M and N in halves when the slices exceed one launch's
-// limits or the free memory (chunks are sliced as temporaries)
-static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
-                             int64_t sAk, const double* B, int64_t sBk, int64_t sBn, double beta, double* C,
-                             const GemmEpilogue& epi, int S, bool allow_cache, bool& wrote) {
+bool sliced_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                     const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi,
+                     int S) {
+  return sliced_gemm_run(c, M, N, K, alpha, MatView::strided(A, M, K, sAm, sAk), MatView::strided(B, N, K, sBn, sBk),
+                         beta, C, epi, S);
+}
+
+// one sliced product, or the longer of M and N (else K) in halves when the slices exceed one
+// launch's limits or the free memory (chunks are sliced as temporaries; a chunk boundary must
+// not split a two-stride run)
+static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const MatView& A,
+                             const MatView& B, double beta, double* C, const GemmEpilogue& epi, int S, bool allow_cache,
+                             bool& wrote) {
   using namespace tc;
   UCC_REQUIRE(S >= 2 && SB * S <= 56, UCC_BAD_ARGS, "sliced GEMM: 2 to 9 slices");
   const double aa = std::fabs(alpha);
@@ -1081,48 +1112,46 @@ static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alp
   Cache& k = cache(c);
   {
     const int64_t Mp = (M + BM - 1) / BM * BM, Np = (N + bn - 1) / bn * bn, kp = (K + BK - 1) / BK * BK;
-    auto cached = [&](const double* x, int64_t rows, int64_t sr, int64_t sk, int box) {
-      return allow_cache && k.sliced.count(Key{x, rows, K, sr, sk, box, S}) != 0;
-    };
-    const double needA = cached(A, M, sAm, sAk, BM) ? 0.0 : 2.0 * S * (double)Mp * kp;
-    const double needB = cached(B, N, sBn, sBk, bn) ? 0.0 : 2.0 * S * (double)Np * kp;
+    auto cached = [&](const MatView& x, int box) { return allow_cache && k.sliced.count(make_key(x, box, S)) != 0; };
+    const double needA = cached(A, BM) ? 0.0 : 2.0 * S * (double)Mp * kp;
+    const double needB = cached(B, bn) ? 0.0 : 2.0 * S * (double)Np * kp;
     size_t free_b = 0, total_b = 0;
     UCC_CUDA(cudaMemGetInfo(&free_b, &total_b));
     const bool too_big = (double)S * Mp >= 2e9 || (double)S * Np >= 2e9 || Np / 32 > 65535 || Mp / 32 > 65535 ||
                          needA + needB > (double)free_b - 4e9;
     if (too_big) {
+      MatView x1, x2, y1, y2;
       if (needB >= needA && N > bn) {
         const int64_t n1 = ((N + 1) / 2 + bn - 1) / bn * bn;
-        GemmEpilogue e2 = epi;
-        return sliced_gemm_part(c, M, n1, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, S, false, wrote) &&
-               sliced_gemm_part(c, M, N - n1, K, alpha, A, sAm, sAk, B + n1 * sBn, sBk, sBn, beta, C + n1 * epi.s_n,
-                                e2, S, false, wrote);
+        if (B.sub_rows(0, n1, x1) && B.sub_rows(n1, N - n1, x2))
+          return sliced_gemm_part(c, M, n1, K, alpha, A, x1, beta, C, epi, S, false, wrote) &&
+                 sliced_gemm_part(c, M, N - n1, K, alpha, A, x2, beta, C + n1 * epi.s_n, epi, S, false, wrote);
       }
       const int64_t unit = epi.msplit ? (int64_t)BM * epi.msplit : BM;  // row chunks keep the row split whole
       if (M > unit && needA >= needB) {
         const int64_t m1 = ((M + 1) / 2 + unit - 1) / unit * unit;
-        if (m1 < M) {
+        if (m1 < M && A.sub_rows(0, m1, x1) && A.sub_rows(m1, M - m1, x2)) {
           const int64_t off = epi.msplit ? (m1 / epi.msplit) * epi.s_mhi : m1 * epi.s_mhi;
-          return sliced_gemm_part(c, m1, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, S, false, wrote) &&
-                 sliced_gemm_part(c, M - m1, N, K, alpha, A + m1 * sAm, sAm, sAk, B, sBk, sBn, beta, C + off, epi, S,
-                                  false, wrote);
+          return sliced_gemm_part(c, m1, N, K, alpha, x1, B, beta, C, epi, S, false, wrote) &&
+                 sliced_gemm_part(c, M - m1, N, K, alpha, x2, B, beta, C + off, epi, S, false, wrote);
         }
       }
       // both operands short and K long (or little memory left): K in halves, the second
       // accumulating onto the first
       if (K >= 2 * 4096) {
         const int64_t k1 = ((K + 1) / 2 + BK - 1) / BK * BK;
-        return sliced_gemm_part(c, M, N, k1, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, S, false, wrote) &&
-               sliced_gemm_part(c, M, N, K - k1, alpha, A + k1 * sAk, sAm, sAk, B + k1 * sBk, sBk, sBn, 1.0, C, epi, S,
-                                false, wrote);
+        if (A.sub_cols(0, k1, x1) && A.sub_cols(k1, K - k1, x2) && B.sub_cols(0, k1, y1) &&
+            B.sub_cols(k1, K - k1, y2))
+          return sliced_gemm_part(c, M, N, k1, alpha, x1, y1, beta, C, epi, S, false, wrote) &&
+                 sliced_gemm_part(c, M, N, K - k1, alpha, x2, y2, 1.0, C, epi, S, false, wrote);
       }
       return false;
     }
   }
   UCC_CUDA(cudaEventRecord(k.ev0, c.stream));  // the time includes the slicing of non-cached operands
   std::unique_ptr<Sliced> ta, tb;
-  Sliced* a = slice_prepare(c, A, M, K, sAm, sAk, BM, S, ta, allow_cache);
-  Sliced* b = a ? slice_prepare(c, B, N, K, sBn, sBk, bn, S, tb, allow_cache) : nullptr;
+  Sliced* a = slice_prepare(c, A, BM, S, ta, allow_cache);
+  Sliced* b = a ? slice_prepare(c, B, bn, S, tb, allow_cache) : nullptr;
   if (!a || !b || !a->range_ok || !b->range_ok) return false;
   wrote = true;
   if (!k.sattr_set) {
@@ -1202,16 +1231,16 @@ static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alp
   return true;
 }
 
-void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
-                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi, int parts,
-                 int kc) {
+// A: M x K, B: N x K (rows = the output's columns)
+void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const MatView& A, const MatView& B,
+                 double beta, double* C, const GemmEpilogue& epi, int parts, int kc) {
   using namespace tc;
   UCC_REQUIRE(parts == 2 || parts == 3, UCC_BAD_ARGS, "tensor-core GEMM: 2 or 3 split parts");
   Cache& k = cache(c);
   std::unique_ptr<Split> ta, tb;
   const int bn = N >= BN ? BN : (int)((N + 31) / 32 * 32);  // a short N is padded to a multiple of 32 only
-  Split* a = prepare(c, A, M, K, sAm, sAk, BM, ta, parts);
-  Split* b = prepare(c, B, N, K, sBn, sBk, bn, tb, parts);
+  Split* a = prepare(c, A, BM, ta, parts);
+  Split* b = prepare(c, B, bn, tb, parts);
   if (!k.attr_set) {
     UCC_CUDA(cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     k.attr_set = true;
@@ -1290,6 +1319,13 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
 }
 
 void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi, int parts,
+                 int kc) {
+  tc_gemm_run(c, M, N, K, alpha, MatView::strided(A, M, K, sAm, sAk), MatView::strided(B, N, K, sBn, sBk), beta, C,
+              epi, parts, kc);
+}
+
+void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                  const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi) {
   tc_gemm_run(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, 2, 0);
 }
@@ -1300,28 +1336,34 @@ bool tc_eligible(int64_t M, int64_t N, int64_t K) {
   return M <= INT32_MAX && N <= INT32_MAX;
 }
 
-void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
-                      int64_t sAk, const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm,
-                      int64_t sCn, int parts, int kc) {
+// C (strides sCm, sCn) = alpha A B + beta C with A: M x K and B: N x K views; a short M becomes
+// the narrow N tile of C^T = B^T A^T so that the long side fills the 128-row MMA tile
+void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const MatView& A, const MatView& B,
+                      double beta, double* C, int64_t sCm, int64_t sCn, int parts, int kc) {
   GemmEpilogue epi;
   epi.msplit = 0;
   if (M <= 256 && N > M) {
-    // short M: compute C^T = B^T A^T so that the long side fills the 128-row MMA tile and
-    // the short one a narrow N tile
     epi.s_mhi = sCn;
     epi.s_n = sCm;
-    tc_gemm_run(c, N, M, K, alpha, B, sBn, sBk, A, sAk, sAm, beta, C, epi, parts, kc);
+    tc_gemm_run(c, N, M, K, alpha, B, A, beta, C, epi, parts, kc);
   } else {
     epi.s_mhi = sCm;
     epi.s_n = sCn;
-    tc_gemm_run(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, parts, kc);
+    tc_gemm_run(c, M, N, K, alpha, A, B, beta, C, epi, parts, kc);
   }
+}
+
+void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,
+                      int64_t sAk, const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm,
+                      int64_t sCn, int parts, int kc) {
+  tc_gemm_oriented(c, M, N, K, alpha, MatView::strided(A, M, K, sAm, sAk), MatView::strided(B, N, K, sBn, sBk), beta,
+                   C, sCm, sCn, parts, kc);
 }
 
 // FP64-accurate GEMM on the tensor cores (sliced operands) for the FP64 work of the MIXED
 // form; false when the problem is too small for it or outside its exponent range
-bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
-                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn) {
+bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const MatView& A, const MatView& B,
+                 double beta, double* C, int64_t sCm, int64_t sCn) {
   // a short K (a few occupied indices) leaves too little work per slice and output
   if (K < 48 || (double)M * N * K < kSlicedMinWork || M > INT32_MAX || N > INT32_MAX) return false;
   // the output must fill at least 1/16 of its 128 x (N rounded to 32) tiles
@@ -1332,18 +1374,30 @@ bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
   if (M <= 256 && N > M) {  // the short side becomes the (narrow) N tile
     epi.s_mhi = sCn;
     epi.s_n = sCm;
-    return sliced_gemm_run(c, N, M, K, alpha, B, sBn, sBk, A, sAk, sAm, beta, C, epi, kSlices);
+    return sliced_gemm_run(c, N, M, K, alpha, B, A, beta, C, epi, kSlices);
   }
   epi.s_mhi = sCm;
   epi.s_n = sCn;
-  return sliced_gemm_run(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, epi, kSlices);
+  return sliced_gemm_run(c, M, N, K, alpha, A, B, beta, C, epi, kSlices);
+}
+
+bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
+                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn) {
+  return sliced_gemm(c, M, N, K, alpha, MatView::strided(A, M, K, sAm, sAk), MatView::strided(B, N, K, sBn, sBk), beta,
+                     C, sCm, sCn);
+}
+
+bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const MatView& A, const MatView& B, double beta,
+                double* C, int64_t sCm, int64_t sCn) {
+  if (!tc_eligible(M, N, K)) return false;
+  tc_gemm_oriented(c, M, N, K, alpha, A, B, beta, C, sCm, sCn, 2, 0);
+  return true;
 }
 
 bool mixed_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                 const double* B, int64_t sBk, int64_t sBn, double beta, double* C, int64_t sCm, int64_t sCn) {
-  if (!tc_eligible(M, N, K)) return false;
-  tc_gemm_oriented(c, M, N, K, alpha, A, sAm, sAk, B, sBk, sBn, beta, C, sCm, sCn, 2, 0);
-  return true;
+  return mixed_gemm(c, M, N, K, alpha, MatView::strided(A, M, K, sAm, sAk), MatView::strided(B, N, K, sBn, sBk), beta,
+                    C, sCm, sCn);
 }
 
 // ------------------------------------------------------------------------------------
