@@ -46,6 +46,7 @@ ucc_status guard(ucc_ctx* ctx, F&& f) {
   ctx->c.last_error.clear();
   try {
     f(ctx->c);
+    tc_check(ctx->c);  // deferred status of the tensor-core launches of this call
     return UCC_OK;
   } catch (const Error& e) {
     ctx->c.last_error = e.what();

@@ -263,6 +263,7 @@ CCSDResult run_lambda(Ctx& c) {  // :93-129
     UCC_CUDA(cudaMemcpyAsync(&ss, sumsq.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     UCC_CUDA(cudaStreamSynchronize(c.stream));
     rms = std::sqrt(ss);
+    tc_check(c);
     UCC_REQUIRE(std::isfinite(rms), UCC_NAN_DETECTED, "Lambda residual is not finite");
     bool restart = false;
     if (sw.after(rms, &restart)) {

@@ -607,6 +607,7 @@ CCSDResult run_ccsd(Ctx& c) {
     UCC_CUDA(cudaMemcpyAsync(&ss, sumsq.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     UCC_CUDA(cudaStreamSynchronize(c.stream));
     rms = std::sqrt(ss);
+    tc_check(c);
     UCC_REQUIRE(std::isfinite(rms), UCC_NAN_DETECTED, "CCSD residual is not finite");
     bool restart = false;
     if (sw.after(rms, &restart)) {

@@ -454,6 +454,7 @@ CCSDResult pert_solve(Ctx& c, int h, bool right) {  // ccpert.cc:177-229
     UCC_CUDA(cudaMemcpyAsync(&ss, sumsq.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     UCC_CUDA(cudaStreamSynchronize(c.stream));
     rms = std::sqrt(ss);
+    tc_check(c);
     UCC_REQUIRE(std::isfinite(rms), UCC_NAN_DETECTED, "perturbed-wavefunction residual is not finite");
     bool restart = false;
     if (sw.after(rms, &restart)) {

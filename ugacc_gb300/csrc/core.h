@@ -228,6 +228,7 @@ struct Ctx {
   struct TimedLaunch {
     cudaEvent_t a, b;
     double flops;
+    int kind = 0;  // 0 FP64 GEMM, 1 split tensor-core GEMM, 2 sliced FP64 GEMM
   };
   std::vector<TimedLaunch> gemm_timers;
   std::vector<cudaEvent_t> event_pool;
@@ -299,6 +300,9 @@ void dgemm(Ctx& c, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alp
            int64_t sA = 0, int64_t sB = 0, int64_t sC = 0, const GemmPtrs* ptrs = nullptr);
 
 // Same with arbitrary operand strides: op(A)[m][k] = A[m*sAm + k*sAk], op(B)[k][n] = B[k*sBk + n*sBn].
+// Status of the tensor-core launches since the last check (pipeline-wait timeout, sliced
+// operand out of range), read after synchronising the stream; throws on either.
+void tc_check(Ctx& c);
 // FP64 GEMM for a small output (M, N <= 256, M N <= 4096) and a long K (>= 8192): K chunks
 // per block and a fixed-order reduce.  False when the shape does not qualify.
 bool dgemm_small_output(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm,

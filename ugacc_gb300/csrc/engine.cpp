@@ -165,9 +165,17 @@ void Ctx::resolve_timers() {
   for (auto& t : gemm_timers) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, t.a, t.b);
-    stats.fp64_gemm_ms += ms;
-    stats.fp64_gemm_flops += t.flops;
-    stats.fp64_gemm_launches++;
+    if (t.kind == 1) {
+      stats.tc_gemm_ms += ms;
+      stats.tc_gemm_flops += t.flops;
+    } else if (t.kind == 2) {
+      stats.sliced_gemm_ms += ms;
+      stats.sliced_gemm_flops += t.flops;
+    } else {
+      stats.fp64_gemm_ms += ms;
+      stats.fp64_gemm_flops += t.flops;
+      stats.fp64_gemm_launches++;
+    }
     event_pool.push_back(t.a);
     event_pool.push_back(t.b);
   }

@@ -895,7 +895,6 @@ struct Sliced {
   std::unique_ptr<Scratch> tmp;  // storage of a temporary (non-constant) operand
   int64_t rows = 0, rows_p = 0, kp = 0;
   int S = 0;
-  bool range_ok = true;
   CUtensorMap map;
   ~Sliced() {
     if (!tmp) {
@@ -914,7 +913,8 @@ struct Triples;
 struct Cache {
   std::map<Key, std::unique_ptr<Split>> ops;
   std::map<Key, std::unique_ptr<Sliced>> sliced;
-  int* range = nullptr;
+  int* range = nullptr;    // device flag: a sliced operand row maximum beyond the range (sticky)
+  int* pinned = nullptr;   // host copies of err and range, refreshed in stream order after launches
   bool sattr_set = false;
   std::shared_ptr<Triples> triples;
   int* err = nullptr;
@@ -922,8 +922,8 @@ struct Cache {
   bool attr_set = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   ~Cache() {
-    if (err) cudaFree(err);
-    if (range) cudaFree(range);
+    if (err) cudaFree(err);  // err and range share one allocation
+    if (pinned) cudaFreeHost(pinned);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
   }
@@ -956,10 +956,11 @@ static Cache& cache(Ctx& c) {
   if (!c.tc_cache) {
     auto* k = new Cache;
     c.tc_cache = std::shared_ptr<void>(k, [](void* p) { delete static_cast<Cache*>(p); });
-    UCC_CUDA(cudaMalloc(&k->err, sizeof(int)));
-    UCC_CUDA(cudaMemset(k->err, 0, sizeof(int)));
-    UCC_CUDA(cudaMalloc(&k->range, sizeof(int)));
-    UCC_CUDA(cudaMemset(k->range, 0, sizeof(int)));
+    UCC_CUDA(cudaMalloc(&k->err, 2 * sizeof(int)));
+    UCC_CUDA(cudaMemset(k->err, 0, 2 * sizeof(int)));
+    k->range = k->err + 1;
+    UCC_CUDA(cudaMallocHost(&k->pinned, 2 * sizeof(int)));
+    k->pinned[0] = k->pinned[1] = 0;
     UCC_CUDA(cudaDeviceGetAttribute(&k->sms, cudaDevAttrMultiProcessorCount, c.device));
     UCC_CUDA(cudaEventCreate(&k->ev0));
     UCC_CUDA(cudaEventCreate(&k->ev1));
@@ -1047,7 +1048,6 @@ static Sliced* slice_prepare(Ctx& c, const MatView& x, int box_rows, int S, std:
   const int64_t rblocks = (rows + 31) / 32;
   const int64_t want = std::max<int64_t>(1, (int64_t)k.sms * 8 / rblocks);
   const int64_t kchunk = std::max<int64_t>(1024, (cols + want - 1) / want);
-  UCC_CUDA(cudaMemsetAsync(k.range, 0, sizeof(int), c.stream));
   const dim3 blk(32, 8);
   slice_absmax_kernel<<<dim3((unsigned)((cols + kchunk - 1) / kchunk), (unsigned)rblocks), blk, 0, c.stream>>>(
       x, kchunk, static_cast<unsigned long long*>(amax.p));
@@ -1056,10 +1056,6 @@ static Sliced* slice_prepare(Ctx& c, const MatView& x, int box_rows, int S, std:
       x, s->rows_p, s->kp, static_cast<const unsigned long long*>(amax.p), S, s->d, s->e, k.range);
   count_kernel_launch();
   UCC_CUDA(cudaGetLastError());
-  int hrange = 0;
-  UCC_CUDA(cudaMemcpyAsync(&hrange, k.range, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  UCC_CUDA(cudaStreamSynchronize(c.stream));
-  s->range_ok = hrange == 0;
   make_map(&s->map, s->d, (int64_t)S * s->rows_p, s->kp, box_rows);
   Sliced* raw = s.get();
   if (constant)
@@ -1148,11 +1144,16 @@ static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alp
       return false;
     }
   }
-  UCC_CUDA(cudaEventRecord(k.ev0, c.stream));  // the time includes the slicing of non-cached operands
+  cudaEvent_t ev0 = c.take_event(), ev1 = c.take_event();
+  UCC_CUDA(cudaEventRecord(ev0, c.stream));  // the time includes the slicing of non-cached operands
   std::unique_ptr<Sliced> ta, tb;
   Sliced* a = slice_prepare(c, A, BM, S, ta, allow_cache);
   Sliced* b = a ? slice_prepare(c, B, bn, S, tb, allow_cache) : nullptr;
-  if (!a || !b || !a->range_ok || !b->range_ok) return false;
+  if (!a || !b) {
+    c.event_pool.push_back(ev0);
+    c.event_pool.push_back(ev1);
+    return false;
+  }
   wrote = true;
   if (!k.sattr_set) {
     UCC_CUDA(cudaFuncSetAttribute(sliced_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1216,18 +1217,12 @@ static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alp
   c.stats.sliced_gemm_launches++;
   UCC_CUDA(cudaGetLastError());
   if (part) splitk_reduce(c, M, N, p.ksplit, part->d(), alpha, beta, C, epi);
-  UCC_CUDA(cudaEventRecord(k.ev1, c.stream));
-  int herr = 0;
-  UCC_CUDA(cudaMemcpyAsync(&herr, k.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  UCC_CUDA(cudaStreamSynchronize(c.stream));  // keeps the temporary slices alive until the GEMM is done
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, k.ev0, k.ev1);
-  c.stats.sliced_gemm_ms += ms;
-  c.stats.sliced_gemm_flops += 2.0 * (double)M * (double)N * (double)K;
-  if (herr) {
-    cudaMemsetAsync(k.err, 0, sizeof(int), c.stream);
-    throw Error(UCC_DEVICE_TIMEOUT, "sliced FP64 GEMM: a pipeline wait timed out");
-  }
+  UCC_CUDA(cudaEventRecord(ev1, c.stream));
+  // no synchronisation: temporaries are freed in stream order, the time is resolved with the
+  // other GEMM timers and the status flags are read at the next synchronisation (tc_check)
+  c.gemm_timers.push_back({ev0, ev1, 2.0 * (double)M * (double)N * (double)K, 2});
+  if (c.gemm_timers.size() >= 4096) c.resolve_timers();
+  UCC_CUDA(cudaMemcpyAsync(k.pinned, k.err, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
   return true;
 }
 
@@ -1293,7 +1288,8 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const Ma
     }
   }
   const int grid = std::min(tiles * p.ksplit, k.sms);
-  UCC_CUDA(cudaEventRecord(k.ev0, c.stream));
+  cudaEvent_t ev0 = c.take_event(), ev1 = c.take_event();
+  UCC_CUDA(cudaEventRecord(ev0, c.stream));
   p.nterms = 1;
   p.a_row1 = p.b_row1 = nullptr;
   p.C32 = nullptr;
@@ -1304,18 +1300,27 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const Ma
   c.stats.tc_gemm_launches++;
   UCC_CUDA(cudaGetLastError());
   if (part) splitk_reduce(c, M, N, p.ksplit, part->d(), alpha, beta, C, epi);
-  UCC_CUDA(cudaEventRecord(k.ev1, c.stream));
-  int herr = 0;
-  UCC_CUDA(cudaMemcpyAsync(&herr, k.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  UCC_CUDA(cudaStreamSynchronize(c.stream));  // also keeps the temporary splits alive until the GEMM is done
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, k.ev0, k.ev1);
-  c.stats.tc_gemm_ms += ms;
-  c.stats.tc_gemm_flops += 2.0 * (double)M * (double)N * (double)K;
-  if (herr) {
-    cudaMemsetAsync(k.err, 0, sizeof(int), c.stream);
-    throw Error(UCC_DEVICE_TIMEOUT, "tensor-core GEMM: a pipeline wait timed out");
-  }
+  UCC_CUDA(cudaEventRecord(ev1, c.stream));
+  // no synchronisation (see sliced_gemm_part)
+  c.gemm_timers.push_back({ev0, ev1, 2.0 * (double)M * (double)N * (double)K, 1});
+  if (c.gemm_timers.size() >= 4096) c.resolve_timers();
+  UCC_CUDA(cudaMemcpyAsync(k.pinned, k.err, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+}
+
+// the status of the tensor-core launches since the last check, after a synchronisation of
+// the stream: a pipeline wait that timed out, or a sliced operand whose row maximum is
+// beyond 2^498 (the product of such rows is not formed; FP64 covers them)
+void tc_check(Ctx& c) {
+  if (!c.tc_cache) return;
+  tc::Cache& k = *static_cast<tc::Cache*>(c.tc_cache.get());
+  UCC_CUDA(cudaStreamSynchronize(c.stream));
+  const int herr = k.pinned[0], hrange = k.pinned[1];
+  if (!herr && !hrange) return;
+  k.pinned[0] = k.pinned[1] = 0;
+  UCC_CUDA(cudaMemsetAsync(k.err, 0, 2 * sizeof(int), c.stream));
+  UCC_CUDA(cudaStreamSynchronize(c.stream));
+  if (herr) throw Error(UCC_DEVICE_TIMEOUT, "tensor-core GEMM: a pipeline wait timed out");
+  throw Error(UCC_BAD_ARGS, "sliced FP64 GEMM: an operand row maximum is beyond 2^498; use PRECISION FP64");
 }
 
 void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,

@@ -128,6 +128,7 @@ double run_triples(Ctx& c) {
     c.drop("T3_A");
     c.drop("T3_B");
   }
+  tc_check(c);
   UCC_REQUIRE(std::isfinite(e), UCC_NAN_DETECTED, "(T) energy is not finite");
   return e;
 }
