@@ -163,6 +163,17 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// FP32 -> FP64 by moving the bit fields (integer pipe, GB300 has few FP64 units); zero,
+// subnormal, infinite and NaN inputs take the converting instruction
+__device__ __forceinline__ double f32_bits_to_f64(uint32_t fb) {
+  const uint32_t e = (fb >> 23) & 0xFFu;
+  if (e == 0u || e == 0xFFu) return (double)__uint_as_float(fb);
+  const unsigned long long sgn = (unsigned long long)(fb >> 31) << 63;
+  const unsigned long long ex = (unsigned long long)(e + 896u) << 52;
+  const unsigned long long mt = (unsigned long long)(fb & 0x7FFFFFu) << 29;
+  return __longlong_as_double((long long)(sgn | ex | mt));
+}
+
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
@@ -353,7 +364,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int j = 0; j < 32; j++) old[j] = (beta != 0.0 && n0 + j < p.N) ? Cb[(n0 + j) * ep.s_n] : 0.0;
 #pragma unroll
             for (int j = 0; j < 32; j++)
-              if (n0 + j < p.N) Cb[(n0 + j) * ep.s_n] = old[j] + (double)__uint_as_float(r[j]);
+              if (n0 + j < p.N) Cb[(n0 + j) * ep.s_n] = old[j] + f32_bits_to_f64(r[j]);
           } else {
             double* Cb = p.C + coff + mo;
 #pragma unroll
@@ -455,16 +466,6 @@ __device__ __forceinline__ int sunit_items(const SUnit& U) {
 
 __device__ __forceinline__ double pow2i(int e) {  // 2^e for -1022 <= e <= 1023
   return __longlong_as_double((long long)(e + 1023) << 52);
-}
-
-// FP32 -> FP64 by moving the bit fields (integer pipe); exact for zero and normal values,
-// which are all an accumulator of slice products can hold (multiples of 2^-63)
-__device__ __forceinline__ double f32_bits_to_f64(uint32_t fb) {
-  if ((fb & 0x7FFFFFFFu) == 0) return 0.0;
-  const unsigned long long sgn = (unsigned long long)(fb >> 31) << 63;
-  const unsigned long long ex = (unsigned long long)(((fb >> 23) & 0xFFu) + 896u) << 52;
-  const unsigned long long mt = (unsigned long long)(fb & 0x7FFFFFu) << 29;
-  return __longlong_as_double((long long)(sgn | ex | mt));
 }
 
 // shared memory of the sliced kernel: the operand ring, barriers, and a 32 x 33 FP32
