@@ -167,3 +167,20 @@ def test_mixed_record_sweeps_use_the_sliced_gemm():
     st = H.ctx.stats()
     assert st["sliced_gemm_launches"] > 0 and st["fp64_iterations"] >= 2
     assert abs(emx - e64) < 1e-9
+
+
+def test_sliced_gemm_reports_operands_out_of_range():
+    """A row maximum beyond 2^498 sets the sliced form's range flag in the slicing kernel
+    (which only reads and writes inside its buffers); the call then fails with UCC_BAD_ARGS
+    instead of returning a wrong product, and the context stays usable."""
+    ctx = U.Context()
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((128, 64))
+    B = rng.standard_normal((64, 256))
+    A[5, 3] = 1e160
+    with pytest.raises(U.UccError) as e:
+        ctx.gemm(A, B, precision=U.FP64_SLICED)
+    assert e.value.status == 4
+    A[5, 3] = 1.0
+    got = ctx.gemm(A, B, precision=U.FP64_SLICED)
+    np.testing.assert_allclose(got, A @ B, rtol=0, atol=1e-12)
