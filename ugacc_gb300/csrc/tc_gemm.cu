@@ -39,6 +39,10 @@ constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4, THREADS = 192;
 constexpr int A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2;
 constexpr uint32_t TMEM_COLS = 2 * BN;
 constexpr size_t SMEM_BYTES = 1024 + (size_t)STAGES * (A_BYTES + B_BYTES) + 256;
+// gemm_kernel: an operand ring of 216 KB (four 48 KB stages, or fused stages of
+// A_hi | A_lo | B_hi | B_lo), then the barriers
+constexpr size_t GEMM_RING = 216 * 1024;
+constexpr size_t GEMM_SMEM_BYTES = 1024 + GEMM_RING + 256;
 // instruction descriptor, kind::f16: D f32 (bit 4), A bf16 (bits 7-9 = 1), B bf16
 // (bits 10-12 = 1), both K-major, N>>3 at bits 17-22, M>>4 at bits 24-28
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
@@ -75,6 +79,10 @@ struct Params {
   // accumulator added into the FP64 output by the epilogue (the first with beta, the
   // rest with 1), which bounds the FP32 accumulation chain; FP64 output only
   int kc;
+  // fused (two parts, kc == 0): one ring stage holds A_hi, A_lo, B_hi and B_lo of a K block
+  // and the three products are issued from it (a third less operand traffic than one
+  // stage per product); nst stages of stage_bytes each
+  int fused, nst, stage_bytes;
 };
 
 // the split products of one K block: (A part, B part), part 0 = hi, 1 = lo (2 parts) or
@@ -195,12 +203,13 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = smem;
   uint8_t* sB = smem + STAGES * A_BYTES;
-  uint64_t* full = (uint64_t*)(sB + STAGES * B_BYTES);
+  uint64_t* full = (uint64_t*)(smem + GEMM_RING);
   uint64_t* empty = full + STAGES;
   uint64_t* tfull = empty + STAGES;
   uint64_t* tempty = tfull + 2;
   uint32_t* tslot = (uint32_t*)(tempty + 2);
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int nst = p.fused ? p.nst : STAGES;  // ring stages (at most STAGES)
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
@@ -224,7 +233,9 @@ __global__ void __launch_bounds__(THREADS, 1)
   const uint32_t tmem = *tslot;
   const int tiles_per = p.mtiles * p.ntiles;
   const int ntile = tiles_per * (p.nprob ? p.nprob : (p.ksplit > 1 ? p.ksplit : 1));
-  const int nseg = p.nparts == 3 ? 6 : 3;
+  // ring items per K block and term: one fused stage, or one stage per split product
+  const int nseg = p.fused ? 1 : (p.nparts == 3 ? 6 : 3);
+  const uint32_t b_tile = (uint32_t)(p.bn * BK * 2);
   // K chunks of one tile (in-kernel chunking) and the K blocks of chunk ch
   const int nch = p.kc > 0 ? (p.kblocks + p.kc - 1) / p.kc : 1;
 
@@ -255,26 +266,35 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             const int term = kb / (nseg * kn), w = kb - term * nseg * kn;
             const int seg = w / kn, kk = (k0 + w - seg * kn) * BK;
-            int pa, pbp;
-            seg_parts(p.nparts, seg, pa, pbp);
-            const CUtensorMap* ma = term == 0 ? (pa == 0 ? &mAhi : (pa == 1 && p.nparts == 3) ? &mAmid : &mAlo)
-                                              : (pa == 0 ? &mA2hi : &mA2lo);
-            const CUtensorMap* mb = pbp == 0 ? &mBhi : (pbp == 1 && p.nparts == 3) ? &mBmid : &mBlo;
-            mbar_expect_tx(&full[stage], (uint32_t)(A_BYTES + p.bn * BK * 2));
-            tma_load(sA + stage * A_BYTES, ma, &full[stage], kk, term == 0 ? ar0 : ar1);
-            tma_load(sB + stage * B_BYTES, mb, &full[stage], kk, term == 0 ? br0 : br1);
+            if (p.fused) {  // A_hi | A_lo | B_hi | B_lo of K block kk
+              uint8_t* st = smem + (size_t)stage * p.stage_bytes;
+              mbar_expect_tx(&full[stage], (uint32_t)(2 * A_BYTES) + 2 * b_tile);
+              tma_load(st, term == 0 ? &mAhi : &mA2hi, &full[stage], kk, term == 0 ? ar0 : ar1);
+              tma_load(st + A_BYTES, term == 0 ? &mAlo : &mA2lo, &full[stage], kk, term == 0 ? ar0 : ar1);
+              tma_load(st + 2 * A_BYTES, &mBhi, &full[stage], kk, term == 0 ? br0 : br1);
+              tma_load(st + 2 * A_BYTES + b_tile, &mBlo, &full[stage], kk, term == 0 ? br0 : br1);
+            } else {
+              int pa, pbp;
+              seg_parts(p.nparts, seg, pa, pbp);
+              const CUtensorMap* ma = term == 0 ? (pa == 0 ? &mAhi : (pa == 1 && p.nparts == 3) ? &mAmid : &mAlo)
+                                                : (pa == 0 ? &mA2hi : &mA2lo);
+              const CUtensorMap* mb = pbp == 0 ? &mBhi : (pbp == 1 && p.nparts == 3) ? &mBmid : &mBlo;
+              mbar_expect_tx(&full[stage], (uint32_t)A_BYTES + b_tile);
+              tma_load(sA + stage * A_BYTES, ma, &full[stage], kk, term == 0 ? ar0 : ar1);
+              tma_load(sB + stage * B_BYTES, mb, &full[stage], kk, term == 0 ? br0 : br1);
+            }
             ++issued;
-            if (++stage == STAGES) {
+            if (++stage == nst) {
               stage = 0;
               phase ^= 1u;
             }
           }
         }
       }
-      // the last STAGES loads must have landed before the CTA may exit (matters only on
-      // an error path; normally the epilogue's final wait already implies it)
-      for (int64_t n = issued > STAGES ? issued - STAGES : 0; n < issued; n++)
-        mbar_wait_deadline(&full[n % STAGES], (uint32_t)((n / STAGES) & 1));
+      // the last ring loads must have landed before the CTA may exit (matters only on an
+      // error path; normally the epilogue's final wait already implies it)
+      for (int64_t n = issued > nst ? issued - nst : 0; n < issued; n++)
+        mbar_wait_deadline(&full[n % nst], (uint32_t)((n / nst) & 1));
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -302,12 +322,25 @@ __global__ void __launch_bounds__(THREADS, 1)
               break;
             }
             fence_after();
-            const uint64_t ad = sdesc(sA + stage * A_BYTES), bd = sdesc(sB + stage * B_BYTES);
+            if (p.fused) {  // hi.hi, hi.lo, lo.hi from one stage
+              uint8_t* st = smem + (size_t)stage * p.stage_bytes;
+              const uint64_t ahi = sdesc(st), alo = sdesc(st + A_BYTES);
+              const uint64_t bhi = sdesc(st + 2 * A_BYTES), blo = sdesc(st + 2 * A_BYTES + b_tile);
 #pragma unroll
-            for (int k = 0; k < BK / 16; k++)  // +32 bytes along K per 16-element step
-              mma_i(d, ad + (uint64_t)(k * 2), bd + (uint64_t)(k * 2), idesc, (kb | k) != 0);
+              for (int pr = 0; pr < 3; pr++) {
+                const uint64_t ad = pr == 2 ? alo : ahi, bd = pr == 1 ? blo : bhi;
+#pragma unroll
+                for (int k = 0; k < BK / 16; k++)
+                  mma_i(d, ad + (uint64_t)(k * 2), bd + (uint64_t)(k * 2), idesc, (kb | pr | k) != 0);
+              }
+            } else {
+              const uint64_t ad = sdesc(sA + stage * A_BYTES), bd = sdesc(sB + stage * B_BYTES);
+#pragma unroll
+              for (int k = 0; k < BK / 16; k++)  // +32 bytes along K per 16-element step
+                mma_i(d, ad + (uint64_t)(k * 2), bd + (uint64_t)(k * 2), idesc, (kb | k) != 0);
+            }
             mma_commit(&empty[stage]);
-            if (++stage == STAGES) {
+            if (++stage == nst) {
               stage = 0;
               phase ^= 1u;
             }
@@ -1227,6 +1260,15 @@ static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alp
   return true;
 }
 
+namespace tc {
+// ring layout of a two-part launch: fused stages (A_hi | A_lo | B_hi | B_lo), as many as fit
+static void set_fused(Params& p, bool fused) {
+  p.fused = fused ? 1 : 0;
+  p.stage_bytes = 2 * A_BYTES + 2 * p.bn * BK * 2;
+  p.nst = fused ? (int)std::min<size_t>(STAGES, GEMM_RING / (size_t)p.stage_bytes) : STAGES;
+}
+}  // namespace tc
+
 // A: M x K, B: N x K (rows = the output's columns)
 void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const MatView& A, const MatView& B,
                  double beta, double* C, const GemmEpilogue& epi, int parts, int kc) {
@@ -1238,7 +1280,7 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const Ma
   Split* a = prepare(c, A, BM, ta, parts);
   Split* b = prepare(c, B, bn, tb, parts);
   if (!k.attr_set) {
-    UCC_CUDA(cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+    UCC_CUDA(cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM_BYTES));
     k.attr_set = true;
   }
   Params p;
@@ -1295,7 +1337,8 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const Ma
   p.a_row1 = p.b_row1 = nullptr;
   p.C32 = nullptr;
   p.nparts = parts;
-  gemm_kernel<<<grid, THREADS, SMEM_BYTES, c.stream>>>(a->mhi, a->mlo, b->mhi, b->mlo, a->mhi, a->mlo,
+  set_fused(p, parts == 2 && p.kc == 0);
+  gemm_kernel<<<grid, THREADS, GEMM_SMEM_BYTES, c.stream>>>(a->mhi, a->mlo, b->mhi, b->mlo, a->mhi, a->mlo,
                                                       parts == 3 ? a->mmid : a->mhi, parts == 3 ? b->mmid : b->mhi, p);
   count_kernel_launch();
   c.stats.tc_gemm_launches++;
@@ -1508,7 +1551,7 @@ bool mixed_triples_prepare(Ctx& c, int max_batch) {
   UCC_CUDA(cudaMalloc(&T->d_coff, sizeof(int64_t) * max_batch));
   k.triples = T;
   if (!k.attr_set) {
-    UCC_CUDA(cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+    UCC_CUDA(cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM_BYTES));
     k.attr_set = true;
   }
   return true;
@@ -1576,7 +1619,8 @@ bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, float* W3) {
     UCC_CUDA(cudaEventRecord(k.ev0, c.stream));
     p.nparts = 2;
     p.kc = 0;
-    gemm_kernel<<<std::min(tiles, k.sms), THREADS, SMEM_BYTES, c.stream>>>(T.A.mhi, T.A.mlo, T.B.mhi, T.B.mlo,
+    set_fused(p, true);
+    gemm_kernel<<<std::min(tiles, k.sms), THREADS, GEMM_SMEM_BYTES, c.stream>>>(T.A.mhi, T.A.mlo, T.B.mhi, T.B.mlo,
                                                                           T.A2.mhi, T.A2.mlo, T.A.mhi, T.B.mhi, p);
     count_kernel_launch();
     c.stats.tc_gemm_launches++;
