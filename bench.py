@@ -264,6 +264,10 @@ def main():
     flops_step = flops_ccsd_iter(NO, NV) * iters + flops_triples(NO, NV)
     value = world * flops_step / (ms * 1e-3) / 1e12
 
+    # the device-resident context is no longer needed: release its memory (the no=32/nv=320
+    # blocks and their tensor-core copies would not fit twice)
+    del cc
+    H.ctx.close()
     # end to end through the public API from pinned host memory
     Bp = torch.from_numpy(np.ascontiguousarray(h.B)).pin_memory()
     Fp = torch.from_numpy(np.ascontiguousarray(h.fock)).pin_memory()

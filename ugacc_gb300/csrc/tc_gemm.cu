@@ -39,6 +39,13 @@ constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4, THREADS = 192;
 constexpr int A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2;
 constexpr uint32_t TMEM_COLS = 2 * BN;
 constexpr size_t SMEM_BYTES = 1024 + (size_t)STAGES * (A_BYTES + B_BYTES) + 256;
+// N tile for N output columns: the fewest tiles of at most 256 columns, each a multiple of
+// 32 (N = 320 takes two tiles of 160 rather than 256 + 64)
+inline int pick_bn(int64_t N) {
+  const int64_t nt = (N + 255) / 256;
+  return (int)(((N + nt - 1) / nt + 31) / 32 * 32);
+}
+
 // gemm_kernel: an operand ring of 216 KB (four 48 KB stages, or fused stages of
 // A_hi | A_lo | B_hi | B_lo), then the barriers
 constexpr size_t GEMM_RING = 216 * 1024;
@@ -1137,8 +1144,8 @@ static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alp
   UCC_REQUIRE(S >= 2 && SB * S <= 56, UCC_BAD_ARGS, "sliced GEMM: 2 to 9 slices");
   const double aa = std::fabs(alpha);
   if (!(aa >= 0x1p-20 && aa <= 0x1p20) || M > INT32_MAX || N > INT32_MAX) return false;
-  // N tile: a short N is padded to a multiple of 32 only
-  const int bn = N >= BN ? BN : (int)((N + 31) / 32 * 32);
+  // N tile (pick_bn): no more tiles than 256-column ones would need, padded to multiples of 32
+  const int bn = pick_bn(N);
   Cache& k = cache(c);
   {
     const int64_t Mp = (M + BM - 1) / BM * BM, Np = (N + bn - 1) / bn * bn, kp = (K + BK - 1) / BK * BK;
@@ -1276,7 +1283,7 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const Ma
   UCC_REQUIRE(parts == 2 || parts == 3, UCC_BAD_ARGS, "tensor-core GEMM: 2 or 3 split parts");
   Cache& k = cache(c);
   std::unique_ptr<Split> ta, tb;
-  const int bn = N >= BN ? BN : (int)((N + 31) / 32 * 32);  // a short N is padded to a multiple of 32 only
+  const int bn = pick_bn(N);
   Split* a = prepare(c, A, BM, ta, parts);
   Split* b = prepare(c, B, bn, tb, parts);
   if (!k.attr_set) {
@@ -1484,7 +1491,7 @@ __global__ void split_into_kernel(int64_t rows, int64_t cols, const double* src,
 
 struct Triples {
   Split A, A2, B;  // A2: A with its (a,b) row pairs in (b,a) order
-  int bn = BN;     // N tile: the virtual index c, padded to a multiple of 32
+  int bn = BN;     // N tile over the virtual index c (pick_bn)
   int* d_arow = nullptr;
   int* d_brow = nullptr;
   int64_t* d_coff = nullptr;
@@ -1543,7 +1550,7 @@ bool mixed_triples_prepare(Ctx& c, int max_batch) {
   make_map(&T->A.mlo, T->A.lo, T->A.rows, kp, BM);
   make_map(&T->A2.mhi, T->A2.hi, T->A2.rows, kp, BM);
   make_map(&T->A2.mlo, T->A2.lo, T->A2.rows, kp, BM);
-  T->bn = nv >= BN ? BN : (int)((nv + 31) / 32 * 32);
+  T->bn = pick_bn(nv);
   make_map(&T->B.mhi, T->B.hi, T->B.rows, kp, T->bn);
   make_map(&T->B.mlo, T->B.lo, T->B.rows, kp, T->bn);
   UCC_CUDA(cudaMalloc(&T->d_arow, sizeof(int) * 2 * max_batch));
