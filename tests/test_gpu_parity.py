@@ -175,3 +175,22 @@ def test_triples_gradient_vs_oracle_larger():
         ref = tg[k]
         np.testing.assert_allclose(H.ctx.get(name, shp), ref, atol=1e-20 + 1e-9 * np.abs(ref).max(), rtol=0,
                                    err_msg=k)
+
+
+@pytest.mark.skipif("c2" not in cases(), reason="the no=16/nv=160 reference run is not recorded")
+def test_c2_workload_vs_reference():
+    """The bench workload itself (no=16, nv=160, seed 1): E_CCSD and E_(T) of the
+    reference's own compiled code (hours on one core) against the FP64 and the mixed form."""
+    meta, arr = load("c2")
+    h, _ = hamiltonian(meta)
+    run = meta["runs"]["ccsd_t"]
+    H = U.Hamiltonian.from_synthetic(h)
+    cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "MAXITER": 100, "WFN": "CCSD_T"})
+    cc.compute_energy()
+    assert abs(cc.eccsd - run["e_ccsd"]) < ETOL
+    assert abs(cc.et - run["e_t_tjl"]) < ETOL
+    np.testing.assert_allclose(cc.t1, arr["ccsd_t/t1"], atol=TTOL, rtol=0)
+    mx = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "MAXITER": 100, "WFN": "CCSD_T", "PRECISION": "MIXED"})
+    mx.compute_energy()
+    assert abs(mx.eccsd - run["e_ccsd"]) < 1e-10
+    assert abs(mx.et - run["e_t_tjl"]) < 1e-8
