@@ -304,6 +304,25 @@ void dgemm(Ctx& c, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alp
 // Permutation: out (dense, dims od) = alpha * in(strides is, in out's axis order) + beta * out
 // ------------------------------------------------------------------------------------
 namespace {
+// alpha * x + beta * y with the common coefficients taken off the FP64 pipe (GB300 issues
+// about two FP64 operations per SM clock, so a multiply per element already competes with
+// HBM): alpha = +-1 is exact (a sign flip), beta = 0 stores, beta = 1 adds once.  The
+// results are bit-identical to fma(beta, y, alpha * x).
+__device__ __forceinline__ double combine(double alpha, double x, double beta, const double* y) {
+  double v;
+  if (alpha == 1.0)
+    v = x;
+  else if (alpha == -1.0)
+    v = __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+  else
+    v = alpha * x;
+  if (beta == 0.0) return v;
+  if (beta == 1.0) return *y + v;
+  return fma(beta, *y, v);
+}
+}  // namespace
+
+namespace {
 struct PermArgs {
   int rank;
   int64_t od[kMaxRank];
@@ -315,18 +334,72 @@ struct PermArgs {
   int64_t total;
 };
 
+// Index arithmetic runs in 32 bits (I = uint32_t) whenever every element count and offset
+// fits: a 64-bit division is a long software sequence, and with one per axis per element
+// the index math, not HBM, bounded these kernels.
+template <class I>
 __global__ void permute_kernel_elem(PermArgs a) {
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < a.total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t rem = idx, off = 0, oo = 0;
+  I od[kMaxRank], is[kMaxRank], os[kMaxRank];
+  for (int k = 0; k < a.rank; k++) od[k] = (I)a.od[k], is[k] = (I)a.is[k], os[k] = (I)a.os[k];
+  const I total = (I)a.total;
+  for (I idx = (I)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (I)gridDim.x * blockDim.x) {
+    I rem = idx, off = 0, oo = 0;
     for (int k = a.rank - 1; k >= 0; k--) {
-      const int64_t x = rem % a.od[k];
-      rem /= a.od[k];
-      off += x * a.is[k];
-      oo += x * a.os[k];
+      const I x = rem % od[k];
+      rem /= od[k];
+      off += x * is[k];
+      oo += x * os[k];
     }
-    const double v = a.alpha * a.in[off];
-    a.out[oo] = (a.beta == 0.0) ? v : fma(a.beta, a.out[oo], v);
+    a.out[oo] = combine(a.alpha, a.in[off], a.beta, a.out + oo);
+  }
+}
+
+// Rows of the last output axis cut into 128-element segments; each warp takes a contiguous
+// range of segments, decomposes a row's base offsets only when its row changes, and keeps
+// four loads per lane in flight before the stores.
+template <class I>
+__global__ void permute_kernel_rows(PermArgs a) {
+  const int r = a.rank;
+  I od[kMaxRank], is[kMaxRank], os[kMaxRank];
+  for (int k = 0; k < r; k++) od[k] = (I)a.od[k], is[k] = (I)a.is[k], os[k] = (I)a.os[k];
+  const I dl = od[r - 1], isl = is[r - 1], osl = os[r - 1];
+  const I rows = (I)(a.total / a.od[r - 1]);
+  const I nseg = (dl + 127) / 128, items = rows * nseg;
+  const int lane = threadIdx.x & 31;
+  const I nwarps = ((I)gridDim.x * blockDim.x) >> 5;
+  const I warp = ((I)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const I per = (items + nwarps - 1) / nwarps;
+  const I w0 = warp * per, w1 = (w0 + per < items) ? w0 + per : items;
+  const double* __restrict__ in = a.in;
+  double* __restrict__ out = a.out;
+  I cur = (I)-1, bi = 0, bo = 0;
+  for (I w = w0; w < w1; w++) {
+    const I row = w / nseg, x0 = (w - row * nseg) * 128;
+    if (row != cur) {
+      I rem = row;
+      bi = 0, bo = 0;
+      for (int k = r - 2; k >= 0; k--) {
+        const I x = rem % od[k];
+        rem /= od[k];
+        bi += x * is[k];
+        bo += x * os[k];
+      }
+      cur = row;
+    }
+    double v[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const I x = x0 + (I)(u * 32 + lane);
+      v[u] = x < dl ? in[bi + x * isl] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const I x = x0 + (I)(u * 32 + lane);
+      if (x < dl) {
+        double* o = out + bo + x * osl;
+        *o = combine(a.alpha, v[u], a.beta, o);
+      }
+    }
   }
 }
 
@@ -342,35 +415,70 @@ struct TileArgs {
   int64_t tiles_last;
 };
 
+template <class I>
 __global__ void permute_kernel_tile(TileArgs t) {
   __shared__ double tile[32][33];
   const int r = t.p.rank;
-  const int64_t dl = t.p.od[r - 1], dq = t.p.od[t.q];
-  const int64_t tl = (blockIdx.x % t.tiles_last) * 32, tq = (blockIdx.x / t.tiles_last) * 32;
-  const int64_t isl = t.p.is[r - 1], osq = t.p.os[t.q];
-  for (int64_t rest = blockIdx.y; rest < t.rest_total; rest += gridDim.y) {
-    int64_t rem = rest, bi = 0, bo = 0;
+  const I dl = (I)t.p.od[r - 1], dq = (I)t.p.od[t.q];
+  const I tiles_last = (I)t.tiles_last;
+  const I tl = ((I)blockIdx.x % tiles_last) * 32, tq = ((I)blockIdx.x / tiles_last) * 32;
+  const I isl = (I)t.p.is[r - 1], osq = (I)t.p.os[t.q], osl = (I)t.p.os[r - 1];
+  I rd[kMaxRank], ris[kMaxRank], ros[kMaxRank];
+  for (int k = 0; k < t.nrest; k++) rd[k] = (I)t.rd[k], ris[k] = (I)t.ris[k], ros[k] = (I)t.ros[k];
+  const I rest_total = (I)t.rest_total;
+  for (I rest = blockIdx.y; rest < rest_total; rest += gridDim.y) {
+    I rem = rest, bi = 0, bo = 0;
     for (int k = t.nrest - 1; k >= 0; k--) {
-      const int64_t x = rem % t.rd[k];
-      rem /= t.rd[k];
-      bi += x * t.ris[k];
-      bo += x * t.ros[k];
+      const I x = rem % rd[k];
+      rem /= rd[k];
+      bi += x * ris[k];
+      bo += x * ros[k];
     }
     for (int jj = threadIdx.y; jj < 32; jj += blockDim.y) {
-      const int64_t xl = tl + jj, xq = tq + threadIdx.x;
+      const I xl = tl + jj, xq = tq + threadIdx.x;
       if (xl < dl && xq < dq) tile[jj][threadIdx.x] = t.p.in[bi + xl * isl + xq];
     }
     __syncthreads();
     for (int jj = threadIdx.y; jj < 32; jj += blockDim.y) {
-      const int64_t xq = tq + jj, xl = tl + threadIdx.x;
+      const I xq = tq + jj, xl = tl + threadIdx.x;
       if (xl < dl && xq < dq) {
-        double* o = t.p.out + bo + xq * osq + xl * t.p.os[r - 1];
-        const double v = t.p.alpha * tile[threadIdx.x][jj];
-        *o = (t.p.beta == 0.0) ? v : fma(t.p.beta, *o, v);
+        double* o = t.p.out + bo + xq * osq + xl * osl;
+        *o = combine(t.p.alpha, tile[threadIdx.x][jj], t.p.beta, o);
       }
     }
     __syncthreads();
   }
+}
+
+// Drop unit axes and merge neighbours that are contiguous in both tensors, so that e.g.
+// ijab <- jiab becomes a rank-3 copy with rows of nv*nv elements.
+void canonical_axes(PermArgs& a) {
+  int r = 0;
+  for (int k = 0; k < a.rank; k++) {
+    if (a.od[k] == 1) continue;
+    if (r > 0 && a.is[r - 1] == a.is[k] * a.od[k] && a.os[r - 1] == a.os[k] * a.od[k]) {
+      a.od[r - 1] *= a.od[k];
+      a.is[r - 1] = a.is[k];
+      a.os[r - 1] = a.os[k];
+      continue;
+    }
+    a.od[r] = a.od[k], a.is[r] = a.is[k], a.os[r] = a.os[k];
+    r++;
+  }
+  if (r == 0) a.od[0] = 1, a.is[0] = 1, a.os[0] = 1, r = 1;
+  a.rank = r;
+}
+
+// True when every element count and every in/out offset of the permutation is below 2^31.
+bool fits32(const PermArgs& a) {
+  int64_t mi = 0, mo = 0;
+  for (int k = 0; k < a.rank; k++) {
+    mi += (a.od[k] - 1) * (a.is[k] < 0 ? -a.is[k] : a.is[k]);
+    mo += (a.od[k] - 1) * (a.os[k] < 0 ? -a.os[k] : a.os[k]);
+    if (a.is[k] < 0 || a.os[k] < 0) return false;
+  }
+  const int64_t lim = (int64_t)1 << 31;
+  return a.total < lim && mi < lim && mo < lim;
 }
 }  // namespace
 
@@ -398,23 +506,21 @@ void permute_add(Ctx& c, const Tensor& in, double alpha, double beta, const Tens
     UCC_REQUIRE(in.d[k] == out.d[k], UCC_BAD_ARGS, "permute_add: dim mismatch");
     a.od[k] = out.d[k];
     a.is[k] = in.s[k];
+    a.os[k] = out.s[k];
   }
-  for (int k = 0; k < out.rank; k++) a.os[k] = out.s[k];
   a.alpha = alpha;
   a.beta = beta;
   a.in = in.p;
   a.out = out.p;
-  const int r = out.rank;
+  canonical_axes(a);
+  const bool narrow = fits32(a);
+  const int r = a.rank;
   int q = -1;
-  if (r >= 2 && in.s[r - 1] != 1 && out.s[r - 1] == 1 && out.d[r - 1] >= 8) {
+  if (r >= 2 && a.is[r - 1] != 1 && a.os[r - 1] == 1 && a.od[r - 1] >= 8) {
     for (int k = 0; k < r - 1; k++)
-      if (in.s[k] == 1 && out.d[k] >= 8) q = k;
+      if (a.is[k] == 1 && a.od[k] >= 8) q = k;
   }
-  if (q < 0) {
-    const int threads = 256;
-    const int64_t blocks = std::min<int64_t>((a.total + threads - 1) / threads, 152 * 64);
-    permute_kernel_elem<<<(unsigned)blocks, threads, 0, c.stream>>>(a);
-  } else {
+  if (q >= 0) {
     TileArgs t{};
     t.p = a;
     t.q = q;
@@ -431,7 +537,25 @@ void permute_add(Ctx& c, const Tensor& in, double alpha, double beta, const Tens
     t.tiles_last = (a.od[r - 1] + 31) / 32;
     const int64_t tiles_q = (a.od[q] + 31) / 32;
     dim3 grid((unsigned)(t.tiles_last * tiles_q), (unsigned)std::min<int64_t>(t.rest_total, 65535));
-    permute_kernel_tile<<<grid, dim3(32, 8), 0, c.stream>>>(t);
+    if (narrow)
+      permute_kernel_tile<uint32_t><<<grid, dim3(32, 8), 0, c.stream>>>(t);
+    else
+      permute_kernel_tile<int64_t><<<grid, dim3(32, 8), 0, c.stream>>>(t);
+  } else if (a.od[r - 1] >= 32) {
+    const int threads = 256;
+    const int64_t items = (a.total / a.od[r - 1]) * ((a.od[r - 1] + 127) / 128);
+    const int64_t blocks = std::min<int64_t>((items + 7) / 8, 152 * 16);
+    if (narrow)
+      permute_kernel_rows<uint32_t><<<(unsigned)blocks, threads, 0, c.stream>>>(a);
+    else
+      permute_kernel_rows<int64_t><<<(unsigned)blocks, threads, 0, c.stream>>>(a);
+  } else {
+    const int threads = 256;
+    const int64_t blocks = std::min<int64_t>((a.total + threads - 1) / threads, 152 * 64);
+    if (narrow)
+      permute_kernel_elem<uint32_t><<<(unsigned)blocks, threads, 0, c.stream>>>(a);
+    else
+      permute_kernel_elem<int64_t><<<(unsigned)blocks, threads, 0, c.stream>>>(a);
   }
   count_launch();
   check_launch("permute");
@@ -443,8 +567,7 @@ void permute_add(Ctx& c, const Tensor& in, double alpha, double beta, const Tens
 namespace {
 __global__ void axpby_kernel(int64_t n, double alpha, const double* x, double beta, double* y) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double v = alpha * x[i];
-    y[i] = (beta == 0.0) ? v : fma(beta, y[i], v);
+    y[i] = combine(alpha, x[i], beta, y + i);
   }
 }
 __global__ void fill_kernel(int64_t n, double v, double* y) {
@@ -524,6 +647,24 @@ __global__ void dot_pass1(int64_t n, const double* const* xs, const double* x0, 
   if (threadIdx.x == 0) partial[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = tot;
 }
 
+// The DIIS overlaps: one FMA per element per thread (a thread's share is ~n / 131072
+// terms), the block and cross-block folds as above.  The compensated per-element form
+// costs about six FP64 operations per element and bounded this kernel on GB300's FP64
+// pipe; the overlaps only feed the extrapolation coefficients.
+__global__ void multidot_pass1(int64_t n, const double* const* xs, const double* y, double* partial) {
+  const double* __restrict__ x = xs[blockIdx.y];
+  double s0 = 0.0, s1 = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + stride < n; i += 2 * stride) {
+    s0 = fma(x[i], y[i], s0);
+    s1 = fma(x[i + stride], y[i + stride], s1);
+  }
+  if (i < n) s0 = fma(x[i], y[i], s0);
+  const double tot = block_sum(s0 + s1);
+  if (threadIdx.x == 0) partial[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = tot;
+}
+
 __global__ void sum_pass2(int nparts, const double* partial, double* out) {
   // one block per output
   const double* p = partial + (int64_t)blockIdx.x * nparts;
@@ -557,7 +698,7 @@ void multidot_async(Ctx& c, int nvec, const double* const* d_xs, const double* y
   UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
   if (nvec <= 0) return;
   Scratch part(c, sizeof(double) * RED_BLOCKS * nvec);
-  dot_pass1<<<dim3(RED_BLOCKS, nvec), RED_THREADS, 0, c.stream>>>(n, d_xs, nullptr, y, part.d());
+  multidot_pass1<<<dim3(RED_BLOCKS, nvec), RED_THREADS, 0, c.stream>>>(n, d_xs, y, part.d());
   sum_pass2<<<nvec, RED_THREADS, 0, c.stream>>>(RED_BLOCKS, part.d(), d_out);
   count_launch();
   count_launch();
@@ -585,34 +726,36 @@ __global__ void tau_kernel(int no, int nv, const double* t1, const double* t2, d
   }
 }
 
-// sum of squares of the residuals goes to partial[block]
+// Sum of squares of the residuals goes to partial[block] (one FMA per element: all terms
+// are non-negative, so the plain sum is accurate to the number of terms a thread folds
+// times the unit roundoff).  Index arithmetic in I (32 bits when no*no*nv*nv < 2^31).
+template <class I>
 __global__ void jacobi_kernel(int no, int nv, const double* d_do, const double* d_dv, double shift, const double* R1,
                               const double* R2, const double* t1o, const double* t2o, double* t1n, double* t2n,
                               double* partial) {
-  const int64_t n1 = (int64_t)no * nv, n2 = (int64_t)no * no * nv * nv;
-  double s = 0.0, cc = 0.0;
-  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n1 + n2;
-       x += (int64_t)gridDim.x * blockDim.x) {
+  const I n1 = (I)no * nv, n2 = (I)no * no * nv * nv, v = (I)nv, o = (I)no;
+  double s = 0.0;
+  for (I x = (I)blockIdx.x * blockDim.x + threadIdx.x; x < n1 + n2; x += (I)gridDim.x * blockDim.x) {
     if (x < n1) {
-      const int a = (int)(x % nv), i = (int)(x / nv);
+      const I a = x % v, i = x / v;
       const double r = R1[x];
-      neumaier(s, cc, r * r);
+      s = fma(r, r, s);
       t1n[x] = t1o[x] + r / ((d_do[i] - d_dv[a]) + shift);
     } else {
-      const int64_t y = x - n1;
-      const int b = (int)(y % nv);
-      int64_t q = y / nv;
-      const int a = (int)(q % nv);
-      q /= nv;
-      const int j = (int)(q % no);
-      const int i = (int)(q / no);
+      const I y = x - n1;
+      const I b = y % v;
+      I q = y / v;
+      const I a = q % v;
+      q /= v;
+      const I j = q % o;
+      const I i = q / o;
       const double r = R2[y];
-      neumaier(s, cc, r * r);
+      s = fma(r, r, s);
       const double D = ((d_do[i] + d_do[j]) - d_dv[a]) - d_dv[b];
       t2n[y] = t2o[y] + r / (D + shift);
     }
   }
-  const double tot = block_sum(s + cc);
+  const double tot = block_sum(s);
   if (threadIdx.x == 0) partial[blockIdx.x] = tot;
 }
 
@@ -639,8 +782,13 @@ void jacobi_update(Ctx& c, int no, int nv, const double* d_do, const double* d_d
                    double* d_sumsq) {
   UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
   Scratch part(c, sizeof(double) * RED_BLOCKS);
-  jacobi_kernel<<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(no, nv, d_do, d_dv, shift, R1, R2, t1old, t2old, t1new,
-                                                          t2new, part.d());
+  const int64_t n = (int64_t)no * nv + (int64_t)no * no * nv * nv;
+  if (n + (int64_t)RED_BLOCKS * RED_THREADS < ((int64_t)1 << 31))
+    jacobi_kernel<uint32_t><<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(no, nv, d_do, d_dv, shift, R1, R2, t1old, t2old,
+                                                                      t1new, t2new, part.d());
+  else
+    jacobi_kernel<int64_t><<<RED_BLOCKS, RED_THREADS, 0, c.stream>>>(no, nv, d_do, d_dv, shift, R1, R2, t1old, t2old,
+                                                                     t1new, t2new, part.d());
   sum_pass2<<<1, RED_THREADS, 0, c.stream>>>(RED_BLOCKS, part.d(), d_sumsq);
   count_launch();
   count_launch();
