@@ -134,11 +134,13 @@ def test_fine_split_gemm_matches_fp64():
 
 @pytest.mark.parametrize("M,N,K,ta,tb", [(128, 256, 64, 0, 0), (300, 520, 777, 0, 1), (257, 129, 1000, 1, 0),
                                           (40, 3000, 5000, 0, 1), (1000, 300, 96, 1, 1), (640, 768, 20000, 0, 0),
-                                          (2200000, 40, 64, 0, 0)])
+                                          (2200000, 40, 64, 0, 0), (2560, 2560, 16, 0, 0), (160, 40960, 16, 1, 0),
+                                          (3000, 700, 24, 0, 1), (999, 1001, 40, 1, 1)])
 def test_sliced_fp64_gemm(M, N, K, ta, tb):
     """UCC_FP64_SLICED: 9 exact bf16 slices per operand on the tensor cores, FP64-accurate
-    (error of the order of FP64 rounding, relative to the row / column maxima).  The last
-    shape exceeds one slicing launch and runs in row chunks."""
+    (error of the order of FP64 rounding, relative to the row / column maxima).  The
+    2200000-row shape exceeds one slicing launch and runs in row chunks; K = 16 ... 40 are
+    zero-padded to the 64-wide K block."""
     rng = np.random.default_rng(M * 7 + N + K)
     A = rng.standard_normal((K, M) if ta else (M, K)) * np.exp(2.0 * rng.standard_normal((K, M) if ta else (M, K)))
     B = rng.standard_normal((N, K) if tb else (K, N))

@@ -138,6 +138,22 @@ __global__ void __launch_bounds__(GT) dgemm_kernel(GemmArgs g) {
   }
 }
 
+// alpha * x + beta * y with the common coefficients taken off the FP64 pipe (GB300 issues
+// about two FP64 operations per SM clock, so a multiply per element already competes with
+// HBM): alpha = +-1 is exact (a sign flip), beta = 0 stores, beta = 1 adds once.  The
+// results are bit-identical to fma(beta, y, alpha * x).
+__device__ __forceinline__ double combine(double alpha, double x, double beta, const double* y) {
+  double v;
+  if (alpha == 1.0)
+    v = x;
+  else if (alpha == -1.0)
+    v = __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+  else
+    v = alpha * x;
+  if (beta == 0.0) return v;
+  if (beta == 1.0) return *y + v;
+  return fma(beta, *y, v);
+}
 // C(epi) = alpha * sum_z P[z][m][n] + beta * C(epi), the fixed-order split-K reduction
 __global__ void splitk_reduce_kernel(int64_t M, int64_t N, int nsplit, const double* P, double alpha, double beta,
                                      double* C, GemmEpilogue ep) {
@@ -303,25 +319,6 @@ void dgemm(Ctx& c, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alp
 // ------------------------------------------------------------------------------------
 // Permutation: out (dense, dims od) = alpha * in(strides is, in out's axis order) + beta * out
 // ------------------------------------------------------------------------------------
-namespace {
-// alpha * x + beta * y with the common coefficients taken off the FP64 pipe (GB300 issues
-// about two FP64 operations per SM clock, so a multiply per element already competes with
-// HBM): alpha = +-1 is exact (a sign flip), beta = 0 stores, beta = 1 adds once.  The
-// results are bit-identical to fma(beta, y, alpha * x).
-__device__ __forceinline__ double combine(double alpha, double x, double beta, const double* y) {
-  double v;
-  if (alpha == 1.0)
-    v = x;
-  else if (alpha == -1.0)
-    v = __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
-  else
-    v = alpha * x;
-  if (beta == 0.0) return v;
-  if (beta == 1.0) return *y + v;
-  return fma(beta, *y, v);
-}
-}  // namespace
-
 namespace {
 struct PermArgs {
   int rank;
@@ -709,20 +706,21 @@ void multidot_async(Ctx& c, int nvec, const double* const* d_xs, const double* y
 // Amplitude kernels
 // ------------------------------------------------------------------------------------
 namespace {
+template <class I>
 __global__ void tau_kernel(int no, int nv, const double* t1, const double* t2, double f1, double* tau, double f2,
                            double* ttau) {
-  const int64_t n = (int64_t)no * no * nv * nv;
-  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
-    const int b = (int)(x % nv);
-    int64_t r = x / nv;
-    const int a = (int)(r % nv);
-    r /= nv;
-    const int j = (int)(r % no);
-    const int i = (int)(r / no);
-    const double tt = t1[(int64_t)i * nv + a] * t1[(int64_t)j * nv + b];
+  const I n = (I)no * no * nv * nv, v_ = (I)nv, o_ = (I)no;
+  for (I x = (I)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (I)gridDim.x * blockDim.x) {
+    const I b = x % v_;
+    I r = x / v_;
+    const I a = r % v_;
+    r /= v_;
+    const I j = r % o_;
+    const I i = r / o_;
+    const double tt = t1[i * v_ + a] * t1[j * v_ + b];
     const double v = t2[x];
-    tau[x] = v + f1 * tt;
-    if (ttau) ttau[x] = v + f2 * tt;
+    tau[x] = fma(f1, tt, v);
+    if (ttau) ttau[x] = fma(f2, tt, v);
   }
 }
 
@@ -772,7 +770,10 @@ void build_tau(Ctx& c, int no, int nv, const double* t1, const double* t2, doubl
                double* ttau) {
   UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
   const int64_t n = (int64_t)no * no * nv * nv;
-  tau_kernel<<<grid_for(n), 256, 0, c.stream>>>(no, nv, t1, t2, f1, tau, f2, ttau);
+  if (n + 152 * 32 * 256 < ((int64_t)1 << 31))
+    tau_kernel<uint32_t><<<grid_for(n), 256, 0, c.stream>>>(no, nv, t1, t2, f1, tau, f2, ttau);
+  else
+    tau_kernel<int64_t><<<grid_for(n), 256, 0, c.stream>>>(no, nv, t1, t2, f1, tau, f2, ttau);
   count_launch();
   check_launch("tau");
 }
@@ -1022,23 +1023,24 @@ __global__ void pack_tau_kernel(int no, int nv, const double* __restrict__ tau, 
 
 // R2[ijab] += S[(i,j) sorted][(a,b) sorted] + sign * A[...], sign = (-1)^[i>j] (-1)^[a>b],
 // A = 0 on i == j or a == b
+template <class I>
 __global__ void unpack_ladder_kernel(int no, int nv, double alpha, const double* __restrict__ S,
                                      const double* __restrict__ A, double* R2) {
-  const int64_t n = (int64_t)no * no * nv * nv;
-  const int64_t vp = (int64_t)nv * (nv + 1) / 2, vm = (int64_t)nv * (nv - 1) / 2;
-  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
-    const int b = (int)(x % nv);
-    int64_t r = x / nv;
-    const int a = (int)(r % nv);
-    r /= nv;
-    const int j = (int)(r % no), i = (int)(r / no);
-    const int i0 = min(i, j), j0 = max(i, j), a0 = min(a, b), b0 = max(a, b);
-    double v = S[((int64_t)j0 * (j0 + 1) / 2 + i0) * vp + (int64_t)b0 * (b0 + 1) / 2 + a0];
+  const I n = (I)no * no * nv * nv, v_ = (I)nv, o_ = (I)no;
+  const I vp = v_ * (v_ + 1) / 2, vm = v_ * (v_ - 1) / 2;
+  for (I x = (I)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (I)gridDim.x * blockDim.x) {
+    const I b = x % v_;
+    I r = x / v_;
+    const I a = r % v_;
+    r /= v_;
+    const I j = r % o_, i = r / o_;
+    const I i0 = i < j ? i : j, j0 = i < j ? j : i, a0 = a < b ? a : b, b0 = a < b ? b : a;
+    double v = S[(int64_t)(j0 * (j0 + 1) / 2 + i0) * vp + b0 * (b0 + 1) / 2 + a0];
     if (i != j && a != b) {
-      const double am = A[((int64_t)j0 * (j0 - 1) / 2 + i0) * vm + (int64_t)b0 * (b0 - 1) / 2 + a0];
+      const double am = A[(int64_t)(j0 * (j0 - 1) / 2 + i0) * vm + b0 * (b0 - 1) / 2 + a0];
       v += ((i > j) != (a > b)) ? -am : am;
     }
-    R2[x] += alpha * v;
+    R2[x] = combine(alpha, v, 1.0, R2 + x);
   }
 }
 }  // namespace
@@ -1062,7 +1064,10 @@ void pack_tau(Ctx& c, int no, int nv, const double* tau, double* Tp, double* Tm)
 void unpack_ladder(Ctx& c, int no, int nv, double alpha, const double* S, const double* A, double* R2) {
   UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
   const int64_t n = (int64_t)no * no * nv * nv;
-  unpack_ladder_kernel<<<grid_for(n), 256, 0, c.stream>>>(no, nv, alpha, S, A, R2);
+  if (n + 152 * 32 * 256 < ((int64_t)1 << 31))
+    unpack_ladder_kernel<uint32_t><<<grid_for(n), 256, 0, c.stream>>>(no, nv, alpha, S, A, R2);
+  else
+    unpack_ladder_kernel<int64_t><<<grid_for(n), 256, 0, c.stream>>>(no, nv, alpha, S, A, R2);
   count_launch();
   check_launch("unpack_ladder");
 }
@@ -1101,21 +1106,34 @@ void triples_energy(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, con
 // free side is a single vector; a 64x64 GEMM tile would waste 63/64 of its work)
 // ------------------------------------------------------------------------------------
 namespace {
-__global__ void gemv_ncontig(int64_t N, int64_t K, double alpha, const double* x, int64_t sx, const double* A,
-                             int64_t sk, int64_t sn, double beta, double* y, int64_t sy) {
+// Block (bx, z) folds the k range [z*kc, min(K, (z+1)*kc)) of 32 consecutive n; with one
+// K chunk it writes y, otherwise the chunk sums go to P[z][n] for gemv_reduce (fixed order).
+__global__ void gemv_ncontig(int64_t N, int64_t K, int64_t kc, double alpha, const double* x, int64_t sx,
+                             const double* A, int64_t sk, int64_t sn, double beta, double* y, int64_t sy, double* P) {
   // blockDim = (32, 8): threadIdx.x over n (coalesced when sn == 1), threadIdx.y over k
   __shared__ double red[8][33];
   const int64_t n = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  const int64_t k0 = (int64_t)blockIdx.y * kc, k1 = k0 + kc < K ? k0 + kc : K;
   double s = 0.0;
   if (n < N)
-    for (int64_t k = threadIdx.y; k < K; k += 8) s = fma(x[k * sx], A[k * sk + n * sn], s);
+    for (int64_t k = k0 + threadIdx.y; k < k1; k += 8) s = fma(x[k * sx], A[k * sk + n * sn], s);
   red[threadIdx.y][threadIdx.x] = s;
   __syncthreads();
   if (threadIdx.y == 0 && n < N) {
     double t = 0.0;
     for (int r = 0; r < 8; r++) t += red[r][threadIdx.x];
-    double* o = y + n * sy;
-    *o = (beta == 0.0) ? alpha * t : fma(beta, *o, alpha * t);
+    if (P)
+      P[(int64_t)blockIdx.y * N + n] = t;
+    else
+      y[n * sy] = combine(alpha, t, beta, y + n * sy);
+  }
+}
+__global__ void gemv_reduce(int64_t N, int nz, const double* __restrict__ P, double alpha, double beta, double* y,
+                            int64_t sy) {
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    double t = P[n];
+    for (int z = 1; z < nz; z++) t += P[(int64_t)z * N + n];
+    y[n * sy] = combine(alpha, t, beta, y + n * sy);
   }
 }
 __global__ void gemv_kcontig(int64_t N, int64_t K, double alpha, const double* x, int64_t sx, const double* A,
@@ -1150,7 +1168,22 @@ void dgemv_strided(Ctx& c, int64_t N, int64_t K, double alpha, const double* x, 
     gemv_kcontig<<<(unsigned)((N + wpb - 1) / wpb), 32 * wpb, 0, c.stream>>>(N, K, alpha, x, sx, A, sk, sn, beta, y,
                                                                             sy);
   } else {
-    gemv_ncontig<<<(unsigned)((N + 31) / 32), dim3(32, 8), 0, c.stream>>>(N, K, alpha, x, sx, A, sk, sn, beta, y, sy);
+    // enough blocks for ~4 per SM: split K into chunks of at least 256 when the n tiles are few
+    const int64_t nb = (N + 31) / 32;
+    int64_t nz = std::min<int64_t>((4 * 152 + nb - 1) / nb, K / 256);
+    nz = std::max<int64_t>(1, std::min<int64_t>(nz, 256));
+    const int64_t kc = nz > 1 ? (K + nz - 1) / nz : K;
+    if (nz > 1) nz = (K + kc - 1) / kc;
+    if (nz <= 1) {
+      gemv_ncontig<<<dim3((unsigned)nb, 1), dim3(32, 8), 0, c.stream>>>(N, K, K, alpha, x, sx, A, sk, sn, beta, y, sy,
+                                                                         nullptr);
+    } else {
+      Scratch part(c, sizeof(double) * nz * N);
+      gemv_ncontig<<<dim3((unsigned)nb, (unsigned)nz), dim3(32, 8), 0, c.stream>>>(N, K, kc, alpha, x, sx, A, sk, sn,
+                                                                                   beta, y, sy, part.d());
+      gemv_reduce<<<grid_for(N), 256, 0, c.stream>>>(N, (int)nz, part.d(), alpha, beta, y, sy);
+      count_launch();
+    }
   }
   count_launch();
   check_launch("gemv");

@@ -189,6 +189,18 @@ __device__ __forceinline__ double f32_bits_to_f64(uint32_t fb) {
   return __longlong_as_double((long long)(sgn | ex | mt));
 }
 
+// FP64 -> FP32 truncated toward zero by moving the bit fields (relative error below 2^-23,
+// integer pipe); zeros keep their sign, values outside FP32's normal range take the
+// converting instruction
+__device__ __forceinline__ float f64_to_f32_trunc(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const uint32_t sgn = (uint32_t)(b >> 32) & 0x80000000u;
+  if ((b << 1) == 0ull) return __uint_as_float(sgn);
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;
+  if (e < -126 || e > 127) return (float)v;
+  return __uint_as_float(sgn | ((uint32_t)(e + 127) << 23) | (uint32_t)((b >> 29) & 0x7FFFFFu));
+}
+
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
@@ -861,7 +873,8 @@ __global__ void slice_digits_kernel(MatView x, int64_t rows_p, int64_t kp, const
       } else {
         d = X;  // what remains: |d| <= H
       }
-      dst[(size_t)s * plane] = __float2bfloat16_rn((float)d * __int_as_float((127 - SB * (s + 1)) << 23));
+      // |d| <= 2^(SB-1): a 32-bit conversion, exact, and exact in bf16 after the power-of-2 scale
+      dst[(size_t)s * plane] = __float2bfloat16_rn((float)(int)d * __int_as_float((127 - SB * (s + 1)) << 23));
     }
   }
 }
@@ -870,7 +883,8 @@ __global__ void slice_digits_kernel(MatView x, int64_t rows_p, int64_t kp, const
 // (mid != null: three parts, x = hi + mid + lo, each the bf16 rounding of what remains)
 // 32 x 32 tiles through shared memory: reads coalesced along whichever stride is 1 (sk == 1:
 // along k, otherwise along the rows), writes along k.  Two parts are formed in FP32 (x
-// rounded to FP32 first: 2^-24, far below the lo part's 2^-17), three parts in FP64.
+// truncated to FP32 first, from its bit fields: 2^-23, far below the lo part's 2^-17),
+// three parts in FP64.
 __global__ void split_kernel(MatView x, int64_t kp, __nv_bfloat16* hi, __nv_bfloat16* lo, __nv_bfloat16* mid) {
   __shared__ double t[32][33];
   const int64_t rows = x.rows, cols = x.cols;
@@ -902,7 +916,7 @@ __global__ void split_kernel(MatView x, int64_t kp, __nv_bfloat16* hi, __nv_bflo
       mid[o] = m;
       lo[o] = __double2bfloat16(rest);
     } else {
-      const float f = (float)v;
+      const float f = f64_to_f32_trunc(v);
       const __nv_bfloat16 h = __float2bfloat16_rn(f);
       hi[o] = h;
       lo[o] = __float2bfloat16_rn(f - __bfloat162float(h));
@@ -1420,7 +1434,10 @@ void tc_gemm_oriented(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, con
 // form; false when the problem is too small for it or outside its exponent range
 bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const MatView& A, const MatView& B,
                  double beta, double* C, int64_t sCm, int64_t sCn) {
-  // a short K (a few occupied indices) leaves too little work per slice and output
+  // a short K (a few occupied indices) leaves too little work per slice and output: routing
+  // the K = 16 contractions of a no=16/nv=160 CCSD solve here instead of the DFMA kernel
+  // (operands sliced per call, 45 padded products, the 9-order epilogue) made its sweeps
+  // slower (203 -> 220 ms per solve)
   if (K < 48 || (double)M * N * K < kSlicedMinWork || M > INT32_MAX || N > INT32_MAX) return false;
   // the output must fill at least 1/16 of its 128 x (N rounded to 32) tiles
   const int64_t lo = std::min(M, N), hi = std::max(M, N);
@@ -1473,18 +1490,19 @@ __global__ void split_into_kernel(int64_t rows, int64_t cols, const double* src,
   const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
   for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
     const int64_t r = r0 + threadIdx.x, k = k0 + yy;
-    t[yy][threadIdx.x] =
-        (r < rows && k < cols) ? scale * src[(r / rsplit) * sr_hi + (r % rsplit) * sr + k * sk] : 0.0;
+    const double x = (r < rows && k < cols) ? src[(r / rsplit) * sr_hi + (r % rsplit) * sr + k * sk] : 0.0;
+    t[yy][threadIdx.x] = scale == 1.0 ? x : scale * x;
   }
   __syncthreads();
   for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
     const int64_t r = r0 + yy, k = k0 + threadIdx.x;
     if (r < rows && k < cols) {
-      const double v = t[threadIdx.x][yy];
-      const __nv_bfloat16 h = __double2bfloat16(v);
+      // in FP32 from the truncated value (2^-23, below the lo part's 2^-18): no FP64 pipe work
+      const float f = f64_to_f32_trunc(t[threadIdx.x][yy]);
+      const __nv_bfloat16 h = __float2bfloat16_rn(f);
       const int64_t o = (row0 + r) * ld + col0 + k;
       hi[o] = h;
-      lo[o] = __double2bfloat16(v - (double)__bfloat162float(h));
+      lo[o] = __float2bfloat16_rn(f - __bfloat162float(h));
     }
   }
 }
