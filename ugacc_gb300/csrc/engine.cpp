@@ -215,8 +215,10 @@ Temp::Temp(Ctx& c, const std::vector<int64_t>& dims, bool zero) : buf(c, [&] {
 namespace {
 
 // GEMMs with at least this many multiply-adds are anchored during refinement; lighter
-// ones simply run in FP64 there
-constexpr double kAnchorMinWork = 5e8;
+// ones simply run in FP64 there.  The contractions over one occupied index (K = no) sit
+// near 1e8 at no=16/nv=160: in FP64 they are bound by GB300's FP64 pipe (2 M N K
+// operations), anchored they cost a copy, one split tensor-core product and a permute
+constexpr double kAnchorMinWork = 5e7;
 // the corrections of a delta sweep use the two-part split: the three-part split with
 // FP64-summed K chunks (UCC_MIXED_FINE) measured 8x less noise in the delta residuals at
 // no=16/nv=160 but costs ~10 % of the step and still leaves the final FP64 sweep needed
