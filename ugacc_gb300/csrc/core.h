@@ -317,8 +317,6 @@ void dgemv_strided(Ctx& c, int64_t N, int64_t K, double alpha, const double* x, 
 
 // out = alpha * in + beta * out over out's dims; both may be strided views.
 void permute_add(Ctx& c, const Tensor& in, double alpha, double beta, const Tensor& out);
-// out = in - sub, sub laid out like out (one pass; the delta operands of anchored GEMMs)
-void permute_sub(Ctx& c, const Tensor& in, const double* sub, const Tensor& out);
 
 // y = alpha * x + beta * y, dense, n elements
 void axpby(Ctx& c, int64_t n, double alpha, const double* x, double beta, double* y);

@@ -278,19 +278,18 @@ void anchored_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const 
   const Ctx::AnchorTerm& t = an.terms[an.next++];
   UCC_REQUIRE(t.M == M && t.N == N && t.K == K && t.a_const == a_const && t.b_const == b_const, UCC_BAD_STATE,
               "anchored refinement: the GEMM sequence changed since the record sweep");
-  // P = P0 + (A - A0) B + A0 (B - B0) in a dense temporary (the corrections' epilogues write
-  // coalesced rows; accumulating them into C's own, usually permuted, strides measured
-  // slower), then C = alpha P + beta C by one permute
   Temp P(c, {M, N});
   UCC_CUDA(cudaMemcpyAsync(P->p, t.p0->p, sizeof(double) * M * N, cudaMemcpyDeviceToDevice, c.stream));
-  if (!a_const) {
+  if (!a_const) {  // P += (A - A0) B
     Temp dA(c, {M, K});
-    permute_sub(c, av, t.a0->p, dA);
+    permute_add(c, av, 1.0, 0.0, dA);
+    axpby(c, M * K, -1.0, t.a0->p, 1.0, dA->p);
     tc_gemm_oriented(c, M, N, K, 1.0, dA->p, K, 1, B, sBk, sBn, 1.0, P->p, N, 1, kDeltaParts, kDeltaChunk);
   }
-  if (!b_const) {
+  if (!b_const) {  // P += A0 (B - B0)
     Temp dB(c, {K, N});
-    permute_sub(c, bv, t.b0->p, dB);
+    permute_add(c, bv, 1.0, 0.0, dB);
+    axpby(c, K * N, -1.0, t.b0->p, 1.0, dB->p);
     if (a_const)
       tc_gemm_oriented(c, M, N, K, 1.0, A, sAm, sAk, dB->p, N, 1, 1.0, P->p, N, 1, kDeltaParts, kDeltaChunk);
     else

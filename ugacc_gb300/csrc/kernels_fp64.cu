@@ -328,7 +328,6 @@ struct PermArgs {
   double alpha, beta;
   const double* in;
   double* out;
-  const double* sub;  // null, or subtracted from in (laid out like out)
   int64_t total;
 };
 
@@ -348,8 +347,7 @@ __global__ void permute_kernel_elem(PermArgs a) {
       off += x * is[k];
       oo += x * os[k];
     }
-    const double x = a.sub ? a.in[off] - a.sub[oo] : a.in[off];
-    a.out[oo] = combine(a.alpha, x, a.beta, a.out + oo);
+    a.out[oo] = combine(a.alpha, a.in[off], a.beta, a.out + oo);
   }
 }
 
@@ -396,8 +394,7 @@ __global__ void permute_kernel_rows(PermArgs a) {
       const I x = x0 + (I)(u * 32 + lane);
       if (x < dl) {
         double* o = out + bo + x * osl;
-        const double y = a.sub ? v[u] - a.sub[bo + x * osl] : v[u];
-        *o = combine(a.alpha, y, a.beta, o);
+        *o = combine(a.alpha, v[u], a.beta, o);
       }
     }
   }
@@ -442,10 +439,8 @@ __global__ void permute_kernel_tile(TileArgs t) {
     for (int jj = threadIdx.y; jj < 32; jj += blockDim.y) {
       const I xq = tq + jj, xl = tl + threadIdx.x;
       if (xl < dl && xq < dq) {
-        const I oo = bo + xq * osq + xl * osl;
-        double* o = t.p.out + oo;
-        const double y = t.p.sub ? tile[threadIdx.x][jj] - t.p.sub[oo] : tile[threadIdx.x][jj];
-        *o = combine(t.p.alpha, y, t.p.beta, o);
+        double* o = t.p.out + bo + xq * osq + xl * osl;
+        *o = combine(t.p.alpha, tile[threadIdx.x][jj], t.p.beta, o);
       }
     }
     __syncthreads();
@@ -484,20 +479,7 @@ bool fits32(const PermArgs& a) {
 }
 }  // namespace
 
-static void permute_launch(Ctx& c, const Tensor& in, double alpha, double beta, const Tensor& out,
-                           const double* sub);
-
 void permute_add(Ctx& c, const Tensor& in, double alpha, double beta, const Tensor& out) {
-  permute_launch(c, in, alpha, beta, out, nullptr);
-}
-
-void permute_sub(Ctx& c, const Tensor& in, const double* sub, const Tensor& out) {
-  UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "permute_sub: not recordable");
-  permute_launch(c, in, 1.0, 0.0, out, sub);
-}
-
-static void permute_launch(Ctx& c, const Tensor& in, double alpha, double beta, const Tensor& out,
-                           const double* sub) {
   UCC_REQUIRE(in.rank == out.rank, UCC_BAD_ARGS, "permute_add: rank mismatch");
   if (Recorder* r = recorder()) {
     RecordedOp o;
@@ -527,7 +509,6 @@ static void permute_launch(Ctx& c, const Tensor& in, double alpha, double beta, 
   a.beta = beta;
   a.in = in.p;
   a.out = out.p;
-  a.sub = sub;
   canonical_axes(a);
   const bool narrow = fits32(a);
   const int r = a.rank;
