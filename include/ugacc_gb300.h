@@ -73,6 +73,25 @@ ucc_status ucc_set_options(ucc_ctx* ctx, const ucc_options* opt);
 ucc_status ucc_load_hamiltonian(ucc_ctx* ctx, int no, int nv, const double* fock, const double* ints);
 ucc_status ucc_load_hamiltonian_df(ucc_ctx* ctx, int no, int nv, int naux, const double* fock, const double* B);
 
+/* Replaces: the integral side of psi::ugacc::Hamiltonian::Hamiltonian (hamiltonian.cc:21-102)
+ * for hosts with MO integrals in a file instead of psi4's libtrans.  The file has the
+ * FCIDUMP layout: a header "&FCI NORB=n, NELEC=N, MS2=0, ... &END" (or a "/" line), then
+ * lines "value i j k l" with (ij|kl) over real orbitals (1-based, any of the 8 equivalent
+ * orders), "value i j 0 0" = h_ij, "value 0 0 0 0" = nuclear repulsion ("value i 0 0 0",
+ * orbital energies, is ignored).  Orbitals are taken in the file's order, the first
+ * NELEC/2 doubly occupied; the first nfzc are frozen core and the last nfzv frozen
+ * virtuals (hamiltonian.cc:24-27).  Host code only: no context and no device needed.
+ *   ucc_fcidump_dims: NORB and NELEC of the header.
+ *   ucc_fcidump_read: fock [nact][nact] (the determinant's Fock matrix over the active
+ *     orbitals, QT order, hamiltonian.cc:43-56), ints [nact]^4 with ints[p][q][r][s] =
+ *     <pq|rs> = (pr|qs) (hamiltonian.cc:76-91), energies[3] = {nuclear repulsion,
+ *     frozen-core energy (hamiltonian.cc:72), SCF energy}; nact = NORB - nfzc - nfzv,
+ *     no = NELEC/2 - nfzc.  Closed-shell files only (UCC_UNSUPPORTED otherwise).
+ * Errors are written to err (errlen bytes, may be null). */
+ucc_status ucc_fcidump_dims(const char* path, int* norb, int* nelec, char* err, size_t errlen);
+ucc_status ucc_fcidump_read(const char* path, int nfzc, int nfzv, double* fock, double* ints, double* energies,
+                            char* err, size_t errlen);
+
 /* Replaces: CCWfn::CCWfn + CCWfn::compute_energy, CCSD part (ccwfn.cc:12-120, :188-235).
  * e_ccsd is the energy of the amplitudes before the final update, as the reference
  * reports it (ccwfn.cc:224,233). */

@@ -55,16 +55,39 @@ class Hamiltonian {
     check(nullptr, ucc_ctx_create(&ctx_, device));
     check(ctx_, ucc_load_hamiltonian_df(ctx_, no, nv, naux, fock, B));
   }
+  // hamiltonian.cc:21-102 from an MO-integral file in the FCIDUMP layout (ucc_fcidump_read):
+  // nfzc frozen core and nfzv frozen virtual orbitals; enuc(), efzc() and escf() keep the
+  // file's nuclear repulsion, the frozen-core energy and the SCF energy
+  static std::shared_ptr<Hamiltonian> from_fcidump(const std::string& path, int nfzc = 0, int nfzv = 0,
+                                                   int device = 0) {
+    char err[512];
+    int norb = 0, nelec = 0;
+    ucc_status st = ucc_fcidump_dims(path.c_str(), &norb, &nelec, err, sizeof err);
+    if (st != UCC_OK) throw Error(st, err);
+    const int nact = norb - nfzc - nfzv, no = nelec / 2 - nfzc;
+    if (nact <= 0 || no <= 0 || no >= nact) throw Error(UCC_BAD_ARGS, "fcidump: frozen orbitals leave no active space");
+    std::vector<double> fock((size_t)nact * nact), ints((size_t)nact * nact * nact * nact);
+    double en[3];
+    st = ucc_fcidump_read(path.c_str(), nfzc, nfzv, fock.data(), ints.data(), en, err, sizeof err);
+    if (st != UCC_OK) throw Error(st, err);
+    auto H = std::make_shared<Hamiltonian>(no, nact - no, fock.data(), ints.data(), device);
+    H->enuc_ = en[0], H->efzc_ = en[1], H->escf_ = en[2];
+    return H;
+  }
   ~Hamiltonian() { ucc_ctx_destroy(ctx_); }
   Hamiltonian(const Hamiltonian&) = delete;
   Hamiltonian& operator=(const Hamiltonian&) = delete;
   ucc_ctx* ctx() const { return ctx_; }
   int no() const { return no_; }
   int nv() const { return nv_; }
+  double enuc() const { return enuc_; }
+  double efzc() const { return efzc_; }
+  double escf() const { return escf_; }
 
  private:
   ucc_ctx* ctx_ = nullptr;
   int no_, nv_;
+  double enuc_ = 0.0, efzc_ = 0.0, escf_ = 0.0;
 };
 
 class CCWfn {

@@ -39,3 +39,29 @@ def test_driver_reports_nonconvergence(tmp_path):
     out = subprocess.run([DRIVER, inp, "MAXITER=1", "R_CONVERGENCE=1e-12"], capture_output=True, text=True,
                          timeout=300)
     assert out.returncode == 3 and "not converged" in out.stderr
+
+
+def test_driver_reads_fcidump_with_frozen_orbitals(tmp_path):
+    """An MO-integral file (FCIDUMP layout) through Hamiltonian::from_fcidump: the driver's
+    energies equal the Python API's on the same file; E_total = E_SCF + E_CC."""
+    import numpy as np
+
+    import ugacc_gb300 as U
+    from oracle import fcidump as FD
+
+    build()
+    h = make_hamiltonian(6, 22, 9)
+    eri = h.eri_chemist()
+    path = str(tmp_path / "FCIDUMP")
+    FD.write(path, FD.core_hamiltonian_for(h.fock, eri, h.no), eri, 2.5, 2 * h.no)
+    out = subprocess.run([DRIVER, path, "WFN=CCSD_T", "NFZC=1", "NFZV=3", "R_CONVERGENCE=1e-10"],
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    r = json.loads(out.stdout)
+    H = U.Hamiltonian.from_fcidump(path, nfzc=1, nfzv=3)
+    cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "WFN": "CCSD_T"})
+    e = cc.compute_energy()
+    assert abs(r["e_ccsd"] - cc.eccsd) < 1e-12 and abs(r["e_t"] - cc.et) < 1e-12
+    assert abs(r["e_scf"] - H.escf) < 1e-12 and abs(r["e_frozen_core"] - H.efzc) < 1e-12
+    assert abs(r["e_total"] - (H.escf + e)) < 1e-12
+    assert np.isfinite(r["e_total"])

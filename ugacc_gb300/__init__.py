@@ -138,6 +138,8 @@ def load_library(path: str | None = None):
         "ucc_batch_get_info": (i, [vp, P(BatchInfo)]),
         "ucc_batch_get_t2": (i, [vp, i, dp, ctypes.c_size_t]),
         "ucc_batch_features": (i, [vp, i, fp, ctypes.c_size_t, i, fp]),
+        "ucc_fcidump_dims": (i, [cp, P(i), P(i), cp, ctypes.c_size_t]),
+        "ucc_fcidump_read": (i, [cp, i, i, dp, dp, dp, cp, ctypes.c_size_t]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -223,6 +225,33 @@ DEFAULT_OPTIONS = {"WFN": "CCSD", "DERTYPE": "NONE", "MAXITER": 100, "R_CONVERGE
                    "MIXED_SWITCH": 1e-5, "OOC": False}
 
 
+def read_fcidump(path: str, nfzc: int = 0, nfzv: int = 0) -> dict:
+    """Active-space Hamiltonian from an MO-integral file in the FCIDUMP layout (host code,
+    no GPU): the integral side of hamiltonian.cc:21-102 with ``nfzc`` frozen core and
+    ``nfzv`` frozen virtual orbitals (orbitals in the file's order, the first NELEC/2
+    doubly occupied).  Returns ``no``, ``nv``, ``fock`` [nact][nact], ``ints`` [nact]^4
+    (``ints[p,q,r,s] = <pq|rs>``), ``enuc``, ``efzc`` (frozen-core energy) and ``escf``."""
+    lib = load_library()
+    err = ctypes.create_string_buffer(512)
+    norb, nelec = ctypes.c_int(), ctypes.c_int()
+    bpath = os.fsencode(path)
+    st = lib.ucc_fcidump_dims(bpath, ctypes.byref(norb), ctypes.byref(nelec), err, 512)
+    if st:
+        raise UccError(st, err.value.decode())
+    nact = norb.value - nfzc - nfzv
+    if nact <= 0:
+        raise UccError(4, "fcidump: frozen orbitals leave no active orbital")
+    fock = np.empty((nact, nact))
+    ints = np.empty((nact,) * 4)
+    en = np.empty(3)
+    st = lib.ucc_fcidump_read(bpath, nfzc, nfzv, _ptr(fock), _ptr(ints), _ptr(en), err, 512)
+    if st:
+        raise UccError(st, err.value.decode())
+    no = nelec.value // 2 - nfzc
+    return {"no": no, "nv": nact - no, "fock": fock, "ints": ints, "enuc": float(en[0]), "efzc": float(en[1]),
+            "escf": float(en[2])}
+
+
 class Hamiltonian:
     """hamiltonian.h:12-34: Fock matrix (QT order) and two-electron integrals.
 
@@ -245,6 +274,15 @@ class Hamiltonian:
             self.ctx.check(self.ctx.lib.ucc_load_hamiltonian_df(self.ctx.h, no, nv, b.shape[0], _ptr(f), _ptr(b)))
         else:
             raise ValueError("need ints or B")
+
+    @classmethod
+    def from_fcidump(cls, path: str, nfzc: int = 0, nfzv: int = 0, **kw):
+        """hamiltonian.cc:21-102 from an FCIDUMP file (``read_fcidump``); the file's
+        energies are kept as ``enuc``, ``efzc`` and ``escf``."""
+        d = read_fcidump(path, nfzc, nfzv)
+        H = cls(d["no"], d["nv"], d["fock"], ints=d["ints"], **kw)
+        H.enuc, H.efzc, H.escf = d["enuc"], d["efzc"], d["escf"]
+        return H
 
     @classmethod
     def from_synthetic(cls, ham, use_ints: bool = False, **kw):

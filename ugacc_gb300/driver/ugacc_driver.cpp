@@ -1,11 +1,15 @@
 // Command-line driver: the reference plugin's pipeline (ugacc.cc:108-241) on the
 // C++ class surface of the GB300 library, for a Hamiltonian stored in the synthetic
-// input format of ugacc_gb300/generator.py (three-index factors are used).
+// input format of ugacc_gb300/generator.py (three-index factors are used) or in an
+// MO-integral file in the FCIDUMP layout (first non-blank text "&FCI"; NFZC / NFZV frozen
+// core and virtual orbitals, hamiltonian.cc:24-27).
 //
-// usage: ugacc_driver <input.bin> [WFN=CCSD|CCSD_T] [DERTYPE=NONE|FIRST|SECOND]
+// usage: ugacc_driver <input.bin | FCIDUMP> [WFN=CCSD|CCSD_T] [DERTYPE=NONE|FIRST|SECOND]
 //        [MAXITER=100] [R_CONVERGENCE=1e-7] [DIIS=1] [MY_OMEGA=0] [MYHAND=RIGHT|LEFT]
-//        [PRECISION=FP64|MIXED] [REFINE_SWEEPS=2] [PRINT=0] [OOC=0|1]
-// Prints one JSON object with the energies (and polarizabilities for DERTYPE=SECOND).
+//        [PRECISION=FP64|MIXED] [REFINE_SWEEPS=2] [PRINT=0] [OOC=0|1] [NFZC=0] [NFZV=0]
+// Prints one JSON object with the energies (and polarizabilities for DERTYPE=SECOND with
+// the synthetic format's perturbations).
+#include <cctype>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -23,6 +27,21 @@ struct Input {
   std::vector<double> eps, B;
   std::vector<std::vector<double>> perts;
 };
+
+// true when the file's first non-blank characters are "&FCI" (any case)
+bool is_fcidump(const char* path) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return false;
+  char buf[256];
+  const size_t n = std::fread(buf, 1, sizeof buf, f);
+  std::fclose(f);
+  size_t k = 0;
+  while (k < n && (buf[k] == ' ' || buf[k] == '\t' || buf[k] == '\r' || buf[k] == '\n')) k++;
+  if (k + 4 > n || buf[k] != '&') return false;
+  for (int j = 1; j < 4; j++)
+    if (std::toupper((unsigned char)buf[k + j]) != "&FCI"[j]) return false;
+  return true;
+}
 
 Input read_input(const char* path) {
   FILE* f = std::fopen(path, "rb");
@@ -65,10 +84,9 @@ int main(int argc, char** argv) {
   }
   auto get = [&](const char* k, const char* d) { return kv.count(k) ? kv[k] : std::string(d); };
   try {
-    Input in = read_input(argv[1]);
-    const int n = in.no + in.nv;
-    std::vector<double> fock((size_t)n * n, 0.0);
-    for (int p = 0; p < n; p++) fock[(size_t)p * n + p] = in.eps[p];
+    const bool dump = is_fcidump(argv[1]);
+    Input in;
+    if (!dump) in = read_input(argv[1]);
     Options o;
     o.wfn = get("WFN", "CCSD");
     o.dertype = get("DERTYPE", "NONE");
@@ -82,10 +100,21 @@ int main(int argc, char** argv) {
     o.diis = get("DIIS", "1") == "1";
     o.ooc = get("OOC", "0") == "1";
 
-    auto H = std::make_shared<Hamiltonian>(in.no, in.nv, in.naux, fock.data(), in.B.data());
+    std::shared_ptr<Hamiltonian> H;
+    if (dump) {
+      H = Hamiltonian::from_fcidump(argv[1], std::atoi(get("NFZC", "0").c_str()), std::atoi(get("NFZV", "0").c_str()));
+    } else {
+      const int n = in.no + in.nv;
+      std::vector<double> fock((size_t)n * n, 0.0);
+      for (int p = 0; p < n; p++) fock[(size_t)p * n + p] = in.eps[p];
+      H = std::make_shared<Hamiltonian>(in.no, in.nv, in.naux, fock.data(), in.B.data());
+    }
     auto cc = std::make_shared<CCWfn>(H, o);
     const double ecc = cc->compute_energy();
     std::printf("{\"e_ccsd\": %.17g, \"e_t\": %.17g, \"e_cc\": %.17g", cc->eccsd(), cc->et(), ecc);
+    if (dump)
+      std::printf(", \"e_scf\": %.17g, \"e_frozen_core\": %.17g, \"e_total\": %.17g", H->escf(), H->efzc(),
+                  H->escf() + ecc);
     if (o.dertype != "NONE") {
       auto hbar = std::make_shared<HBAR>(H, cc);
       auto lam = std::make_shared<CCLambda>(cc, hbar);
