@@ -861,7 +861,12 @@ __global__ void triples_energy_kernel(int no, int nv, const int* tuples, const d
 // every W3 element is read from memory once; the Voovv blocks and t1 / eps pieces of the
 // three tile ranges are staged too.  Roles 0, 1, 2 are the index ranges of a, b, c.
 constexpr int ET = 8;
-__global__ void __launch_bounds__(128) triples_energy_f32_tiled_kernel(int no, int nv, const int* __restrict__ tuples,
+// Threads per block.  The staging and energy loops below run a compile-time number of
+// iterations with closed-form local indices of (thread, iteration), which these relations
+// make exact: thread t, iteration k covers element t + TNT*k of each loop.
+constexpr int TNT = 128;
+static_assert(TNT == 2 * ET * ET && (ET * ET * ET) % TNT == 0 && (6 * ET * ET) % TNT == 0, "tile/thread layout");
+__global__ void __launch_bounds__(TNT) triples_energy_f32_tiled_kernel(int no, int nv, const int* __restrict__ tuples,
                                                                       const int* __restrict__ tri, int ntri,
                                                                       const float* __restrict__ W3,
                                                                       const double* __restrict__ t1,
@@ -882,20 +887,23 @@ __global__ void __launch_bounds__(128) triples_energy_f32_tiled_kernel(int no, i
   // for (0,1,2), (0,2,1), (1,0,2), (1,2,0), (2,0,1), (2,1,0)
   constexpr uint64_t kPerm = 0x24ull | (0x18ull << 6) | (0x21ull << 12) | (0x09ull << 18) | (0x12ull << 24) |
                              (0x06ull << 30);
-  for (int e = threadIdx.x; e < 6 * ET * ET * ET; e += blockDim.x) {
-    const int p = e / (ET * ET * ET), rem = e - p * (ET * ET * ET);
-    const int x = rem / (ET * ET), y = (rem / ET) % ET, z = rem % ET;
+  // local coordinates of this thread inside an ET^3 tile: (tx + 2 it, ty, tz) at iteration it
+  const int tid = threadIdx.x, tx = tid / (ET * ET), ty = (tid / ET) % ET, tz = tid % ET;
+#pragma unroll
+  for (int it = 0; it < 6 * ET * ET * ET / TNT; it++) {
+    const int p = it / (ET * ET * ET / TNT), x = tx + 2 * (it % (ET * ET * ET / TNT));
     const uint64_t code6 = kPerm >> (6 * p);
-    const int gx = R0((int)(code6 & 3)) + x, gy = R0((int)((code6 >> 2) & 3)) + y, gz = R0((int)((code6 >> 4) & 3)) + z;
-    Ws[p][x][y][z] = (gx < nv && gy < nv && gz < nv) ? W[(int64_t)gx * nv2 + (int64_t)gy * nv + gz] : 0.f;
+    const int gx = R0((int)(code6 & 3)) + x, gy = R0((int)((code6 >> 2) & 3)) + ty, gz = R0((int)((code6 >> 4) & 3)) + tz;
+    Ws[p][x][ty][tz] = (gx < nv && gy < nv && gz < nv) ? W[(int64_t)gx * nv2 + (int64_t)gy * nv + gz] : 0.f;
   }
   auto Vm = [&](int m) {  // Vij, Vik, Vjk
     return Voovv + ((m == 2 ? (int64_t)j : (int64_t)i) * no + (m == 0 ? j : k)) * nv2;
   };
-  for (int e = threadIdx.x; e < 3 * 6 * ET * ET; e += blockDim.x) {
-    const int m = e / (6 * ET * ET), rem = e - m * (6 * ET * ET);
-    const int pid = rem / (ET * ET), x = (rem / ET) % ET, y = rem % ET;
-    const int u = pid / 2, v0 = pid % 2, v = v0 < u ? v0 : v0 + 1;  // ordered role pair (u, v), u != v
+  // element tid + TNT*it: matrix m = it / 3, role pair pid = 2 (it % 3) + tx, row ty, column tz
+#pragma unroll
+  for (int it = 0; it < 3 * 6 * ET * ET / TNT; it++) {
+    const int m = it / 3, u = it % 3, v0 = tx, pid = 2 * u + v0, x = ty, y = tz;
+    const int v = v0 < u ? v0 : v0 + 1;  // ordered role pair (u, v), u != v
     const int gx = R0(u) + x, gy = R0(v) + y;
     Vs[m][pid][x][y] = (gx < nv && gy < nv) ? (float)Vm(m)[(int64_t)gx * nv + gy] : 0.f;
   }
@@ -920,8 +928,9 @@ __global__ void __launch_bounds__(128) triples_energy_f32_tiled_kernel(int no, i
     return num * inv[(g0 == g1) + (g0 == g2) + (g1 == g2)];
   };
   double s = 0.0;
-  for (int q = threadIdx.x; q < ET * ET * ET; q += blockDim.x) {
-    const int la = q / (ET * ET), lb = (q / ET) % ET, lc = q % ET;
+#pragma unroll
+  for (int it = 0; it < ET * ET * ET / TNT; it++) {
+    const int la = tx + 2 * it, lb = ty, lc = tz;
     const int a = Ra + la, b = Rb + lb, c = Rc + lc;
     if (a >= nv || b > a || c > b) continue;
     const float wabc = Ws[0][la][lb][lc], wacb = Ws[1][la][lc][lb], wbac = Ws[2][lb][la][lc];
@@ -1084,7 +1093,7 @@ void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples,
   Scratch dtri(c, sizeof(int) * tri.size());
   UCC_CUDA(cudaMemcpyAsync(dtri.p, tri.data(), sizeof(int) * tri.size(), cudaMemcpyHostToDevice, c.stream));
   dim3 grid((unsigned)tri.size(), (unsigned)ntuple);
-  triples_energy_f32_tiled_kernel<<<grid, 128, 0, c.stream>>>(no, nv, d_tuples, static_cast<const int*>(dtri.p),
+  triples_energy_f32_tiled_kernel<<<grid, TNT, 0, c.stream>>>(no, nv, d_tuples, static_cast<const int*>(dtri.p),
                                                              (int)tri.size(), W3, t1, Voovv, eps, d_partial);
   count_launch();
   check_launch("triples_energy_f32");
