@@ -332,8 +332,8 @@ struct PermArgs {
 };
 
 // Index arithmetic runs in 32 bits (I = uint32_t) whenever every element count and offset
-// fits: a 64-bit division is a long software sequence, and with one per axis per element
-// the index math, not HBM, bounded these kernels.
+// fits.  The general kernel decomposes every element's index (a division per axis); merged
+// axes shorten that, and the row kernel below pays it once per row.
 template <class I>
 __global__ void permute_kernel_elem(PermArgs a) {
   I od[kMaxRank], is[kMaxRank], os[kMaxRank];

@@ -1497,7 +1497,7 @@ __global__ void split_into_kernel(int64_t rows, int64_t cols, const double* src,
   for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
     const int64_t r = r0 + yy, k = k0 + threadIdx.x;
     if (r < rows && k < cols) {
-      // in FP32 from the truncated value (2^-23, below the lo part's 2^-18): no FP64 pipe work
+      // in FP32 from the truncated value (2^-23, below the lo part's 2^-17): no FP64 pipe work
       const float f = f64_to_f32_trunc(t[threadIdx.x][yy]);
       const __nv_bfloat16 h = __float2bfloat16_rn(f);
       const int64_t o = (row0 + r) * ld + col0 + k;
