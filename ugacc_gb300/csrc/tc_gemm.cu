@@ -864,17 +864,40 @@ __global__ void slice_digits_kernel(MatView x, int64_t rows_p, int64_t kp, const
     if (k == 0 && r < rows) e_out[r] = e;
     long long X = r < rows ? slice_fixed(t[i][tx], e, SB * S) : 0;
     __nv_bfloat16* dst = slices + (size_t)r * kp + k;
-    for (int s = S - 1; s >= 0; s--) {
-      long long d;
-      if (s > 0) {
-        constexpr long long H = 1ll << (SB - 1);
-        d = ((X + H) & (2 * H - 1)) - H;  // balanced digit in [-H, H)
-        X = (X - d) >> SB;
-      } else {
-        d = X;  // what remains: |d| <= H
+    constexpr int H = 1 << (SB - 1);
+    // digit s (|d| <= 2^(SB-1)): a 32-bit conversion, exact, and exact in bf16 after the
+    // power-of-2 scale
+    auto put = [&](int s, int d) {
+      dst[(size_t)s * plane] = __float2bfloat16_rn((float)d * __int_as_float((127 - SB * (s + 1)) << 23));
+    };
+    if (S >= 6) {
+      // balanced digits in 32-bit arithmetic: the low 30 bits hold the 5 least significant
+      // digits, whose carry out (0 or 1) joins the high part for the other S - 5
+      int lo = (int)(X & 0x3FFFFFFFll), hi = (int)(X >> 30);
+      int s = S - 1;
+      for (int q = 0; q < 5; q++, s--) {
+        const int d = ((lo + H) & (2 * H - 1)) - H;  // balanced digit in [-H, H)
+        lo = (lo - d) >> SB;
+        put(s, d);
       }
-      // |d| <= 2^(SB-1): a 32-bit conversion, exact, and exact in bf16 after the power-of-2 scale
-      dst[(size_t)s * plane] = __float2bfloat16_rn((float)(int)d * __int_as_float((127 - SB * (s + 1)) << 23));
+      hi += lo;
+      for (; s > 0; s--) {
+        const int d = ((hi + H) & (2 * H - 1)) - H;
+        hi = (hi - d) >> SB;
+        put(s, d);
+      }
+      put(0, hi);  // what remains: |d| <= H
+    } else {
+      for (int s = S - 1; s >= 0; s--) {
+        long long d;
+        if (s > 0) {
+          d = ((X + H) & (2 * H - 1)) - H;  // balanced digit in [-H, H)
+          X = (X - d) >> SB;
+        } else {
+          d = X;  // what remains: |d| <= H
+        }
+        put(s, (int)d);
+      }
     }
   }
 }
