@@ -68,3 +68,50 @@ def test_truncated_order_sum_is_fp64_accurate():
     ref = A @ B.T
     scale = np.abs(A).max(axis=1)[:, None] * np.abs(B).max(axis=1)[None, :]
     assert np.all(np.abs(got - ref) <= 1e-14 * np.sqrt(2000) * scale)
+
+
+def _digits_64(X, S):
+    """slice_digits_kernel's balanced base-2^SB digits of one integer, least significant
+    first extracted (tc_gemm.cu, 64-bit form)."""
+    H, out = 1 << (SB - 1), [0] * S
+    for s in range(S - 1, -1, -1):
+        if s > 0:
+            d = ((X + H) & (2 * H - 1)) - H
+            X = (X - d) >> SB
+        else:
+            d = X
+        out[s] = d
+    return out
+
+
+def _digits_32(X, S):
+    """The same in 32-bit parts (the kernel's form for S >= 6): the low 30 bits give the 5
+    least significant digits and a carry of 0 or 1 into the high part."""
+    H, out = 1 << (SB - 1), [0] * S
+    lo, hi = X & ((1 << 30) - 1), X >> 30
+    s = S - 1
+    for _ in range(5):
+        d = ((lo + H) & (2 * H - 1)) - H
+        lo = (lo - d) >> SB
+        out[s] = d
+        s -= 1
+    assert lo in (0, 1)
+    hi += lo
+    for s in range(s, 0, -1):
+        d = ((hi + H) & (2 * H - 1)) - H
+        hi = (hi - d) >> SB
+        out[s] = d
+    out[0] = hi
+    for v in [lo, hi] + out:
+        assert -(2 ** 31) <= v < 2 ** 31  # every intermediate fits an int
+    return out
+
+
+def test_32bit_digit_extraction_equals_the_64bit_form():
+    rng = np.random.default_rng(5)
+    for S in (6, 7, 8, 9):
+        lim = 1 << (SB * S - 1)
+        xs = [0, 1, -1, lim - 1, -(lim - 1), 2 ** 30, -(2 ** 30), 2 ** 30 - 1, -(2 ** 29) - 1]
+        xs += [int(v) for v in rng.integers(-lim + 1, lim, size=20000)]
+        for X in xs:
+            assert _digits_32(X, S) == _digits_64(X, S), (S, X)
