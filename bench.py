@@ -154,6 +154,20 @@ def cpu_oracle_sample(h, iters: int = 1):
     return times
 
 
+def recorded_reference_run() -> dict:
+    """The reference's own compiled loops on this workload, as recorded with the golden
+    fixture (tests/golden/c2.json: one single-core x86 run); empty when absent."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "c2.json")
+    if WORKLOAD != "ccsd_t_no16_nv160_seed1" or not os.path.exists(path):
+        return {}
+    run = json.load(open(path))["runs"]["ccsd_t"]
+    it = len(run["tables"]["ccsd"])  # iterations 0 (MP2) ... n-1 printed; the converging one is not
+    return {"reference_binary_recorded": {
+        "ccsd_s": run["ccsd_s"], "triples_s": run["t_tjl_s"], "ccsd_iterations": it, "cores": 1,
+        "e_ccsd": run["e_ccsd"], "e_t": run["e_t_tjl"],
+        "source": "tests/golden/c2.json (the reference sources compiled by oracle/Makefile, one x86 core)"}}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -172,7 +186,7 @@ def run_reference(args, rank):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": WORKLOAD, "step": "one CCSD iteration (residual + Jacobi update)",
-                       "l2": "inputs larger than L2"},
+                       "l2": "inputs larger than L2", **recorded_reference_run()},
             "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port",
                              "sample": "numpy oracle: one CCSD iteration at no=%d/nv=%d per step" % (NO, NV)},
             "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
