@@ -77,10 +77,12 @@ ucc_status ucc_load_hamiltonian_df(ucc_ctx* ctx, int no, int nv, int naux, const
  * for hosts with MO integrals in a file instead of psi4's libtrans.  The file has the
  * FCIDUMP layout: a header "&FCI NORB=n, NELEC=N, MS2=0, ... &END" (or a "/" line), then
  * lines "value i j k l" with (ij|kl) over real orbitals (1-based, any of the 8 equivalent
- * orders), "value i j 0 0" = h_ij, "value 0 0 0 0" = nuclear repulsion ("value i 0 0 0",
- * orbital energies, is ignored).  Orbitals are taken in the file's order, the first
- * NELEC/2 doubly occupied; the first nfzc are frozen core and the last nfzv frozen
- * virtuals (hamiltonian.cc:24-27).  Host code only: no context and no device needed.
+ * orders), "value i j 0 0" = h_ij, "value i 0 0 0" = orbital energy, "value 0 0 0 0" =
+ * nuclear repulsion.  With an energy for every orbital, the NELEC/2 lowest are doubly
+ * occupied and the orbitals go to QT order (occupied, then virtual, each by ascending
+ * energy); otherwise the file's order is taken with the first NELEC/2 occupied.  The first
+ * nfzc orbitals of that order are frozen core and the last nfzv frozen virtuals
+ * (hamiltonian.cc:24-27).  Host code only: no context and no device needed.
  *   ucc_fcidump_dims: NORB and NELEC of the header.
  *   ucc_fcidump_read: fock [nact][nact] (the determinant's Fock matrix over the active
  *     orbitals, QT order, hamiltonian.cc:43-56), ints [nact]^4 with ints[p][q][r][s] =

@@ -21,9 +21,15 @@ def fock_full(h: np.ndarray, eri: np.ndarray, nocc: int) -> np.ndarray:
     return h + 2.0 * J - K
 
 
-def hamiltonian(h, eri, enuc, nocc, nfzc=0, nfzv=0):
-    """(fock_active, ints_active, enuc, efzc, escf) from full h [n][n], eri [n]^4 = (pq|rs)."""
+def hamiltonian(h, eri, enuc, nocc, nfzc=0, nfzv=0, orbital_energies=None):
+    """(fock_active, ints_active, enuc, efzc, escf) from full h [n][n], eri [n]^4 = (pq|rs).
+    With ``orbital_energies`` the orbitals are first put in ascending-energy order (stable),
+    which puts the nocc lowest (occupied) first, as the file reader does."""
     n = h.shape[0]
+    if orbital_energies is not None:
+        qt = np.argsort(np.asarray(orbital_energies), kind="stable")
+        h = h[np.ix_(qt, qt)]
+        eri = eri[np.ix_(qt, qt, qt, qt)]
     F = fock_full(h, eri, nocc)
     c = slice(0, nfzc)
     efzc = 2.0 * np.trace(h[c, c]) + 2.0 * np.einsum("iijj->", eri[c, c, c, c]) - np.einsum("ijji->", eri[c, c, c, c])

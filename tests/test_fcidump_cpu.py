@@ -113,3 +113,30 @@ def test_driver_rejects_frozen_orbitals_past_the_occupied_space(tmp_path):
     FD.write(path, h, eri, enuc, 6)
     r = subprocess.run([DRIVER, path, "NFZC=3"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "no active" in r.stderr
+
+
+def test_orbital_energies_put_irrep_grouped_files_in_qt_order(tmp_path):
+    """A file whose orbitals are listed out of energy order (as symmetry-using programs
+    group them by irrep), with an energy line for every orbital, reads as the same
+    Hamiltonian as the energy-ordered file; without energy lines the file order is kept."""
+    n, nelec = 10, 8
+    h, eri, enuc = _random_system(n, 4, 21)
+    eps = np.sort(np.random.default_rng(3).uniform(-2.0, 3.0, n))
+    ordered = str(tmp_path / "ordered")
+    FD.write(ordered, h, eri, enuc, nelec, orbital_energies=eps)
+    perm = np.array([0, 4, 8, 1, 5, 9, 2, 6, 3, 7])  # "irreps" {0,4,8}, {1,5,9}, {2,6}, {3,7}
+    hp, ep = h[np.ix_(perm, perm)], eps[perm]
+    erip = eri[np.ix_(perm, perm, perm, perm)]
+    grouped = str(tmp_path / "grouped")
+    FD.write(grouped, hp, erip, enuc, nelec, orbital_energies=ep, scramble=True, seed=2)
+    for nfzc, nfzv in [(0, 0), (1, 2)]:
+        a, b = U.read_fcidump(ordered, nfzc, nfzv), U.read_fcidump(grouped, nfzc, nfzv)
+        np.testing.assert_allclose(b["fock"], a["fock"], atol=1e-13, rtol=0)
+        np.testing.assert_allclose(b["ints"], a["ints"], atol=1e-14, rtol=0)
+        assert abs(a["escf"] - b["escf"]) < 1e-12 and abs(a["efzc"] - b["efzc"]) < 1e-12
+        ref = FD.hamiltonian(hp, erip, enuc, 4, nfzc, nfzv, orbital_energies=ep)
+        np.testing.assert_allclose(b["fock"], ref[0], atol=1e-13, rtol=0)
+    no_e = str(tmp_path / "no_energies")
+    FD.write(no_e, hp, erip, enuc, nelec)
+    c = U.read_fcidump(no_e)
+    np.testing.assert_allclose(c["fock"], FD.hamiltonian(hp, erip, enuc, 4)[0], atol=1e-13, rtol=0)

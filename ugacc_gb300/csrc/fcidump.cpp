@@ -12,20 +12,27 @@
 //   body     value i j k l    i,j,k,l >= 1: (ij|kl), real orbitals, any one of the 8
 //                             equivalent index orders
 //            value i j 0 0    h_ij (one-electron operator, symmetric)
-//            value i 0 0 0    orbital energy (not needed, ignored)
+//            value i 0 0 0    orbital energy
 //            value 0 0 0 0    nuclear repulsion energy
 //   values may use a Fortran D exponent (1.0D-02).
 //
-// Orbitals are taken in the file's order with the first NELEC/2 doubly occupied (an
-// energy-ordered closed-shell file); the first nfzc are frozen core and the last nfzv
-// frozen virtuals.  With all occupied orbitals first, the QT order of the reference's
-// reorder_qt (frozen docc, docc, virtuals, frozen virtuals) is the file order.
+// Orbital order: when every orbital has an energy line, the NELEC/2 lowest are doubly
+// occupied and the orbitals are put in QT order, occupied then virtual, each by ascending
+// energy (a stable sort: an energy-ordered file keeps its order; files grouped by irrep,
+// as symmetry-using programs write them, are regrouped).  Otherwise the file's order is
+// taken with the first NELEC/2 occupied.  The first nfzc orbitals of that order are
+// frozen core and the last nfzv frozen virtuals.  The reference's reorder_qt (frozen
+// docc, docc, virtuals, frozen virtuals, hamiltonian.cc:40-41) also orders each class by
+// irrep; the CC energies do not depend on the order within the occupied or the virtual
+// space.
 #include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <algorithm>
+#include <numeric>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -137,6 +144,8 @@ bool next_number(const char*& p, const char* end, double& v, std::string& tmp) {
 struct Integrals {
   int n = 0;
   std::vector<double> h, eri;  // h[n][n]; eri[n][n][n][n] = (pq|rs)
+  std::vector<double> eorb;    // orbital energies, when given
+  std::vector<char> has_e;
   double enuc = 0.0;
   double& g(int p, int q, int r, int s) { return eri[(((size_t)p * n + q) * n + r) * n + s]; }
 };
@@ -145,6 +154,8 @@ void read_body(const std::string& text, size_t off, Integrals& I) {
   const int n = I.n;
   I.h.assign((size_t)n * n, 0.0);
   I.eri.assign((size_t)n * n * n * n, 0.0);
+  I.eorb.assign(n, 0.0);
+  I.has_e.assign(n, 0);
   const char* p = text.data() + off;
   const char* end = text.data() + text.size();
   std::string tmp;
@@ -170,7 +181,8 @@ void read_body(const std::string& text, size_t off, Integrals& I) {
     } else if (!x[0] && !x[1] && !x[2] && !x[3]) {
       I.enuc = v;
     } else if (x[0] && !x[1] && !x[2] && !x[3]) {
-      // orbital energy: not needed
+      I.eorb[i] = v;
+      I.has_e[i] = 1;
     } else {
       throw DumpError(UCC_BAD_ARGS, "fcidump: unrecognised index pattern");
     }
@@ -230,23 +242,32 @@ ucc_status ucc_fcidump_read(const char* path, int nfzc, int nfzv, double* fock, 
     Integrals I;
     I.n = n;
     read_body(text, hd.body, I);
-    // Fock matrix of the determinant with orbitals 0..nocc-1 doubly occupied (frozen core
-    // included): F_pq = h_pq + sum_k [2 (pq|kk) - (pk|kq)]
+    // qt[P] = the file's orbital at QT position P
+    std::vector<int> qt(n);
+    std::iota(qt.begin(), qt.end(), 0);
+    if (std::all_of(I.has_e.begin(), I.has_e.end(), [](char c) { return c != 0; })) {
+      std::stable_sort(qt.begin(), qt.end(), [&](int a, int b) { return I.eorb[a] < I.eorb[b]; });
+      // (ascending energy: the NELEC/2 lowest come first, each class stays in energy order)
+    }
+    auto h = [&](int p, int q) { return I.h[(size_t)qt[p] * n + qt[q]]; };
+    auto g = [&](int p, int q, int r, int s) { return I.g(qt[p], qt[q], qt[r], qt[s]); };
+    // Fock matrix of the determinant with QT orbitals 0..nocc-1 doubly occupied (frozen
+    // core included): F_pq = h_pq + sum_k [2 (pq|kk) - (pk|kq)]
     std::vector<double> F((size_t)n * n);
     for (int p = 0; p < n; p++)
       for (int q = 0; q < n; q++) {
-        double s = I.h[(size_t)p * n + q];
-        for (int k = 0; k < nocc; k++) s += 2.0 * I.g(p, q, k, k) - I.g(p, k, k, q);
+        double s = h(p, q);
+        for (int k = 0; k < nocc; k++) s += 2.0 * g(p, q, k, k) - g(p, k, k, q);
         F[(size_t)p * n + q] = s;
       }
     // frozen-core energy: sum_i [2 h_ii + sum_j (2 (ii|jj) - (ij|ji))] over frozen i, j
     double efzc = 0.0;
     for (int i = 0; i < nfzc; i++) {
-      efzc += 2.0 * I.h[(size_t)i * n + i];
-      for (int j = 0; j < nfzc; j++) efzc += 2.0 * I.g(i, i, j, j) - I.g(i, j, j, i);
+      efzc += 2.0 * h(i, i);
+      for (int j = 0; j < nfzc; j++) efzc += 2.0 * g(i, i, j, j) - g(i, j, j, i);
     }
     double escf = I.enuc;
-    for (int k = 0; k < nocc; k++) escf += I.h[(size_t)k * n + k] + F[(size_t)k * n + k];
+    for (int k = 0; k < nocc; k++) escf += h(k, k) + F[(size_t)k * n + k];
     const int a0 = nfzc, na = n - nfzc - nfzv;
     for (int p = 0; p < na; p++)
       for (int q = 0; q < na; q++) fock[(size_t)p * na + q] = F[(size_t)(a0 + p) * n + a0 + q];
@@ -255,7 +276,7 @@ ucc_status ucc_fcidump_read(const char* path, int nfzc, int nfzv, double* fock, 
       for (int q = 0; q < na; q++)
         for (int r = 0; r < na; r++)
           for (int s = 0; s < na; s++)
-            ints[(((size_t)p * na + q) * na + r) * na + s] = I.g(a0 + p, a0 + r, a0 + q, a0 + s);
+            ints[(((size_t)p * na + q) * na + r) * na + s] = g(a0 + p, a0 + r, a0 + q, a0 + s);
     energies[0] = I.enuc;
     energies[1] = efzc;
     energies[2] = escf;
