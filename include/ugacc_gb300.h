@@ -87,12 +87,15 @@ ucc_status ucc_load_hamiltonian_df(ucc_ctx* ctx, int no, int nv, int naux, const
  *   ucc_fcidump_read: fock [nact][nact] (the determinant's Fock matrix over the active
  *     orbitals, QT order, hamiltonian.cc:43-56), ints [nact]^4 with ints[p][q][r][s] =
  *     <pq|rs> = (pr|qs) (hamiltonian.cc:76-91), energies[3] = {nuclear repulsion,
- *     frozen-core energy (hamiltonian.cc:72), SCF energy}; nact = NORB - nfzc - nfzv,
- *     no = NELEC/2 - nfzc.  Closed-shell files only (UCC_UNSUPPORTED otherwise).
+ *     frozen-core energy (hamiltonian.cc:72), SCF energy}, order [nact] (may be null) the
+ *     file's 0-based orbital at each active QT position, for cutting the same block out
+ *     of the host's own MO-basis matrices (e.g. the perturbations of ucc_pert_create);
+ *     nact = NORB - nfzc - nfzv, no = NELEC/2 - nfzc.  Closed-shell files only
+ *     (UCC_UNSUPPORTED otherwise).
  * Errors are written to err (errlen bytes, may be null). */
 ucc_status ucc_fcidump_dims(const char* path, int* norb, int* nelec, char* err, size_t errlen);
 ucc_status ucc_fcidump_read(const char* path, int nfzc, int nfzv, double* fock, double* ints, double* energies,
-                            char* err, size_t errlen);
+                            int* order, char* err, size_t errlen);
 
 /* Replaces: CCWfn::CCWfn + CCWfn::compute_energy, CCSD part (ccwfn.cc:12-120, :188-235).
  * e_ccsd is the energy of the amplitudes before the final update, as the reference

@@ -67,11 +67,13 @@ class Hamiltonian {
     const int nact = norb - nfzc - nfzv, no = nelec / 2 - nfzc;
     if (nact <= 0 || no <= 0 || no >= nact) throw Error(UCC_BAD_ARGS, "fcidump: frozen orbitals leave no active space");
     std::vector<double> fock((size_t)nact * nact), ints((size_t)nact * nact * nact * nact);
+    std::vector<int> order(nact);
     double en[3];
-    st = ucc_fcidump_read(path.c_str(), nfzc, nfzv, fock.data(), ints.data(), en, err, sizeof err);
+    st = ucc_fcidump_read(path.c_str(), nfzc, nfzv, fock.data(), ints.data(), en, order.data(), err, sizeof err);
     if (st != UCC_OK) throw Error(st, err);
     auto H = std::make_shared<Hamiltonian>(no, nact - no, fock.data(), ints.data(), device);
     H->enuc_ = en[0], H->efzc_ = en[1], H->escf_ = en[2];
+    H->order_ = std::move(order);
     return H;
   }
   ~Hamiltonian() { ucc_ctx_destroy(ctx_); }
@@ -83,11 +85,14 @@ class Hamiltonian {
   double enuc() const { return enuc_; }
   double efzc() const { return efzc_; }
   double escf() const { return escf_; }
+  // from_fcidump: the file's orbital at each active QT position
+  const std::vector<int>& orbital_order() const { return order_; }
 
  private:
   ucc_ctx* ctx_ = nullptr;
   int no_, nv_;
   double enuc_ = 0.0, efzc_ = 0.0, escf_ = 0.0;
+  std::vector<int> order_;
 };
 
 class CCWfn {

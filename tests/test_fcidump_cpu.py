@@ -40,6 +40,7 @@ def test_active_hamiltonian_matches_oracle(tmp_path, nfzc, nfzv):
     np.testing.assert_allclose(got["ints"], ints, atol=1e-14, rtol=0)
     assert got["enuc"] == enuc
     assert abs(got["efzc"] - efzc) < 1e-12 and abs(got["escf"] - escf) < 1e-12
+    assert list(got["order"]) == list(range(nfzc, n - nfzv))  # no energies: the file order
     if nfzc == 0:
         assert got["efzc"] == 0.0
 
@@ -136,6 +137,11 @@ def test_orbital_energies_put_irrep_grouped_files_in_qt_order(tmp_path):
         assert abs(a["escf"] - b["escf"]) < 1e-12 and abs(a["efzc"] - b["efzc"]) < 1e-12
         ref = FD.hamiltonian(hp, erip, enuc, 4, nfzc, nfzv, orbital_energies=ep)
         np.testing.assert_allclose(b["fock"], ref[0], atol=1e-13, rtol=0)
+        # order maps each active QT orbital to the grouped file's orbital: a file-ordered
+        # matrix cut with it equals the energy-ordered file's active block
+        order = b["order"]
+        assert np.array_equal(ep[order], eps[nfzc:n - nfzv])
+        np.testing.assert_allclose(hp[np.ix_(order, order)], h[nfzc:n - nfzv, nfzc:n - nfzv], atol=0, rtol=0)
     no_e = str(tmp_path / "no_energies")
     FD.write(no_e, hp, erip, enuc, nelec)
     c = U.read_fcidump(no_e)

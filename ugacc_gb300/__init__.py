@@ -139,7 +139,7 @@ def load_library(path: str | None = None):
         "ucc_batch_get_t2": (i, [vp, i, dp, ctypes.c_size_t]),
         "ucc_batch_features": (i, [vp, i, fp, ctypes.c_size_t, i, fp]),
         "ucc_fcidump_dims": (i, [cp, P(i), P(i), cp, ctypes.c_size_t]),
-        "ucc_fcidump_read": (i, [cp, i, i, dp, dp, dp, cp, ctypes.c_size_t]),
+        "ucc_fcidump_read": (i, [cp, i, i, dp, dp, dp, P(i), cp, ctypes.c_size_t]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -230,7 +230,9 @@ def read_fcidump(path: str, nfzc: int = 0, nfzv: int = 0) -> dict:
     no GPU): the integral side of hamiltonian.cc:21-102 with ``nfzc`` frozen core and
     ``nfzv`` frozen virtual orbitals (orbitals in the file's order, the first NELEC/2
     doubly occupied).  Returns ``no``, ``nv``, ``fock`` [nact][nact], ``ints`` [nact]^4
-    (``ints[p,q,r,s] = <pq|rs>``), ``enuc``, ``efzc`` (frozen-core energy) and ``escf``."""
+    (``ints[p,q,r,s] = <pq|rs>``), ``enuc``, ``efzc`` (frozen-core energy), ``escf`` and
+    ``order`` (the file's 0-based orbital at each active QT position: a file-ordered MO
+    matrix ``P`` becomes ``P[np.ix_(order, order)]`` on the active space)."""
     lib = load_library()
     err = ctypes.create_string_buffer(512)
     norb, nelec = ctypes.c_int(), ctypes.c_int()
@@ -244,12 +246,14 @@ def read_fcidump(path: str, nfzc: int = 0, nfzv: int = 0) -> dict:
     fock = np.empty((nact, nact))
     ints = np.empty((nact,) * 4)
     en = np.empty(3)
-    st = lib.ucc_fcidump_read(bpath, nfzc, nfzv, _ptr(fock), _ptr(ints), _ptr(en), err, 512)
+    order = np.empty(nact, dtype=np.int32)
+    st = lib.ucc_fcidump_read(bpath, nfzc, nfzv, _ptr(fock), _ptr(ints), _ptr(en),
+                              order.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), err, 512)
     if st:
         raise UccError(st, err.value.decode())
     no = nelec.value // 2 - nfzc
     return {"no": no, "nv": nact - no, "fock": fock, "ints": ints, "enuc": float(en[0]), "efzc": float(en[1]),
-            "escf": float(en[2])}
+            "escf": float(en[2]), "order": order}
 
 
 class Hamiltonian:
@@ -281,7 +285,7 @@ class Hamiltonian:
         energies are kept as ``enuc``, ``efzc`` and ``escf``."""
         d = read_fcidump(path, nfzc, nfzv)
         H = cls(d["no"], d["nv"], d["fock"], ints=d["ints"], **kw)
-        H.enuc, H.efzc, H.escf = d["enuc"], d["efzc"], d["escf"]
+        H.enuc, H.efzc, H.escf, H.order = d["enuc"], d["efzc"], d["escf"], d["order"]
         return H
 
     @classmethod

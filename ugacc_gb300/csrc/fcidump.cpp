@@ -228,7 +228,7 @@ ucc_status ucc_fcidump_dims(const char* path, int* norb, int* nelec, char* err, 
 }
 
 ucc_status ucc_fcidump_read(const char* path, int nfzc, int nfzv, double* fock, double* ints, double* energies,
-                            char* err, size_t errlen) {
+                            int* order, char* err, size_t errlen) {
   return dump_guard(err, errlen, [&] {
     if (!fock || !ints || !energies) throw DumpError(UCC_BAD_ARGS, "fcidump: null output");
     const std::string text = read_file(path);
@@ -277,6 +277,8 @@ ucc_status ucc_fcidump_read(const char* path, int nfzc, int nfzv, double* fock, 
         for (int r = 0; r < na; r++)
           for (int s = 0; s < na; s++)
             ints[(((size_t)p * na + q) * na + r) * na + s] = g(a0 + p, a0 + r, a0 + q, a0 + s);
+    if (order)  // the file's (0-based) orbital at each active QT position
+      for (int p = 0; p < na; p++) order[p] = qt[a0 + p];
     energies[0] = I.enuc;
     energies[1] = efzc;
     energies[2] = escf;
