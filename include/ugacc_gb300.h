@@ -139,6 +139,14 @@ ucc_status ucc_linresp(ucc_ctx* ctx, int handle_x, int handle_y, double* value);
 ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t M, int64_t N, int64_t K,
                     double alpha, const double* A, const double* B, double beta, double* C);
 
+/* Failure-detection self-test (no counterpart in the reference, which has no device
+ * code).  Every wait inside the tensor-core pipelines is bounded: when one runs out the
+ * kernel raises a device flag and returns, and the call reports UCC_DEVICE_TIMEOUT.  This
+ * entry point runs that path on purpose: one thread waits limit_ns (1 us to 10 s) on a
+ * barrier that nothing completes.  Expected result: UCC_DEVICE_TIMEOUT, with the context
+ * and its stream still usable for the next call. */
+ucc_status ucc_wait_selftest(ucc_ctx* ctx, uint64_t limit_ns);
+
 /* (T) correction computed without allocating any device memory.  No counterpart in the
  * reference: it serves host programs that cannot let a library call cudaMalloc (all
  * device memory belongs to their own arena, or must not be allocated on this path).
@@ -148,15 +156,19 @@ ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t
  * 32 MiB device array per GPU: nv^3 + nv * no(no+1)(no+2)/6 doubles must fit, otherwise
  * UCC_BAD_ARGS with a message in errbuf.  Calls share that array: do not let two calls
  * overlap on the GPU.  The first call on a device looks up the array's address; make it
- * before any stream capture.  stream may be NULL; the call returns after the result is
- * on the host. */
+ * before any stream capture.  Under CUDA's lazy module loading (the default) that first
+ * call is also when the device reserves the 32 MiB, so a host whose own pool claims the
+ * device memory should make it before the pool does.  stream may be NULL; the call
+ * returns after the result is on the host. */
 ucc_status ucc_triples_noalloc(int no, int nv, const double* t1, const double* t2, const double* eps,
                                const double* ovvv, const double* ooov, const double* oovv, double* e_t,
                                void* stream, char* errbuf, size_t errlen);
 
 /* Copy-out of named arrays: "t1" "t2" "tau" "l1" "l2" "Doo" "Dvv" "Dov" "Dvo" and the
  * HBAR blocks "Hov" "Hoo" "Hvv" "Hoooo" "Hvvvv" "Hvovv" "Hooov" "Hovvo" "Hovov" "Hvvvo"
- * "Hovoo"; per perturbation "X1:<h>" "X2:<h>" "Y1:<h>" "Y2:<h>".  count = elements. */
+ * "Hovoo"; per perturbation "X1:<h>" "X2:<h>" "Y1:<h>" "Y2:<h>"; "t2_guess", the T2
+ * starting amplitudes the next ucc_ccsd will use (after ucc_mlp_guess or a "t2" copy-in).
+ * count = elements. */
 ucc_status ucc_get_tensor(ucc_ctx* ctx, const char* name, double* host_out, size_t count);
 /* Copy-in (restart files, learned guesses): "t1" "t2" "l1" "l2". */
 ucc_status ucc_set_tensor(ucc_ctx* ctx, const char* name, const double* host_in, size_t count);
@@ -187,7 +199,11 @@ ucc_status ucc_mlp_train(ucc_mlp* net, const float* X, const float* t, int64_t r
                          uint64_t seed, float* final_loss);
 /* features (and, after a converged ucc_ccsd, targets) of the loaded Hamiltonian */
 ucc_status ucc_mlp_features(ucc_ctx* ctx, float* X, size_t rows, int with_targets, float* targets);
-/* the next ucc_ccsd on ctx starts from t1 = f_ia/D1, t2 = t2_MP2 + prediction/S */
+/* the next ucc_ccsd on ctx starts from t1 = f_ia/D1, t2 = t2_MP2 + prediction/T.  One
+ * fused pass on the tensor cores: per 128 doubles elements the features and the first
+ * layer (FP32), the second layer as a tcgen05 MMA chain (FP16 activations and weights,
+ * FP32 accumulation in tensor memory) and the output layer in the epilogue; no feature
+ * or activation array is written to device memory. */
 ucc_status ucc_mlp_guess(ucc_ctx* ctx, ucc_mlp* net);
 
 /* Per-stage device timings (CUDA events on the library's stream) and FLOP counts. */

@@ -97,6 +97,14 @@ class Hamiltonian {
 
 class CCWfn {
  public:
+  // ccwfn.h:14 takes the reference (SCF) wavefunction first; everything this class needs
+  // from it is in the Hamiltonian, so it is only kept alive alongside, as the reference's
+  // set_reference_wavefunction keeps it
+  template <typename Ref>
+  CCWfn(std::shared_ptr<Ref> reference, std::shared_ptr<Hamiltonian> H, const Options& o)
+      : CCWfn(std::move(H), o) {
+    ref_ = std::move(reference);
+  }
   CCWfn(std::shared_ptr<Hamiltonian> H, const Options& o) : H_(std::move(H)), opt_(o) {
     ucc_options u;
     ucc_options_default(&u);
@@ -138,6 +146,7 @@ class CCWfn {
 
  private:
   std::shared_ptr<Hamiltonian> H_;
+  std::shared_ptr<void> ref_;
   Options opt_;
   double eccsd_ = 0.0, et_ = 0.0;
 };
@@ -197,31 +206,53 @@ enum hand { left, right };  // ccpert.h:15
 
 class CCPert {
  public:
+  // ccpert.h:19: the perturbation as the reference passes it, nact row pointers of nact
+  // elements each (pert[p][q], QT order)
+  CCPert(double** pert, double omega, std::shared_ptr<CCWfn> CC, std::shared_ptr<HBAR> hbar,
+         std::shared_ptr<CCLambda> lam)
+      : CCPert(rows_to_dense(pert, CC).data(), omega, CC, std::move(hbar), std::move(lam)) {}
+  // the same matrix stored contiguously, [nact][nact]
   CCPert(const double* pert, double omega, std::shared_ptr<CCWfn> CC, std::shared_ptr<HBAR> hbar,
          std::shared_ptr<CCLambda> lam)
       : CC_(std::move(CC)), HBAR_(std::move(hbar)), L_(std::move(lam)), omega_(omega) {
     check(CC_->H()->ctx(), ucc_pert_create(CC_->H()->ctx(), pert, omega, &handle_));
   }
-  double solve(hand h) {  // ccpert.cc:177-229
-    double pr = 0.0;
+  // ccpert.h:21 / ccpert.cc:177-229: converge the right-hand (X) or left-hand (Y)
+  // perturbed amplitudes; throws ConvergenceError like the reference
+  void solve(hand h) {
     int it = 0;
-    check(CC_->H()->ctx(), ucc_pert_solve(CC_->H()->ctx(), handle_, h == right ? 1 : 0, &pr, &it));
-    return pr;
+    const int k = h == right ? 1 : 0;
+    check(CC_->H()->ctx(), ucc_pert_solve(CC_->H()->ctx(), handle_, k, &pseudo_[k], &it));
   }
+  // ccpert.cc:233-253: the pseudo-response of the last solve of that hand
+  double pseudoresponse(hand h) const { return pseudo_[h == right ? 1 : 0]; }
   int handle() const { return handle_; }
   ucc_ctx* ctx() const { return CC_->H()->ctx(); }
 
  private:
+  static std::vector<double> rows_to_dense(double** pert, const std::shared_ptr<CCWfn>& CC) {
+    if (!pert || !CC) throw Error(UCC_BAD_ARGS, "CCPert: null perturbation or wavefunction");
+    const size_t n = (size_t)CC->H()->no() + (size_t)CC->H()->nv();
+    std::vector<double> d(n * n);
+    for (size_t p = 0; p < n; p++) {
+      if (!pert[p]) throw Error(UCC_BAD_ARGS, "CCPert: null perturbation row");
+      for (size_t q = 0; q < n; q++) d[p * n + q] = pert[p][q];
+    }
+    return d;
+  }
   std::shared_ptr<CCWfn> CC_;
   std::shared_ptr<HBAR> HBAR_;
   std::shared_ptr<CCLambda> L_;
   double omega_;
   int handle_ = -1;
+  double pseudo_[2] = {0.0, 0.0};
 };
 
 class CCResp {
  public:
   CCResp(std::shared_ptr<CCPert> X, std::shared_ptr<CCPert> Y) : X_(std::move(X)), Y_(std::move(Y)) {}
+  // ccresp.h:13: one perturbation on both sides
+  explicit CCResp(std::shared_ptr<CCPert> X) : X_(X), Y_(std::move(X)) {}
   double linresp(const std::shared_ptr<CCPert>& X, const std::shared_ptr<CCPert>& Y) {  // ccresp.cc:28-124
     double v = 0.0;
     check(X->ctx(), ucc_linresp(X->ctx(), X->handle(), Y->handle(), &v));

@@ -38,13 +38,17 @@ def dsilu(z):
     return s * (1.0 + z * (1.0 - s))
 
 
-def forward(p, X, half_weights=True):
+def forward(p, X, half_weights=True, half_activations=False):
+    """half_activations: the first layer's activations rounded to FP16, as the fused
+    tensor-core guess kernel feeds them to its second-layer MMA."""
     q = unpack(p)
     W1, W2, w3 = (q["W1"], q["W2"], q["w3"])
     if half_weights:
         W1, W2, w3 = _fp16(W1), _fp16(W2), _fp16(w3)
     Z1 = X @ W1 + q["b1"]
     A1 = silu(Z1)
+    if half_activations:
+        A1 = _fp16(A1)
     Z2 = A1 @ W2 + q["b2"]
     A2 = silu(Z2)
     y = A2 @ w3 + q["b3"][0]

@@ -8,8 +8,9 @@ and stores what that binary printed and dumped:
                 from the reference's own iteration tables, timings, input checksum
   <case>.npz    selected tensors (float64), small cases only
 
-Needs the reference tree (default /root/reference) and g++; not run by the tests.
-    python tests/golden/make_golden.py [--big] [--only CASE ...]
+Needs the reference tree (``--reference`` or the UGACC_REFERENCE environment variable)
+and g++; not run by the tests.
+    python tests/golden/make_golden.py --reference /path/to/ugacc [--big] [--only CASE ...]
 """
 from __future__ import annotations
 
@@ -128,9 +129,12 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--big", action="store_true", help="also the no=16/nv=160 case (hours)")
     ap.add_argument("--only", nargs="*")
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("UGACC_REFERENCE"),
+                    help="the reference tree (default: $UGACC_REFERENCE)")
     ap.add_argument("--build-dir", default="_ref", help="build directory under oracle/")
     a = ap.parse_args()
+    if not a.reference:
+        ap.error("the reference tree is needed: --reference PATH or UGACC_REFERENCE=PATH")
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REFERENCE={a.reference}", f"OUT={a.build_dir}"],
                    check=True)
     binary = os.path.join(ROOT, "oracle", a.build_dir, "ugacc_ref")

@@ -56,6 +56,33 @@ def test_features_and_targets_match_oracle():
     np.testing.assert_allclose(t, M.targets(no, nv, blocks["oovv"], h.eps, cc.t2), rtol=1e-6, atol=1e-5)
 
 
+@pytest.mark.parametrize("no,nv", [(4, 40), (3, 27)])
+def test_tensor_core_guess_matches_oracle(no, nv):
+    """The fused guess kernel (features, both layers and t2 = t2_mp2 + y/1000 in one pass,
+    second layer on the tensor cores with FP16 activations) against the oracle's forward
+    pass with the same FP16 rounding, and against the FP32 inference path; nv = 27 leaves
+    a partial last tile of 128 elements."""
+    h = make_hamiltonian(no, nv, 3)
+    H = U.Hamiltonian.from_synthetic(h)
+    net = U.MLP(seed=9)
+    net.guess(H)
+    g = H.ctx.get("t2_guess", (no, no, nv, nv))
+    blocks = dict(M.blocks(h.ints_physicist(), no), eps=h.eps)
+    X = M.features(no, nv, blocks)
+    y, _ = M.forward(net.params.astype(np.float64), X, half_activations=True)
+    D = M._denominators(no, nv, h.eps)
+    mp2 = blocks["oovv"] / D
+    dy = (g - mp2).ravel() * M.TARGET - y
+    # tanh-based SiLU (tanh.approx, ~2^-11) and FP32 features: a few 1e-3 of the output scale
+    assert np.abs(dy).max() <= 4e-3 * np.abs(y).max(), (np.abs(dy).max(), np.abs(y).max())
+    y32 = net.predict(U.mlp_features(H))
+    assert np.abs((g - mp2).ravel() * M.TARGET - y32).max() <= 4e-3 * np.abs(y32).max()
+    # the next solve starts from it and the plain iteration decides the answer
+    e_guess = U.CCWfn(H, {"R_CONVERGENCE": 1e-10}).compute_energy()
+    e_mp2 = U.CCWfn(H, {"R_CONVERGENCE": 1e-10}).compute_energy()
+    assert abs(e_guess - e_mp2) < 1e-9
+
+
 def test_training_lowers_the_loss():
     net = U.MLP(seed=1)
     rng = np.random.default_rng(4)

@@ -118,6 +118,7 @@ def load_library(path: str | None = None):
         "ucc_status_string": (cp, [i]),
         "ucc_triples_noalloc": (i, [i, i, vp, vp, vp, vp, vp, vp, dp, vp, cp, ctypes.c_size_t]),
         "ucc_gemm": (i, [vp, i, i, i, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, d, dp, dp, d, dp]),
+        "ucc_wait_selftest": (i, [vp, ctypes.c_uint64]),
         "ucc_mlp_create": (i, [P(vp), i, ctypes.c_uint64]),
         "ucc_mlp_destroy": (i, [vp]),
         "ucc_mlp_last_error": (cp, [vp]),
@@ -197,6 +198,11 @@ class Context:
                                      beta, _ptr(C)))
         return C
 
+    def wait_selftest(self, limit_s: float = 0.05):
+        """Run a bounded device wait that nothing completes (ucc_wait_selftest); raises
+        UccError with status 7 (device timeout) when the failure path works."""
+        self.check(self.lib.ucc_wait_selftest(self.h, int(limit_s * 1e9)))
+
     def stats(self) -> dict:
         s = Stats()
         self.check(self.lib.ucc_get_stats(self.h, ctypes.byref(s)))
@@ -228,8 +234,11 @@ DEFAULT_OPTIONS = {"WFN": "CCSD", "DERTYPE": "NONE", "MAXITER": 100, "R_CONVERGE
 def read_fcidump(path: str, nfzc: int = 0, nfzv: int = 0) -> dict:
     """Active-space Hamiltonian from an MO-integral file in the FCIDUMP layout (host code,
     no GPU): the integral side of hamiltonian.cc:21-102 with ``nfzc`` frozen core and
-    ``nfzv`` frozen virtual orbitals (orbitals in the file's order, the first NELEC/2
-    doubly occupied).  Returns ``no``, ``nv``, ``fock`` [nact][nact], ``ints`` [nact]^4
+    ``nfzv`` frozen virtual orbitals.  When the file gives an energy for every orbital,
+    the NELEC/2 lowest are occupied and the orbitals go to QT order, occupied then
+    virtual, each by ascending energy (stable, so an energy-ordered file keeps its
+    order); otherwise the file's order is kept, the first NELEC/2 doubly occupied.
+    Returns ``no``, ``nv``, ``fock`` [nact][nact], ``ints`` [nact]^4
     (``ints[p,q,r,s] = <pq|rs>``), ``enuc``, ``efzc`` (frozen-core energy), ``escf`` and
     ``order`` (the file's 0-based orbital at each active QT position: a file-ordered MO
     matrix ``P`` becomes ``P[np.ix_(order, order)]`` on the active space)."""

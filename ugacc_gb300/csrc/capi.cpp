@@ -13,6 +13,7 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
 void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
                  const double* B, int64_t sBk, int64_t sBn, double beta, double* C, const GemmEpilogue& epi, int parts,
                  int kc);
+void wait_selftest(Ctx& c, unsigned long long limit_ns);
 }
 
 using namespace ucc;
@@ -334,6 +335,15 @@ ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t
       dgemm_strided(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi, 1, 0, 0, 0, nullptr);
     UCC_CUDA(cudaMemcpyAsync(C, dC.p, sizeof(double) * M * N, cudaMemcpyDeviceToHost, c.stream));
     UCC_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+ucc_status ucc_wait_selftest(ucc_ctx* ctx, uint64_t limit_ns) {
+  return guard(ctx, [&](Ctx& c) {
+    UCC_REQUIRE(limit_ns >= 1000 && limit_ns <= 10000000000ull, UCC_BAD_ARGS,
+                "ucc_wait_selftest: limit between 1 us and 10 s");
+    UCC_CUDA(cudaSetDevice(c.device));
+    wait_selftest(c, (unsigned long long)limit_ns);
   });
 }
 

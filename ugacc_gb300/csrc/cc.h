@@ -53,6 +53,10 @@ std::vector<double> diis_coefficients(const std::vector<double>& Bfull, int n);
 // delta  - FP64 residual whose heavy GEMMs are anchor + tensor-core corrections.
 // The solve ends only on a record sweep with ||R|| < r_convergence (and at least
 // refine_sweeps record sweeps); a delta sweep that gets there, or stalls, asks for one.
+// A delta residual is accurate to about 3e-5 of the anchor's own residual (its error
+// scales with the distance from the anchor), so an anchor taken above kReanchor *
+// r_convergence is replaced once the delta residual falls below that level: the next
+// anchor is close enough for the deltas to resolve r_convergence without stalling.
 // With precision FP64 every sweep is plain FP64.
 class MixedSweeps {
  public:
@@ -72,7 +76,7 @@ class MixedSweeps {
   Ctx& c_;
   bool mixed_, refine_, split_phase_, record_next_ = true;
   int stalls_ = 0, sweeps_ = 0;
-  double rms_prev_ = INFINITY;
+  double rms_prev_ = INFINITY, anchor_rms_ = INFINITY;
   Kind kind_ = kFp64, last_ = kFp64;
 };
 

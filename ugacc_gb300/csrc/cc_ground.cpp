@@ -1,6 +1,7 @@
 // Ground state: integral blocks, DIIS and the CCSD amplitude equations
 // (ugacc ccwfn.cc:12-120, :188-626).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -451,6 +452,10 @@ double ccsd_energy(Ctx& c, const double* t) { return energy(c, amp1(c, const_cas
 // residual norm near which BF16 hi+lo split products with FP32 accumulation stop
 // resolving the update (measured ~1.5e-6 at no=16/nv=160)
 constexpr double kMixedFloor = 2e-6;
+// delta sweeps resolve residuals down to ~3e-5 of their anchor's residual (measured at
+// no=32/nv=320: an anchor at 4.3e-5 left the delta residuals 1.3e-9 off), so an anchor
+// above kReanchor * r_convergence is re-taken once the deltas reach that level
+constexpr double kReanchor = 1e4;
 
 MixedSweeps::MixedSweeps(Ctx& c)
     : c_(c),
@@ -493,6 +498,7 @@ bool MixedSweeps::after(double rms, bool* restart_diis) {
     record++;
     record_next_ = false;
     stalls_ = 0;
+    anchor_rms_ = rms;
     done = rms < rc && record >= c_.opt.refine_sweeps;
     // the FP64 residual is well above what the last delta sweep reported: those sweeps'
     // anchor was too far away and their vectors would mislead the extrapolation
@@ -501,6 +507,8 @@ bool MixedSweeps::after(double rms, bool* restart_diis) {
     delta++;
     if (rms < rc) {
       record_next_ = true;  // confirm with an FP64 residual
+    } else if (anchor_rms_ > kReanchor * rc && rms < kReanchor * rc) {
+      record_next_ = true;  // the anchor is too far for the deltas to resolve rc: re-anchor here
     } else if (rms > 0.7 * rms_prev_) {
       if (++stalls_ >= 2) record_next_ = true;  // corrections no longer resolved: re-anchor
     } else {
@@ -555,6 +563,7 @@ CCSDResult run_ccsd(Ctx& c) {
   const bool mixed = sw.mixed();
   bool converged = false;
   int iter = 0;
+  auto t_prev = std::chrono::steady_clock::now();  // printed sweep times (the loop synchronises each sweep)
   for (iter = 1; iter <= c.opt.maxiter; iter++) {
     c.store["T"].swap(c.store["Told"]);  // amp_save, ccwfn.cc:300-309
     double* to = c.get("Told").p;
@@ -624,7 +633,11 @@ CCSDResult run_ccsd(Ctx& c) {
     if (c.opt.print) {
       double t1n = std::sqrt(dot(c, (int64_t)no * nv, tn, tn) / (2 * no));
       static const char* tag[] = {"", " split", " record", " delta"};
+      const auto t_now = std::chrono::steady_clock::now();
+      const double ms = std::chrono::duration<double, std::milli>(t_now - t_prev).count();
+      t_prev = t_now;
       std::printf("\t  %3d  %20.15f  %8.6f  %8.6e%s", iter, eccsd, t1n, rms, tag[kind]);
+      if (mixed) std::printf("  %8.1f ms", ms);
       if (noise >= 0.0) std::printf("  |R-R64| %.3e", noise);
       if (drift >= 0.0) std::printf("  |T-T0| %.3e", drift);
       std::printf("\n");

@@ -547,6 +547,7 @@ Tensor named_tensor(Ctx& c, const std::string& name) {
     if (what == "Y2") return amp2(c, c.get(p.pfx + "Y").p);
     throw Error(UCC_BAD_ARGS, "unknown tensor " + name);
   }
+  if (name == "t2_guess") return amp2(c, c.get("T_guess").p);  // the pending guess of the next CCSD solve
   if (name == "t1") return amp1(c, c.get("T").p);
   if (name == "t2") return amp2(c, c.get("T").p);
   if (name == "l1") return amp1(c, c.get("Lam").p);

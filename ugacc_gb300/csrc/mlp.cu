@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "cc.h"
+#include "tc_ptx.h"
 
 namespace ucc {
 void count_kernel_launch();
@@ -213,21 +214,206 @@ __global__ void targets_kernel(int no, int nv, const double* Voovv, const double
     y[x] = (float)(kTarget * (t2[x] - Voovv[x] / D));
   }
 }
-// t2 = t2_mp2 + prediction / T, written into the packed guess buffer (t1 = f_ia / D1)
-__global__ void guess_kernel(int no, int nv, const double* Voovv, const double* eps, const float* pred, double* t2) {
-  const int64_t n = (int64_t)no * no * nv * nv;
-  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
-    const int b = (int)(x % nv);
-    int64_t r = x / nv;
-    const int a = (int)(r % nv);
-    r /= nv;
-    const int j = (int)(r % no), i = (int)(r / no);
-    const double D = ((eps[i] + eps[j]) - eps[no + a]) - eps[no + b];
-    t2[x] = Voovv[x] / D + (double)pred[x] / kTarget;
+unsigned grid1(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
+
+// ------------------------------------------------------------------------------------
+// The guess in one pass on the tensor cores: for 128 doubles elements per tile, the pair
+// features and the first layer (15 -> 256, FP32 on the CUDA cores), the second layer
+// (256 -> 256) as one tcgen05 MMA chain with FP16 operands and an FP32 accumulator in
+// tensor memory, and the output layer with the guess t2 = t2_mp2 + y / kTarget in the
+// epilogue.  No feature or activation array reaches global memory.
+//
+// Shared memory (1024-aligned): the second layer's weights as the MMA's B operand, W2^T
+// [256 n][256 k] in four 64-wide K blocks (K-major, 128-byte swizzle: the 16-byte chunk c
+// of row r sits at chunk c ^ (r & 7)); the tile's activations as the A operand [128][256]
+// in the same layout; W1, b1, b2, w3 in FP32; the partial outputs of the column halves.
+// SiLU is z * sigmoid(z) with sigmoid(z) = (1 + tanh(z/2)) / 2 (one tanh.approx).
+// ------------------------------------------------------------------------------------
+constexpr int kGuessRows = 128, kGuessThreads = 256;
+constexpr size_t kGW2 = 0, kGA1 = kGW2 + 4 * 256 * 128, kGW1 = kGA1 + 4 * 128 * 128;
+constexpr size_t kGB1 = kGW1 + (size_t)kFeat * kHid * 4, kGB2 = kGB1 + kHid * 4, kGW3 = kGB2 + kHid * 4;
+constexpr size_t kGYP = kGW3 + kHid * 4, kGBAR = kGYP + kGuessRows * 4;
+constexpr size_t kGuessSmem = 1024 + kGBAR + 64;
+// instruction descriptor, kind::f16: D f32 (bit 4), A and B f16 (format 0 at bits 7-9 and
+// 10-12), both K-major, N = 256 (N >> 3 at bits 17-22), M = 128 (M >> 4 at bits 24-28)
+constexpr uint32_t kGuessIdesc = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+
+__device__ __forceinline__ float silu_tanh(float z) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
+  return z * fmaf(0.5f, t, 0.5f);
+}
+
+// diagonal integral tables the features read: vv[a][b] = <ab|ab>, oo[i][j] = <ij|ij>,
+// ov1[i][a] = <ia|ia>, ov2[i][a] = <ii|aa> (= <ia|ai>), in FP32
+__global__ void guess_diag_kernel(int no, int nv, const double* Voovv, const double* Voooo, const double* Vovov,
+                                  const double* Vvvvv, float* vv, float* oo, float* ov1, float* ov2) {
+  const int64_t o = no, v = nv;
+  const int64_t tot = v * v + o * o + 2 * o * v;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < tot; x += (int64_t)gridDim.x * blockDim.x) {
+    if (x < v * v) {
+      const int64_t a = x / v, b = x % v;
+      vv[x] = (float)Vvvvv[((a * v + b) * v + a) * v + b];
+    } else if (x < v * v + o * o) {
+      const int64_t y = x - v * v, i = y / o, j = y % o;
+      oo[y] = (float)Voooo[((i * o + j) * o + i) * o + j];
+    } else if (x < v * v + o * o + o * v) {
+      const int64_t y = x - v * v - o * o, i = y / v, a = y % v;
+      ov1[y] = (float)Vovov[((i * v + a) * o + i) * v + a];
+    } else {
+      const int64_t y = x - v * v - o * o - o * v, i = y / v, a = y % v;
+      ov2[y] = (float)Voovv[((i * o + i) * v + a) * v + a];
+    }
   }
 }
 
-unsigned grid1(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
+__global__ void __launch_bounds__(kGuessThreads, 1)
+    guess_tc_kernel(int no, int nv, int64_t n, const double* __restrict__ Voovv, const double* __restrict__ eps,
+                    const float* __restrict__ vv, const float* __restrict__ oo, const float* __restrict__ ov1,
+                    const float* __restrict__ ov2, const __half* __restrict__ wh, const float* __restrict__ w,
+                    int64_t oW1, int64_t oW2, int64_t ow3, int64_t ob1, int64_t ob2, int64_t ob3,
+                    double* __restrict__ t2out, int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  float* W1s = reinterpret_cast<float*>(smem + kGW1);
+  float* b1s = reinterpret_cast<float*>(smem + kGB1);
+  float* b2s = reinterpret_cast<float*>(smem + kGB2);
+  float* w3s = reinterpret_cast<float*>(smem + kGW3);
+  float* yp = reinterpret_cast<float*>(smem + kGYP);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kGBAR);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kGBAR + 8);
+  int* stop = reinterpret_cast<int*>(smem + kGBAR + 16);
+  const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+
+  // weights: W2^T into the swizzled B operand, 8 k-consecutive FP16 values per 16-byte chunk
+  for (int ch = tid; ch < kHid * (kHid / 8); ch += kGuessThreads) {
+    const int nn = ch / (kHid / 8), c8 = ch % (kHid / 8), kb = c8 / 8, c = c8 % 8;
+    __align__(16) __half hv[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) hv[e] = wh[oW2 + (int64_t)(c8 * 8 + e) * kHid + nn];
+    *reinterpret_cast<uint4*>(smem + kGW2 + (size_t)kb * 256 * 128 + (size_t)nn * 128 + ((c ^ (nn & 7)) << 4)) =
+        *reinterpret_cast<const uint4*>(hv);
+  }
+  for (int x = tid; x < kFeat * kHid; x += kGuessThreads) W1s[x] = __half2float(wh[oW1 + x]);
+  for (int x = tid; x < kHid; x += kGuessThreads) {
+    b1s[x] = w[ob1 + x];
+    b2s[x] = w[ob2 + x];
+    w3s[x] = __half2float(wh[ow3 + x]);
+  }
+  const float b3 = w[ob3];
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    *stop = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::smem_u32(tslot)),
+                 "r"(256));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc::fence_proxy_async();
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *tslot;
+  const int lr = tid & (kGuessRows - 1), half = tid / kGuessRows;  // row of the tile, hidden-unit half
+  const int q = warp & 3;                                          // TMEM lane quarter (rows q*32..q*32+31)
+  const int64_t ntiles = (n + kGuessRows - 1) / kGuessRows;
+  const int64_t o = no, v = nv;
+  uint32_t phase = 0;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t x = tile * kGuessRows + lr;
+    const bool valid = x < n;
+    float f[kFeat];
+    double t2mp2 = 0.0;
+    if (valid) {
+      const int b = (int)(x % v), a = (int)((x / v) % v), j = (int)((x / (v * v)) % o), i = (int)(x / (v * v * o));
+      const double D = ((eps[i] + eps[j]) - eps[no + a]) - eps[no + b];
+      const double vij = Voovv[x];
+      t2mp2 = vij / D;
+      const float rD = 1.0f / (float)D, S = (float)kScale;
+      const float vx = (float)Voovv[((int64_t)(i * o + j) * v + b) * v + a];
+      const float ei = (float)eps[i], ej = (float)eps[j], ea = (float)eps[no + a], eb = (float)eps[no + b];
+      f[0] = S * (float)vij * rD;
+      f[1] = S * vx * rD;
+      f[2] = S * (float)vij;
+      f[3] = -rD;
+      f[4] = 0.5f * (ei + ej);
+      f[5] = 0.5f * (ea + eb);
+      f[6] = i == j ? 1.f : 0.f;
+      f[7] = a == b ? 1.f : 0.f;
+      f[8] = S * vv[(int64_t)a * v + b];
+      f[9] = S * oo[(int64_t)i * o + j];
+      f[10] = S * (ov1[(int64_t)i * v + a] + ov1[(int64_t)j * v + b]);
+      f[11] = S * (ov2[(int64_t)i * v + a] + ov2[(int64_t)j * v + b]);
+      f[12] = 0.5f * fabsf(ei - ej);
+      f[13] = 0.5f * fabsf(ea - eb);
+      f[14] = 0.25f * (ei - ej) * (ea - eb);
+    } else {
+#pragma unroll
+      for (int k = 0; k < kFeat; k++) f[k] = 0.f;
+    }
+    // layer 1 for this thread's 128 hidden units, SiLU, FP16, into the A operand: unit u is
+    // K index u of the second layer (K block u / 64, chunk (u % 64) / 8)
+    for (int u0 = half * 128; u0 < half * 128 + 128; u0 += 8) {
+      __align__(16) __half hv[8];
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const int u = u0 + e;
+        float z = b1s[u];
+#pragma unroll
+        for (int k = 0; k < kFeat; k++) z = fmaf(f[k], W1s[k * kHid + u], z);
+        hv[e] = __float2half_rn(valid ? silu_tanh(z) : 0.f);
+      }
+      const int kb = u0 / 64, c = (u0 % 64) / 8;
+      *reinterpret_cast<uint4*>(smem + kGA1 + (size_t)kb * 128 * 128 + (size_t)lr * 128 + ((c ^ (lr & 7)) << 4)) =
+          *reinterpret_cast<const uint4*>(hv);
+    }
+    tc::fence_proxy_async();
+    tc::fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+#pragma unroll
+      for (int kb = 0; kb < 4; kb++) {
+        const uint64_t ad = tc::sdesc(smem + kGA1 + (size_t)kb * 128 * 128);
+        const uint64_t bd = tc::sdesc(smem + kGW2 + (size_t)kb * 256 * 128);
+#pragma unroll
+        for (int k = 0; k < 4; k++)  // +32 bytes along K per 16-element step
+          tc::mma_i(tmem, ad + (uint64_t)(k * 2), bd + (uint64_t)(k * 2), kGuessIdesc, (kb | k) != 0);
+      }
+      tc::mma_commit(bar);
+      if (!tc::mbar_wait(bar, phase, err)) *stop = 1;
+    }
+    __syncthreads();
+    if (*stop) break;
+    phase ^= 1u;
+    tc::fence_after();
+    // output layer: warp w reads TMEM lanes (w % 4) * 32.. (its rows) and columns of its half
+    float part = 0.f;
+#pragma unroll 1
+    for (int ch = 0; ch < 4; ch++) {
+      uint32_t r[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(half * 128 + ch * 32), r);
+#pragma unroll
+      for (int jj = 0; jj < 32; jj++) {
+        const int u = half * 128 + ch * 32 + jj;
+        part = fmaf(silu_tanh(__uint_as_float(r[jj]) + b2s[u]), w3s[u], part);
+      }
+    }
+    if (half == 1) yp[lr] = part;
+    tc::fence_before();
+    __syncthreads();
+    if (half == 0 && valid) t2out[x] = t2mp2 + (double)(part + yp[lr] + b3) / kTarget;
+  }
+  if (tid == 0 && *stop) tc::mbar_wait_deadline(bar, phase);  // no MMA in flight when TMEM is released
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
+  }
+}
 
 }  // namespace mlp
 }  // namespace ucc
@@ -562,33 +748,47 @@ void mlp_features(Ctx& c, float* out, size_t rows, float* targets, bool with_tar
   UCC_CUDA(cudaStreamSynchronize(c.stream));
 }
 
+// the network's T2 guess into the context's T_guess (t1 = f_ia / D1): one fused
+// tensor-core pass over the doubles elements on the context's stream; the weights are
+// read on that stream after the network's own stream has finished updating them
 void mlp_guess(Ctx& c, ucc_mlp* net) {
-  {
-    UCC_REQUIRE(c.loaded, UCC_BAD_STATE, "no Hamiltonian loaded");
-    UCC_REQUIRE(net->device == c.device, UCC_BAD_ARGS, "network and context on different devices");
-    const int no = c.no, nv = c.nv;
-    const int64_t n = (int64_t)no * no * nv * nv, n1 = (int64_t)no * nv;
-    ensure_rows(*net, n);
-    Scratch X(c, sizeof(float) * n * kFeat);
-    features_kernel<<<grid1(n), 256, 0, c.stream>>>(no, nv, c.get("Voovv").p, c.get("Voooo").p,
-                                                    c.get("Vovov").p, c.get("Vvvvv").p, c.get("eps").p,
-                                                    static_cast<float*>(X.p));
-    count_kernel_launch();
-    UCC_CUDA(cudaStreamSynchronize(c.stream));
-    forward(*net, static_cast<float*>(X.p), n);
-    UCC_CUDA(cudaStreamSynchronize(net->stream));
-    if (!c.has("T_guess")) c.alloc("T_guess", {n1 + n}, true);
-    double* g = c.get("T_guess").p;
-    // t1 part: f_ia / (f_ii - f_aa) on the host (small)
-    std::vector<double> t1(n1);
-    const int nact = no + nv;
-    for (int i = 0; i < no; i++)
-      for (int a = 0; a < nv; a++)
-        t1[(size_t)i * nv + a] = c.fock[(size_t)i * nact + no + a] / (c.eps[i] - c.eps[no + a]);
-    UCC_CUDA(cudaMemcpyAsync(g, t1.data(), sizeof(double) * n1, cudaMemcpyHostToDevice, c.stream));
-    guess_kernel<<<grid1(n), 256, 0, c.stream>>>(no, nv, c.get("Voovv").p, c.get("eps").p, net->y, g + n1);
-    count_kernel_launch();
-    UCC_CUDA(cudaStreamSynchronize(c.stream));
-  }
+  UCC_REQUIRE(c.loaded, UCC_BAD_STATE, "no Hamiltonian loaded");
+  UCC_REQUIRE(net->device == c.device, UCC_BAD_ARGS, "network and context on different devices");
+  const int no = c.no, nv = c.nv;
+  const int64_t n = (int64_t)no * no * nv * nv, n1 = (int64_t)no * nv;
+  UCC_CUDA(cudaStreamSynchronize(net->stream));
+  if (!c.has("T_guess")) c.alloc("T_guess", {n1 + n}, true);
+  double* g = c.get("T_guess").p;
+  // t1 part: f_ia / (f_ii - f_aa) on the host (small)
+  std::vector<double> t1(n1);
+  const int nact = no + nv;
+  for (int i = 0; i < no; i++)
+    for (int a = 0; a < nv; a++)
+      t1[(size_t)i * nv + a] = c.fock[(size_t)i * nact + no + a] / (c.eps[i] - c.eps[no + a]);
+  UCC_CUDA(cudaMemcpyAsync(g, t1.data(), sizeof(double) * n1, cudaMemcpyHostToDevice, c.stream));
+  const int64_t ndiag = (int64_t)nv * nv + (int64_t)no * no + 2LL * no * nv;
+  Scratch diag(c, sizeof(float) * ndiag);
+  float* vv = static_cast<float*>(diag.p);
+  float* oo = vv + (int64_t)nv * nv;
+  float* ov1 = oo + (int64_t)no * no;
+  float* ov2 = ov1 + (int64_t)no * nv;
+  guess_diag_kernel<<<grid1(ndiag), 256, 0, c.stream>>>(no, nv, c.get("Voovv").p, c.get("Voooo").p,
+                                                        c.get("Vovov").p, c.get("Vvvvv").p, vv, oo, ov1, ov2);
+  count_kernel_launch();
+  UCC_CUDA(cudaFuncSetAttribute(guess_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGuessSmem));
+  int sms = 0;
+  UCC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
+  const int64_t ntiles = (n + kGuessRows - 1) / kGuessRows;
+  Scratch errflag(c, sizeof(int));
+  UCC_CUDA(cudaMemsetAsync(errflag.p, 0, sizeof(int), c.stream));
+  guess_tc_kernel<<<(unsigned)std::min<int64_t>(ntiles, sms), kGuessThreads, kGuessSmem, c.stream>>>(
+      no, nv, n, c.get("Voovv").p, c.get("eps").p, vv, oo, ov1, ov2, net->wh, net->w, net->oW1(), net->oW2(),
+      net->ow3(), net->ob1(), net->ob2(), net->ob3(), g + n1, static_cast<int*>(errflag.p));
+  count_kernel_launch();
+  UCC_CUDA(cudaGetLastError());
+  int herr = 0;
+  UCC_CUDA(cudaMemcpyAsync(&herr, errflag.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  UCC_CUDA(cudaStreamSynchronize(c.stream));
+  UCC_REQUIRE(!herr, UCC_DEVICE_TIMEOUT, "guess network: a tensor-core wait timed out");
 }
 }  // namespace ucc

@@ -18,7 +18,11 @@
 //    race on it and must not be issued;
 //  * the first call on a device looks up the array's device address with that device
 //    current (cudaGetSymbolAddress) and caches it; make that first call before any
-//    stream capture.
+//    stream capture.  With CUDA's lazy module loading (the default) that first call is
+//    also when the 32 MiB are reserved on the device, so a host whose own pool takes the
+//    device memory should make it before the pool does;
+//  * a call whose stream is not capturing looks the address up again (cheap), so the
+//    cached value never outlives a cudaDeviceReset or a module reload.
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -152,10 +156,17 @@ extern "C" ucc_status ucc_triples_noalloc(int no, int nv, const double* t1, cons
     put_msg(errbuf, errlen, "ucc_triples_noalloc: no current CUDA device");
     return UCC_CUDA_ERROR;
   }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
   double* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {  // once per device, with that device current
+    // once per device, with that device current; again on every call outside a stream
+    // capture, so that a reset device (a reloaded module) gets its new address
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const cudaError_t qrc = cudaStreamIsCapturing(st, &cap);
+    if (qrc != cudaSuccess) cudaGetLastError();  // the failed query's error is not left behind
+    const bool capturing = qrc != cudaSuccess || cap != cudaStreamCaptureStatusNone;
+    if (!g_scratch_ptr[dev] || !capturing) {
       void* p = nullptr;
       const cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (rc != cudaSuccess || !p) {
@@ -166,7 +177,6 @@ extern "C" ucc_status ucc_triples_noalloc(int no, int nv, const double* t1, cons
     }
     scratch = g_scratch_ptr[dev];
   }
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   double* W = scratch;
   double* partial = scratch + nv3;
   double* total = partial + ntup * nv;

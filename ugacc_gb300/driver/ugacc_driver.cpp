@@ -109,7 +109,13 @@ int main(int argc, char** argv) {
       for (int p = 0; p < n; p++) fock[(size_t)p * n + p] = in.eps[p];
       H = std::make_shared<Hamiltonian>(in.no, in.nv, in.naux, fock.data(), in.B.data());
     }
-    auto cc = std::make_shared<CCWfn>(H, o);
+    // the reference's CCWfn takes the SCF wavefunction first (ccwfn.h:14); here it is the
+    // file's SCF energy (FCIDUMP input) or nothing (synthetic input)
+    struct ScfReference {
+      double energy;
+    };
+    auto ref = std::make_shared<ScfReference>(ScfReference{dump ? H->escf() : 0.0});
+    auto cc = std::make_shared<CCWfn>(ref, H, o);
     const double ecc = cc->compute_energy();
     std::printf("{\"e_ccsd\": %.17g, \"e_t\": %.17g, \"e_cc\": %.17g", cc->eccsd(), cc->et(), ecc);
     if (dump)
@@ -125,16 +131,26 @@ int main(int argc, char** argv) {
       if (o.dertype == "SECOND" && in.npert >= 3) {
         const char* cart = "XYZ";
         std::vector<std::shared_ptr<CCPert>> mu(3);
+        const int n = in.no + in.nv;
         for (int x = 0; x < 3; x++) {
-          mu[x] = std::make_shared<CCPert>(in.perts[x].data(), o.my_omega, cc, hbar, lam);
+          // the reference hands CCPert its perturbation as row pointers (ccpert.h:19)
+          std::vector<double*> rows(n);
+          for (int r = 0; r < n; r++) rows[r] = in.perts[x].data() + (size_t)r * n;
+          mu[x] = std::make_shared<CCPert>(rows.data(), o.my_omega, cc, hbar, lam);
           mu[x]->solve(right);
           if (o.myhand != "RIGHT") mu[x]->solve(left);
+          std::printf(", \"pseudoresponse_%c\": %.17g", cart[x], mu[x]->pseudoresponse(right));
         }
         for (int p = 0; p < 3; p++)
           for (int q = 0; q <= p; q++) {
-            CCResp r(mu[p], mu[q]);
-            const double a = p == q ? r.linresp(mu[p], mu[q])
-                                    : 0.5 * r.linresp(mu[p], mu[q]) + 0.5 * r.linresp(mu[q], mu[p]);
+            double a;
+            if (p == q) {  // one perturbation on both sides: the single-argument form (ccresp.h:13)
+              CCResp r(mu[p]);
+              a = r.linresp(mu[p], mu[p]);
+            } else {
+              CCResp r(mu[p], mu[q]);
+              a = 0.5 * r.linresp(mu[p], mu[q]) + 0.5 * r.linresp(mu[q], mu[p]);
+            }
             std::printf(", \"alpha_%c%c\": %.17g", cart[p], cart[q], a);
           }
       }
