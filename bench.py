@@ -1,18 +1,32 @@
 #!/usr/bin/env python
-"""Benchmark: CCSD(T) on the no=16 / nv=160 synthetic RHF Hamiltonian (seed 1).
+"""Benchmark: mixed-precision + learned-guess CCSD(T) against the plain FP64 GPU form.
 
-One step = one full CCSD(T) solve from the MP2 guess to ||R|| < 1e-10 followed by the
-(T) correction, on Hamiltonian blocks already resident in HBM.  The default arm is the
-mixed form (BF16 hi+lo split tensor-core contractions, FP64-accurate refinement sweeps,
-tensor-core (T)); the plain FP64 form of the same step is timed alongside and the energy
-differences between the two are reported.  value = algorithmic
-TFLOP/s of the whole job (CCSD iterations x 2(no^2 nv^4 + 2 no^4 nv^2 + 10 no^3 nv^3 +
-8 no^2 nv^3) + (T) 2 no(no+1)(no+2) nv^3 (nv+no)), device time from CUDA events on the
-library's stream.  e2e repeats the step through the public API from pinned host
-buffers: Hamiltonian upload (DF factors) + block build + CCSD(T) + energies back.
+Default workload: the synthetic RHF Hamiltonian no=32 / nv=320 (naux = 1056, seed 2;
+<ab|ef> alone is 84 GB in FP64).  One step = the learned T2 guess (one fused tensor-core
+pass) + a full CCSD solve to ||R|| < 1e-10 (BF16 hi+lo split sweeps, FP64-accurate
+refinement sweeps on the sliced tensor-core GEMM) + the (T) correction, on Hamiltonian
+blocks already resident in HBM.  Reported beside it, in the same run:
+
+* the plain FP64 GPU form of the same CCSD(T) (DFMA kernels), timed once, and the energy
+  and amplitude differences |dE_CCSD|, |dE_(T)|, max|dT2| of the mixed result against it;
+* the same mixed solve from the MP2 guess, so that the sweeps the learned guess saves are
+  measured on the workload itself;
+* the guess network's training cost (outside the timed region): it is trained on the GPU
+  by the library's own kernels on converged amplitudes of smaller Hamiltonians of the same
+  generator (no=16 / nv=160, seeds 11-14), never on the benchmark Hamiltonian.
+
+value = algorithmic TFLOP/s of the whole job: (CCSD iterations of the FP64 form, i.e. the
+reference's own iteration count) x 2(no^2 nv^4 + 2 no^4 nv^2 + 10 no^3 nv^3 + 8 no^2 nv^3)
++ (T) 2 no(no+1)(no+2) nv^3 (nv+no), over the device time (CUDA events on the library's
+stream) of guess + CCSD + (T).  e2e repeats the step through the public API from pinned
+host buffers: DF factors upload, block build, guess, CCSD(T), energies back.
+
+--workload c2 keeps the no=16 / nv=160 case (seed 1) whose reference arm times the numpy
+oracle's CCSD iteration.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--precision mixed|fp64] [--no-fp64-reference] [--no-cpu-baseline]
+                    [--workload c3|c2] [--precision mixed|fp64] [--no-fp64-reference]
+                    [--no-cpu-baseline] [--no-guess]
 Multi-GPU: replicas only (each rank solves its own copy; weak scaling).
 """
 from __future__ import annotations
@@ -28,19 +42,22 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# workloads: the default is the no=16 / nv=160 CCSD(T) case; "c3" (no=32 / nv=320, seed 2,
-# Vvvvv 84 GB) is the large mixed-precision case, minutes per step, run on request
+# workloads (no, nv, seed); naux = 3 (no + nv)
 WORKLOADS = {"c2": (16, 160, 1), "c3": (32, 320, 2)}
-NO, NV, SEED = WORKLOADS["c2"]
-WORKLOAD = "ccsd_t_no16_nv160_seed1"
-METRIC = "CCSD(T) TFLOP/s (algorithmic) at no=16/nv=160"
+NO, NV, SEED = WORKLOADS["c3"]
+WORKLOAD = "ccsd_t_no32_nv320_seed2"
+METRIC = "CCSD(T) wall-s & TFLOP/s vs plain FP64 GPU at |dE|<=1 uEh; iterations saved"
+# training Hamiltonians of the guess network: the same generator, smaller, other seeds
+GUESS_TRAIN = {"no": 16, "nv": 160, "seeds": [11, 12, 13, 14], "row_fraction": 0.25, "epochs": 4, "batch": 8192,
+               "lr": 1e-3, "r_convergence": 1e-8}
 
 
 def select_workload(name):
     global NO, NV, SEED, WORKLOAD, METRIC
     NO, NV, SEED = WORKLOADS[name]
     WORKLOAD = "ccsd_t_no%d_nv%d_seed%d" % (NO, NV, SEED)
-    METRIC = "CCSD(T) TFLOP/s (algorithmic) at no=%d/nv=%d" % (NO, NV)
+    if name == "c2":
+        METRIC = "CCSD(T) TFLOP/s (algorithmic) at no=16/nv=160"
 
 
 # bf16 products per sliced FP64 GEMM (9 slices per operand, orders s + t < 9)
@@ -53,6 +70,11 @@ def flops_ccsd_iter(no, nv):
 
 def flops_triples(no, nv):
     return 2.0 * no * (no + 1) * (no + 2) * nv**3 * (nv + no)
+
+
+def flops_triples_tuple(no, nv):
+    """One i >= j >= k term of (T): six e-sums and six m-sums of nv^3 elements each."""
+    return 12.0 * nv**3 * (nv + no)
 
 
 class ClockSampler:
@@ -136,6 +158,9 @@ def fp64_gemm_peak_tflops():
         return None
 
 
+# ------------------------------------------------------------------------------------
+# CPU legs: the numpy oracle (test infrastructure) on a bounded sample of the workload
+# ------------------------------------------------------------------------------------
 def cpu_oracle_sample(h, iters: int = 1):
     """The oracle's CCSD iteration (numpy, all host threads) at the same workload."""
     from oracle import cc as O
@@ -154,10 +179,33 @@ def cpu_oracle_sample(h, iters: int = 1):
     return times
 
 
+def cpu_triples_sample(h, ntuples: int):
+    """The oracle's (T) term (W3 e/m-sums and the energy algebra of ccwfn.cc:795-852 and
+    :1388-1418, numpy on all host threads) for the first `ntuples` occupied triples
+    i >= j >= k, on MP2 amplitudes: a bounded sample of the workload's (T).  Returns the
+    setup seconds and the per-tuple seconds."""
+    from oracle import cc as O
+
+    t0 = time.perf_counter()
+    H = O.Hamiltonian(h)
+    for blk in ["oovv", "ovvv", "ooov"]:
+        H.V(blk)
+    cc = O.CCWfn(H)
+    setup = cc.tuple_setup()
+    setup_s = time.perf_counter() - t0
+    tuples = [(i, j, k) for i in range(h.no) for j in range(i + 1) for k in range(j + 1)][:ntuples]
+    times = []
+    for (i, j, k) in tuples:
+        t1 = time.perf_counter()
+        cc.tcorr_tuple(i, j, k, setup)
+        times.append(time.perf_counter() - t1)
+    return setup_s, times
+
+
 def recorded_reference_run() -> dict:
-    """The reference's own compiled loops on this workload, as recorded with the golden
-    fixture (tests/golden/c2.json: one single-core x86 run); empty when absent."""
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "c2.json")
+    """The reference's own compiled loops on the no=16/nv=160 workload, as recorded with
+    the golden fixture (tests/golden/c2.json: one single-core x86 run); empty otherwise."""
+    path = os.path.join(ROOT, "tests", "golden", "c2.json")
     if WORKLOAD != "ccsd_t_no16_nv160_seed1" or not os.path.exists(path):
         return {}
     run = json.load(open(path))["runs"]["ccsd_t"]
@@ -173,24 +221,74 @@ def run_reference(args, rank):
         return
     from ugacc_gb300.generator import make_hamiltonian
 
-    if args.workload != "c2":
-        print(json.dumps({"impl": "reference", "unavailable": "the CPU path needs the full <pq|rs> array "
-                          "(%.0f GB at no=%d/nv=%d), beyond host memory" % (8.0 * (NO + NV) ** 4 / 1e9, NO, NV)}))
-        return
     h = make_hamiltonian(NO, NV, SEED)
-    times = cpu_oracle_sample(h, args.warmup + args.steps)[args.warmup:]
-    ms = 1e3 * sum(times) / len(times)
-    v = flops_ccsd_iter(NO, NV) / (ms * 1e-3) / 1e12
     cores = os.cpu_count()
+    if args.workload == "c2":
+        times = cpu_oracle_sample(h, args.warmup + args.steps)[args.warmup:]
+        step = "one CCSD iteration (residual + Jacobi update)"
+        flops = flops_ccsd_iter(NO, NV)
+        sample = "numpy oracle: one CCSD iteration at no=%d/nv=%d per step" % (NO, NV)
+        extra = recorded_reference_run()
+    else:
+        # the CCSD iteration needs <ab|ef> (84 GB) and hours per sweep on the host; the (T)
+        # tuples need 9 GB: one tuple term per step
+        setup_s, times = cpu_triples_sample(h, args.warmup + args.steps)
+        times = times[args.warmup:]
+        step = "one (T) tuple term i >= j >= k (W3 e/m-sums + energy algebra) on MP2 amplitudes"
+        flops = flops_triples_tuple(NO, NV)
+        sample = ("numpy oracle: (T) tuple terms at no=%d/nv=%d, one per step (%.3g FLOP each), blocks built from "
+                  "the DF factors in %.1f s" % (NO, NV, flops, setup_s))
+        extra = {}
+    ms = 1e3 * sum(times) / len(times)
+    v = flops / (ms * 1e-3) / 1e12
     line = {"metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "step": "one CCSD iteration (residual + Jacobi update)",
-                       "l2": "inputs larger than L2", **recorded_reference_run()},
-            "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-                             "sample": "numpy oracle: one CCSD iteration at no=%d/nv=%d per step" % (NO, NV)},
+            "config": {"workload": WORKLOAD, "step": step, "l2": "inputs larger than L2", **extra},
+            "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------
+def train_guess_network(U, make_hamiltonian, device):
+    """Guess network trained on the GPU (the library's own forward/backward kernels) on
+    converged amplitudes of the training Hamiltonians; returns the network and its cost."""
+    import numpy as np
+
+    g = GUESS_TRAIN
+    rng = np.random.default_rng(0)
+    t0 = time.perf_counter()
+    Xs, ts = [], []
+    for s in g["seeds"]:
+        h = make_hamiltonian(g["no"], g["nv"], s)
+        H = U.Hamiltonian.from_synthetic(h, device=device, precision="MIXED")
+        U.CCWfn(H, {"R_CONVERGENCE": g["r_convergence"], "PRECISION": "MIXED"}).compute_energy()
+        X, t = U.mlp_features(H, with_targets=True)
+        keep = rng.random(X.shape[0]) < g["row_fraction"]
+        Xs.append(X[keep])
+        ts.append(t[keep])
+        H.ctx.close()
+    X = np.concatenate(Xs)
+    t = np.concatenate(ts)
+    data_s = time.perf_counter() - t0
+    net = U.MLP(device=device, seed=1)
+    t1 = time.perf_counter()
+    loss0 = float(net.loss_grad(X[:200000], t[:200000])[0])
+    loss = float(net.train(X, t, epochs=g["epochs"], batch=g["batch"], lr=g["lr"], seed=1))
+    train_s = time.perf_counter() - t1
+    info = {"hamiltonians": "no=%d/nv=%d, seeds %s, the same generator" % (g["no"], g["nv"], g["seeds"]),
+            "rows": int(X.shape[0]), "epochs": g["epochs"], "loss_before": loss0, "loss_after": loss,
+            "data_s": data_s, "train_s": train_s,
+            "note": "outside the timed region; the benchmark Hamiltonian is not in the training set"}
+    return net, info
+
+
+def sweeps_of(st):
+    return {"total": st["ccsd_iterations"], "split": st["mixed_iterations"], "record": st["fp64_iterations"],
+            "delta": st["anchored_iterations"]}
 
 
 def main():
@@ -202,7 +300,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-reference", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-guess", action="store_true", help="start every solve from the MP2 guess")
+    ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     select_workload(args.workload)
     rank = int(os.environ.get("RANK", "0"))
@@ -234,32 +333,43 @@ def main():
         return _allmax(x, dist if world > 1 else None, device="cuda")
 
     h = make_hamiltonian(NO, NV, SEED)
+    mixed = args.precision == "mixed"
+    use_guess = mixed and not args.no_guess
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == "c2":
-        t = cpu_oracle_sample(h, 1)
-        cpu = {"value": flops_ccsd_iter(NO, NV) / t[0] / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(),
-               "kind": "port", "sample": "numpy oracle (BLAS threads = host cores): one CCSD iteration at "
-                                         "no=%d/nv=%d from the MP2 guess, %.1f s" % (NO, NV, t[0])}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        if args.workload == "c2":
+            t = cpu_oracle_sample(h, 1)
+            cpu = {"value": flops_ccsd_iter(NO, NV) / t[0] / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(),
+                   "kind": "port", "sample": "numpy oracle (BLAS threads = host cores): one CCSD iteration at "
+                                             "no=%d/nv=%d from the MP2 guess, %.1f s" % (NO, NV, t[0])}
+        else:
+            setup_s, t = cpu_triples_sample(h, 2)
+            per = sum(t) / len(t)
+            cpu = {"value": flops_triples_tuple(NO, NV) / per / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(),
+                   "kind": "port", "sample": "numpy oracle (BLAS threads = host cores): 2 (T) tuple terms at "
+                                             "no=%d/nv=%d on MP2 amplitudes, %.1f s each (+%.1f s block build)"
+                                             % (NO, NV, per, setup_s)}
     fp64_peak = fp64_gemm_peak_tflops()
+    net, guess_info = (train_guess_network(U, make_hamiltonian, local) if use_guess else (None, None))
 
-    H = U.Hamiltonian.from_synthetic(h, device=local)
-    # plain FP64 form of the same workload (the comparison the metric is quoted against)
-    fp64 = None
-    if args.precision == "mixed" and not args.no_fp64_reference:
-        c64 = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "MAXITER": 100, "WFN": "CCSD_T", "PRECISION": "FP64"})
-        c64.compute_energy()
-        H.ctx.reset_stats()
-        c64.compute_energy()
-        s64 = H.ctx.stats()
-        fp64 = {"ms_per_step": s64["ccsd_ms"] + s64["triples_ms"], "ccsd_ms": s64["ccsd_ms"],
-                "triples_ms": s64["triples_ms"], "ccsd_iterations": s64["ccsd_iterations"],
-                "e_ccsd": c64.eccsd, "e_t": c64.et}
-
+    H = U.Hamiltonian.from_synthetic(h, device=local, precision="MIXED" if mixed else "FP64")
     opts = {"R_CONVERGENCE": 1e-10, "MAXITER": 100, "WFN": "CCSD_T", "PRECISION": args.precision.upper()}
     cc = U.CCWfn(H, opts)
-    for _ in range(args.warmup):
+
+    def step():
+        if use_guess:
+            net.guess(H)
         cc.compute_energy()
-    e_ref = (cc.eccsd, cc.et)
+
+    for _ in range(args.warmup):
+        step()
+    # the same solve from the MP2 guess: the sweeps the learned guess saves
+    mp2_start = None
+    if use_guess:
+        H.ctx.reset_stats()
+        cc.compute_energy()
+        st0 = H.ctx.stats()
+        mp2_start = {"sweeps": sweeps_of(st0), "ccsd_ms": st0["ccsd_ms"]}
 
     barrier()
     H.ctx.reset_stats()
@@ -267,22 +377,21 @@ def main():
     clocks.start()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        cc.compute_energy()
+        step()
     barrier()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     st = H.ctx.stats()
-    ms_dev = (st["ccsd_ms"] + st["triples_ms"]) / args.steps
+    e_ref = (cc.eccsd, cc.et)
+    ms_dev = (st["ccsd_ms"] + st["triples_ms"] + st["guess_ms"]) / args.steps
     ms = allmax(ms_dev)
-    iters = st["ccsd_iterations"]
-    flops_step = flops_ccsd_iter(NO, NV) * iters + flops_triples(NO, NV)
-    value = world * flops_step / (ms * 1e-3) / 1e12
+    sweeps = sweeps_of(st)  # the library keeps the sweep counts of the last solve
+    t2_mixed = cc.t2 if not args.no_fp64_reference and mixed else None
 
-    # the device-resident context is no longer needed: release its memory (the no=32/nv=320
+    # the device-resident context is released before the end-to-end leg (the no=32/nv=320
     # blocks and their tensor-core copies would not fit twice)
     del cc
     H.ctx.close()
-    # end to end through the public API from pinned host memory
     Bp = torch.from_numpy(np.ascontiguousarray(h.B)).pin_memory()
     Fp = torch.from_numpy(np.ascontiguousarray(h.fock)).pin_memory()
     ctx2 = U.Context(local)
@@ -291,31 +400,60 @@ def main():
     t1 = time.perf_counter()
     for _ in range(e2e_steps):
         H2 = U.Hamiltonian(NO, NV, Fp.numpy(), B=Bp.numpy(), context=ctx2, precision=args.precision.upper())
+        if use_guess:
+            net.guess(H2)
         c2 = U.CCWfn(H2, opts)
         c2.compute_energy()
     barrier()
     e2e_ms = allmax(1e3 * (time.perf_counter() - t1) / e2e_steps)
+    del c2, H2
+    ctx2.close()
+
+    # the plain FP64 form of the same CCSD(T), once (the comparison the metric is quoted against)
+    fp64 = None
+    if mixed and not args.no_fp64_reference:
+        ctx64 = U.Context(local)
+        H64 = U.Hamiltonian.from_synthetic(h, context=ctx64, precision="FP64")
+        c64 = U.CCWfn(H64, dict(opts, PRECISION="FP64"))
+        ctx64.reset_stats()
+        c64.compute_energy()
+        s64 = ctx64.stats()
+        t2_64 = c64.t2
+        fp64 = {"ms_per_step": s64["ccsd_ms"] + s64["triples_ms"], "ccsd_ms": s64["ccsd_ms"],
+                "triples_ms": s64["triples_ms"], "ccsd_iterations": s64["ccsd_iterations"],
+                "e_ccsd": c64.eccsd, "e_t": c64.et, "runs": 1, "warmup": 0}
+        dt2 = float(np.abs(t2_mixed - t2_64).max())
+        del c64, H64, t2_64
+        ctx64.close()
+    # FLOPs per step on the FP64 form's (the reference's) iteration count
+    it_flops = fp64["ccsd_iterations"] if fp64 else sweeps["total"]
+    flops_step = flops_ccsd_iter(NO, NV) * it_flops + flops_triples(NO, NV)
+    value = world * flops_step / (ms * 1e-3) / 1e12
     e2e_value = world * flops_step / (e2e_ms * 1e-3) / 1e12
 
     bf16 = measured_peak("bf16_tflops")
+    bf16s = measured_peak("bf16_tflops_sustained")
     step_ms_total = ms_dev * args.steps
-    tc = f64g = None
+    tc = f64g = sl = None
     if st["tc_gemm_launches"]:
         ach = st["tc_gemm_flops"] / (st["tc_gemm_ms"] * 1e-3) / 1e12
-        tc = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
-              "frac": (ach / bf16) if bf16 else None, "traffic": None,
+        tc = {"bound": "tensor", "achieved": ach, "peak": bf16s, "unit": "TFLOP/s",
+              "frac": (ach / bf16s) if bf16s else None, "traffic": None,
               "kernel": "tcgen05 BF16 hi+lo split GEMM (ucc::tc::gemm_kernel), all launches of the step",
               "flops": "algorithmic 2*M*N*K per launch over its CUDA-event time; the tensor pipe executes 3x "
                        "that (hi.hi + hi.lo + lo.hi)",
-              "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
+              "tensor_pipe_frac": (3 * ach / bf16s) if bf16s else None,
+              "frac_of_burst": (ach / bf16) if bf16 else None,
+              "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (kernel timed inside a seconds-long step), "
+                             "of measured",
               "share_of_step": st["tc_gemm_ms"] / step_ms_total,
               "launches": st["tc_gemm_launches"], "ms_per_launch": st["tc_gemm_ms"] / st["tc_gemm_launches"]}
     if st["fp64_gemm_launches"]:
         ach = st["fp64_gemm_flops"] / (st["fp64_gemm_ms"] * 1e-3) / 1e12
         f64g = {"bound": "tensor", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": (ach / fp64_peak) if fp64_peak else None, "traffic": None,
-                "kernel": "FP64 DFMA GEMM (dgemm_kernel), all launches of the step (FP64 record sweeps of the "
-                          "mixed solve, FP64 pieces)",
+                "kernel": "FP64 DFMA GEMM (dgemm_kernel), all launches of the step (contractions below the tensor-"
+                          "core thresholds)",
                 "compute_unit": "FP64 pipe (compute bound, not the tensor cores)",
                 "flops": "algorithmic 2*M*N*K per launch over its CUDA-event time",
                 "peak_source": "cuBLAS DGEMM 8192^3 measured in this process on this GPU (FP64 has no entry in "
@@ -323,19 +461,19 @@ def main():
                 "share_of_step": st["fp64_gemm_ms"] / step_ms_total,
                 "launches": st["fp64_gemm_launches"],
                 "ms_per_launch": st["fp64_gemm_ms"] / st["fp64_gemm_launches"]}
-    sl = None
     if st["sliced_gemm_launches"]:
         fp64eq = st["sliced_gemm_flops"] / (st["sliced_gemm_ms"] * 1e-3) / 1e12
         ach = SLICE_PRODUCTS * fp64eq
-        sl = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
-              "frac": (ach / bf16) if bf16 else None, "traffic": None,
+        sl = {"bound": "tensor", "achieved": ach, "peak": bf16s, "unit": "TFLOP/s",
+              "frac": (ach / bf16s) if bf16s else None, "traffic": None,
               "kernel": "tcgen05 sliced FP64 GEMM (ucc::tc::sliced_gemm_kernel): FP64-accurate products of 9 exact "
                         "bf16 slices per operand, all launches of the step (refinement sweeps of the mixed solve)",
               "flops": "tensor-pipe rate: 45 slice products x algorithmic 2*M*N*K per launch over its CUDA-event time "
                        "(slicing of non-cached operands included)",
               "fp64_equivalent_tflops": fp64eq,
               "fp64_equivalent_vs_dgemm_peak": (fp64eq / fp64_peak) if fp64_peak else None,
-              "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
+              "frac_of_burst": (ach / bf16) if bf16 else None,
+              "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained, of measured",
               "share_of_step": st["sliced_gemm_ms"] / step_ms_total,
               "launches": st["sliced_gemm_launches"],
               "ms_per_launch": st["sliced_gemm_ms"] / st["sliced_gemm_launches"]}
@@ -343,29 +481,34 @@ def main():
     cands.sort(key=lambda r: -r["share_of_step"])
     roof = cands[0] if cands else None
     roof_other = cands[1] if len(cands) > 1 else None
-    ladder = None
-    if st["ladder_launches"]:
-        ach = st["ladder_flops"] / (st["ladder_ms"] * 1e-3) / 1e12
-        ladder = {"achieved": ach, "unit": "TFLOP/s", "ms_per_launch": st["ladder_ms"] / st["ladder_launches"],
-                  "launches": st["ladder_launches"]}
     if rank == 0:
         cfg = {"workload": WORKLOAD, "no": NO, "nv": NV, "naux": h.naux, "seed": SEED,
-               "precision": args.precision, "ccsd_iterations": iters,
-               "mixed_iterations": st["mixed_iterations"] if args.precision == "mixed" else 0,
+               "precision": args.precision, "learned_guess": use_guess, "sweeps_per_step": sweeps,
                "r_convergence": 1e-10, "e_ccsd": e_ref[0], "e_t": e_ref[1], "wall_s_per_step": wall / args.steps,
+               "guess_ms_per_step": st["guess_ms"] / args.steps,
                "ccsd_ms_per_step": st["ccsd_ms"] / args.steps, "triples_ms_per_step": st["triples_ms"] / args.steps,
-               "l2": "inputs larger than L2 (vvvv block %.1f GB)" % (8.0 * NV**4 / 1e9), "parallelism": f"replicas x{world}"}
+               "flop_iterations": it_flops,
+               "flop_iterations_source": "the FP64 form's CCSD iteration count (the reference's)" if fp64
+               else "this solve's sweeps (no FP64 run)",
+               "l2": "inputs larger than L2 (vvvv block %.1f GB)" % (8.0 * NV**4 / 1e9),
+               "parallelism": f"replicas x{world}"}
+        if use_guess:
+            cfg["guess_training"] = guess_info
+            cfg["mp2_guess_solve"] = mp2_start
+            cfg["iterations_saved"] = mp2_start["sweeps"]["total"] - sweeps["total"]
+            cfg["ccsd_ms_saved_net_of_guess"] = mp2_start["ccsd_ms"] - (st["ccsd_ms"] + st["guess_ms"]) / args.steps
         if fp64:
             cfg["fp64_gpu"] = fp64
             cfg["speedup_vs_fp64_gpu"] = fp64["ms_per_step"] / ms_dev
             cfg["abs_dE_ccsd_vs_fp64"] = abs(e_ref[0] - fp64["e_ccsd"])
             cfg["abs_dE_t_vs_fp64"] = abs(e_ref[1] - fp64["e_t"])
-        if ladder:
-            cfg["ladder"] = ladder
+            cfg["abs_dE_total_vs_fp64"] = abs(e_ref[0] + e_ref[1] - fp64["e_ccsd"] - fp64["e_t"])
+            cfg["max_abs_dT2_vs_fp64"] = dt2
+            cfg["within_1_uEh"] = cfg["abs_dE_total_vs_fp64"] <= 1e-6
         line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None,
-                "dtype": "f64" if args.precision == "fp64" else "bf16x3-split + bf16x45-sliced-f64, f32-acc, f64 epilogue",
+                "dtype": "f64" if not mixed else "bf16x3-split + bf16x45-sliced-f64 + f16 guess net, f32-acc, f64 epilogue",
                 "data": "synthetic", "config": cfg,
                 "e2e": {"value": e2e_value, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
                         "h2d_bytes_per_step": int(Bp.numel() * 8 + Fp.numel() * 8), "d2h_bytes_per_step": 16},

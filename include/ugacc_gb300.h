@@ -260,6 +260,7 @@ typedef struct ucc_stats {
   double sliced_gemm_ms;     /* device time of the sliced FP64 tensor-core GEMMs (slicing included) */
   double sliced_gemm_flops;  /* their algorithmic FLOPs, 2*M*N*K per GEMM */
   int64_t sliced_gemm_launches;
+  double guess_ms;           /* device time of the learned-guess pass (ucc_mlp_guess, CUDA events) */
 } ucc_stats;
 ucc_status ucc_get_stats(ucc_ctx* ctx, ucc_stats* out);
 ucc_status ucc_reset_stats(ucc_ctx* ctx);

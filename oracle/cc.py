@@ -248,49 +248,79 @@ class CCWfn:
     def W3_ijk(self, i, j, k):  # ccwfn.cc:1388-1418
         H, t2 = self.H, self.t2
         Vovvv, Vooov = H.V("ovvv"), H.V("ooov")
-        W = ein("eab,ce->abc", Vovvv[i], t2[k, j])
-        W += ein("eac,be->abc", Vovvv[i], t2[j, k])
-        W += ein("eca,be->abc", Vovvv[k], t2[j, i])
-        W += ein("ecb,ae->abc", Vovvv[k], t2[i, j])
-        W += ein("ebc,ae->abc", Vovvv[j], t2[i, k])
-        W += ein("eba,ce->abc", Vovvv[j], t2[k, i])
-        W -= ein("mc,mab->abc", Vooov[j, k], t2[i])
-        W -= ein("mb,mac->abc", Vooov[k, j], t2[i])
-        W -= ein("mb,mca->abc", Vooov[i, j], t2[k])
-        W -= ein("ma,mcb->abc", Vooov[j, i], t2[k])
-        W -= ein("ma,mbc->abc", Vooov[k, i], t2[j])
-        W -= ein("mc,mba->abc", Vooov[i, k], t2[j])
+
+        def ct(X, Y, perm):
+            """sum_e X[x,e] Y[e,u,v] as one matrix product, indexed [x,u,v] and then
+            transposed to [a,b,c] by perm"""
+            n0, n1, n2 = X.shape[0], Y.shape[1], Y.shape[2]
+            return (X @ Y.reshape(Y.shape[0], n1 * n2)).reshape(n0, n1, n2).transpose(perm)
+
+        # each e-sum shares its output ordering with one m-sum: one transposed add per pair
+        pairs = [((t2[k, j], Vovvv[i]), (Vooov[j, k].T, t2[i]), (1, 2, 0)),  # eab,ce / mc,mab -> abc
+                 ((t2[j, k], Vovvv[i]), (Vooov[k, j].T, t2[i]), (1, 0, 2)),  # eac,be / mb,mac
+                 ((t2[j, i], Vovvv[k]), (Vooov[i, j].T, t2[k]), (2, 0, 1)),  # eca,be / mb,mca
+                 ((t2[i, j], Vovvv[k]), (Vooov[j, i].T, t2[k]), (0, 2, 1)),  # ecb,ae / ma,mcb
+                 ((t2[i, k], Vovvv[j]), (Vooov[k, i].T, t2[j]), (0, 1, 2)),  # ebc,ae / ma,mbc
+                 ((t2[k, i], Vovvv[j]), (Vooov[i, k].T, t2[j]), (2, 1, 0))]  # eba,ce / mc,mba
+        W = None
+        for (Xe, Ye), (Xm, Ym), perm in pairs:
+            G = ct(Xe, Ye, (0, 1, 2))
+            G -= ct(Xm, Ym, (0, 1, 2))
+            if W is None:
+                W = np.ascontiguousarray(G.transpose(perm))
+            else:
+                W += G.transpose(perm)
         return W
 
-    def tcorr_tjl(self):  # ccwfn.cc:795-852
-        H, t1 = self.H, self.t1
+    # the six orderings of (a,b,c) that the energy expression reads, as the positions of
+    # the triple that index W3: (0,2,1) is W3[a][c][b], (2,0,1) is W3[c][a][b], and so on
+    PERMS = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (2, 0, 1), (1, 2, 0), (2, 1, 0)]
+
+    def tuple_setup(self):
+        """What every (T) tuple term uses, on the a >= b >= c triples only (in C order):
+        the occupied energies, the triples (a,b,c), the degeneracy divisor
+        1 + [a==b] + [a==c] + [b==c] and e_a + e_b + e_c."""
+        H = self.H
         no, nv = H.no, H.nv
-        Voovv = H.V("oovv")
         eo = np.diag(H.f)[:no]
         ev = np.diag(H.f)[no:]
         a_, b_, c_ = np.meshgrid(np.arange(nv), np.arange(nv), np.arange(nv), indexing="ij")
-        deg = 1.0 + (a_ == b_) + (a_ == c_) + (b_ == c_)
-        mask = (a_ >= b_) & (b_ >= c_)
-        dv = ev[:, None, None] + ev[None, :, None] + ev[None, None, :]
+        a, b, c = np.nonzero((a_ >= b_) & (b_ >= c_))
+        deg = 1.0 + (a == b) + (a == c) + (b == c)
+        dv = ev[a] + ev[b] + ev[c]
+        return eo, (a, b, c), deg, dv
+
+    def tcorr_tuple(self, i, j, k, setup=None):  # ccwfn.cc:813-849: the term of one i >= j >= k
+        H, t1 = self.H, self.t1
+        nv = H.nv
+        Voovv = H.V("oovv")
+        eo, abc, deg, dv = setup if setup is not None else self.tuple_setup()
+        Wf = self.W3_ijk(i, j, k).ravel()
+        Vij, Vik, Vjk = Voovv[i, j], Voovv[i, k], Voovv[j, k]
+        P, Q = {}, {}
+        for p in self.PERMS:  # W3 and V3 at (x,y,z) = the triple in ordering p
+            x, y, z = abc[p[0]], abc[p[1]], abc[p[2]]
+            w = Wf[(x * nv + y) * nv + z]
+            P[p] = w
+            Q[p] = (w + Vij[x, y] * t1[k, z] + Vik[x, z] * t1[j, y] + Vjk[y, z] * t1[i, x]) / deg
+        X3 = sum(P[p] * Q[p] for p in self.PERMS)
+        Y3 = Q[(0, 1, 2)] + Q[(2, 0, 1)] + Q[(1, 2, 0)]  # V3[abc] + V3[cab] + V3[bca]
+        Z3 = Q[(0, 2, 1)] + Q[(1, 0, 2)] + Q[(2, 1, 0)]  # V3[acb] + V3[bac] + V3[cba]
+        Wp = P[(0, 1, 2)] + P[(2, 0, 1)] + P[(1, 2, 0)]
+        Wm = P[(0, 2, 1)] + P[(1, 0, 2)] + P[(2, 1, 0)]
+        d3 = eo[i] + eo[j] + eo[k] - dv
+        fac = 2.0 - ((i == j) + (i == k) + (j == k))
+        term = ((Y3 - 2.0 * Z3) * Wp + (Z3 - 2.0 * Y3) * Wm + 3.0 * X3) * fac / d3
+        return term.sum()
+
+    def tcorr_tjl(self):  # ccwfn.cc:795-852
+        no = self.H.no
+        setup = self.tuple_setup()
         ET = 0.0
         for i in range(no):
             for j in range(i + 1):
                 for k in range(j + 1):
-                    W = self.W3_ijk(i, j, k)
-                    V = (W + ein("ab,c->abc", Voovv[i, j], t1[k]) + ein("ac,b->abc", Voovv[i, k], t1[j])
-                         + ein("bc,a->abc", Voovv[j, k], t1[i])) / deg
-                    P = {p: W.transpose(p) for p in [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]}
-                    Q = {p: V.transpose(p) for p in P}
-                    # W3[a][c][b] as an array indexed [a,b,c] is W.transpose(0,2,1), etc.
-                    X3 = sum(P[p] * Q[p] for p in P)
-                    Y3 = V + Q[(1, 2, 0)] + Q[(2, 0, 1)]
-                    Z3 = Q[(0, 2, 1)] + Q[(1, 0, 2)] + Q[(2, 1, 0)]
-                    Wp = W + P[(1, 2, 0)] + P[(2, 0, 1)]
-                    Wm = P[(0, 2, 1)] + P[(1, 0, 2)] + P[(2, 1, 0)]
-                    d3 = eo[i] + eo[j] + eo[k] - dv
-                    fac = 2.0 - ((i == j) + (i == k) + (j == k))
-                    term = ((Y3 - 2.0 * Z3) * Wp + (Z3 - 2.0 * Y3) * Wm + 3.0 * X3) * fac / d3
-                    ET += term[mask].sum()
+                    ET += self.tcorr_tuple(i, j, k, setup)
         return ET
 
     # ------------------------------------------------- (T) gradient pieces

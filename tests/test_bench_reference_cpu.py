@@ -17,7 +17,7 @@ def _run(*args):
 
 
 def test_reference_arm_line():
-    line = _run("--steps", "1", "--warmup", "0")
+    line = _run("--workload", "c2", "--steps", "1", "--warmup", "0")
     for k in KEYS:
         assert k in line, k
     assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "TFLOP/s"
@@ -27,6 +27,13 @@ def test_reference_arm_line():
     assert rec["cores"] == 1 and rec["ccsd_s"] > 3600 and rec["ccsd_iterations"] == 10
 
 
-def test_reference_arm_reports_unavailable_where_the_cpu_path_cannot_run():
-    line = _run("--workload", "c3", "--steps", "1", "--warmup", "0")
-    assert line["impl"] == "reference" and "unavailable" in line
+def test_reference_arm_samples_triples_tuples_at_the_default_workload():
+    """no=32/nv=320: the CPU CCSD iteration needs <ab|ef> (84 GB); each step is one (T)
+    tuple term of the oracle instead, with the same metric and unit as the GPU arm."""
+    line = _run("--steps", "1", "--warmup", "0")
+    for k in KEYS:
+        assert k in line, k
+    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "TFLOP/s"
+    assert line["config"]["workload"] == "ccsd_t_no32_nv320_seed2"
+    assert "tuple" in line["config"]["step"] and line["cpu_baseline"]["kind"] == "port"
+    assert line["e2e"]["value"] == line["value"] and line["e2e"]["d2h_bytes_per_step"] == 0

@@ -56,7 +56,7 @@ class Stats(ctypes.Structure):
                 ("anchored_iterations", ctypes.c_int), ("fp64_gemm_ms", ctypes.c_double),
                 ("fp64_gemm_flops", ctypes.c_double), ("fp64_gemm_launches", ctypes.c_int64),
                 ("sliced_gemm_ms", ctypes.c_double), ("sliced_gemm_flops", ctypes.c_double),
-                ("sliced_gemm_launches", ctypes.c_int64)]
+                ("sliced_gemm_launches", ctypes.c_int64), ("guess_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -129,9 +129,18 @@ ucc_status ucc_ctx_create(ucc_ctx** out, int device) {
 
 ucc_status ucc_ctx_destroy(ucc_ctx* ctx) {
   if (!ctx) return UCC_BAD_ARGS;
-  cudaSetDevice(ctx->c.device);
+  const int device = ctx->c.device;
+  cudaSetDevice(device);
   cudaStreamSynchronize(ctx->c.stream);
   delete ctx;
+  // the context's scratch went back to the device's stream-ordered pool, which keeps it
+  // (release threshold: keep); hand it back to the device so that later cudaMalloc calls
+  // (cached tensor-core operands of the next context) can use it
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    cudaDeviceSynchronize();
+    cudaMemPoolTrimTo(pool, 0);
+  }
   return UCC_OK;
 }
 

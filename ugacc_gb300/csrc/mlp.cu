@@ -781,6 +781,8 @@ void mlp_guess(Ctx& c, ucc_mlp* net) {
   const int64_t ntiles = (n + kGuessRows - 1) / kGuessRows;
   Scratch errflag(c, sizeof(int));
   UCC_CUDA(cudaMemsetAsync(errflag.p, 0, sizeof(int), c.stream));
+  Timer timer(c.stream);
+  timer.start();
   guess_tc_kernel<<<(unsigned)std::min<int64_t>(ntiles, sms), kGuessThreads, kGuessSmem, c.stream>>>(
       no, nv, n, c.get("Voovv").p, c.get("eps").p, vv, oo, ov1, ov2, net->wh, net->w, net->oW1(), net->oW2(),
       net->ow3(), net->ob1(), net->ob2(), net->ob3(), g + n1, static_cast<int*>(errflag.p));
@@ -788,7 +790,7 @@ void mlp_guess(Ctx& c, ucc_mlp* net) {
   UCC_CUDA(cudaGetLastError());
   int herr = 0;
   UCC_CUDA(cudaMemcpyAsync(&herr, errflag.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  UCC_CUDA(cudaStreamSynchronize(c.stream));
+  c.stats.guess_ms += timer.stop_ms();
   UCC_REQUIRE(!herr, UCC_DEVICE_TIMEOUT, "guess network: a tensor-core wait timed out");
 }
 }  // namespace ucc
