@@ -64,8 +64,10 @@ def test_mixed_triples_matches_fp64():
     H.ctx.reset_stats()
     emx = mx.triples()
     assert H.ctx.stats()["tc_gemm_launches"] == 3  # one batched launch per pair of W3 terms
-    # split products carry ~2^-16 relative error into W3; E(T) is a weighted sum of W3*V3
-    assert abs(emx - e64) < 1e-8 + 1e-4 * abs(e64)
+    # split products carry ~2^-16 relative error into W3; E(T) is a weighted sum of W3*V3;
+    # never looser than 1 uEh absolute (tests/test_gpu_large.py checks that bound where
+    # |E(T)| is several mEh)
+    assert abs(emx - e64) < min(1e-6, 1e-8 + 1e-4 * abs(e64))
 
 
 def _lambda_response(h, precision, hand):

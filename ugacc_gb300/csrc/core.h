@@ -346,11 +346,13 @@ void lincomb(Ctx& c, int nvec, const double* const* d_vecs, const double* coef, 
 // (T) energy over a batch of (i>=j>=k) tuples, given W3 for each tuple.
 void triples_energy(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const double* W3,
                     const double* t1, const double* Voovv, const double* eps, double* d_partial);
-// The same from an FP32 W3 (mixed form): per-element arithmetic in FP32, the energy sum
-// in FP64 (compensated).
+// The same from an FP32 W3 (mixed form) held as nparts partial arrays part_stride floats
+// apart (W3 = their sum): per-element arithmetic in FP32, the energy sum in FP64
+// (compensated).
 int64_t triples_f32_partials(int nv);  // partial sums per tuple written by triples_energy_f32
-void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, const double* t1,
-                        const double* Voovv, const double* eps, double* d_partial);
+void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, int nparts,
+                        int64_t part_stride, const double* t1, const double* Voovv, const double* eps,
+                        double* d_partial);
 
 // Pair-symmetric particle ladder (sum_ef W_abef tau_ijef = S + sign A over packed pairs,
 // W and tau invariant under the simultaneous pair swap):

@@ -855,7 +855,9 @@ __global__ void triples_energy_kernel(int no, int nv, const int* tuples, const d
 }
 
 // FP32 W3 (mixed form): the per-element V3/X3/Y3/Z3 algebra in FP32, the sums in FP64.
-// Block (r, t) takes the sorted tile triple r (tiles
+// W3 arrives as up to three partial arrays (one per pair of W3 terms, each written without
+// a read-modify-write by its tensor-core GEMM), nparts * part_stride floats apart; their
+// sum is formed while staging.  Block (r, t) takes the sorted tile triple r (tiles
 // A >= B >= C of edge ET along the virtual axis) of tuple t and stages the six permutation
 // tiles W[A][B][C], W[A][C][B], ..., W[C][B][A] in shared memory with coalesced loads, so
 // every W3 element is read from memory once; the Voovv blocks and t1 / eps pieces of the
@@ -868,7 +870,8 @@ constexpr int TNT = 128;
 static_assert(TNT == 2 * ET * ET && (ET * ET * ET) % TNT == 0 && (6 * ET * ET) % TNT == 0, "tile/thread layout");
 __global__ void __launch_bounds__(TNT) triples_energy_f32_tiled_kernel(int no, int nv, const int* __restrict__ tuples,
                                                                       const int* __restrict__ tri, int ntri,
-                                                                      const float* __restrict__ W3,
+                                                                      const float* __restrict__ W3, int nparts,
+                                                                      int64_t part_stride,
                                                                       const double* __restrict__ t1,
                                                                       const double* __restrict__ Voovv,
                                                                       const double* __restrict__ eps, double* partial) {
@@ -894,7 +897,13 @@ __global__ void __launch_bounds__(TNT) triples_energy_f32_tiled_kernel(int no, i
     const int p = it / (ET * ET * ET / TNT), x = tx + 2 * (it % (ET * ET * ET / TNT));
     const uint64_t code6 = kPerm >> (6 * p);
     const int gx = R0((int)(code6 & 3)) + x, gy = R0((int)((code6 >> 2) & 3)) + ty, gz = R0((int)((code6 >> 4) & 3)) + tz;
-    Ws[p][x][ty][tz] = (gx < nv && gy < nv && gz < nv) ? W[(int64_t)gx * nv2 + (int64_t)gy * nv + gz] : 0.f;
+    float w = 0.f;
+    if (gx < nv && gy < nv && gz < nv) {
+      const int64_t o = (int64_t)gx * nv2 + (int64_t)gy * nv + gz;
+      w = W[o];
+      for (int q = 1; q < nparts; q++) w += W[o + q * part_stride];
+    }
+    Ws[p][x][ty][tz] = w;
   }
   auto Vm = [&](int m) {  // Vij, Vik, Vjk
     return Voovv + ((m == 2 ? (int64_t)j : (int64_t)i) * no + (m == 0 ? j : k)) * nv2;
@@ -1081,8 +1090,9 @@ void unpack_ladder(Ctx& c, int no, int nv, double alpha, const double* S, const 
   check_launch("unpack_ladder");
 }
 
-void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, const double* t1,
-                        const double* Voovv, const double* eps, double* d_partial) {
+void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, int nparts,
+                        int64_t part_stride, const double* t1, const double* Voovv, const double* eps,
+                        double* d_partial) {
   UCC_REQUIRE(ntuple <= 65535, UCC_BAD_ARGS, "triples_energy: too many tuples per batch");
   const int T = (nv + ET - 1) / ET;
   UCC_REQUIRE(T <= 1024, UCC_BAD_ARGS, "triples_energy: too many virtual tiles");
@@ -1094,7 +1104,8 @@ void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples,
   UCC_CUDA(cudaMemcpyAsync(dtri.p, tri.data(), sizeof(int) * tri.size(), cudaMemcpyHostToDevice, c.stream));
   dim3 grid((unsigned)tri.size(), (unsigned)ntuple);
   triples_energy_f32_tiled_kernel<<<grid, TNT, 0, c.stream>>>(no, nv, d_tuples, static_cast<const int*>(dtri.p),
-                                                             (int)tri.size(), W3, t1, Voovv, eps, d_partial);
+                                                             (int)tri.size(), W3, nparts, part_stride, t1, Voovv,
+                                                             eps, d_partial);
   count_launch();
   check_launch("triples_energy_f32");
   UCC_CUDA(cudaStreamSynchronize(c.stream));  // the tile list is freed on return

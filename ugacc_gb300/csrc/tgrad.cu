@@ -49,9 +49,11 @@ void triples_w3_fp64(Ctx& c, const Tensor& Acat, const Tensor& Bcat, const int* 
 
 namespace {
 
-// W3 (FP64, or FP32 from the tensor-core tuple GEMMs) -> M3; N3
+// W3 (FP64, or FP32 from the tensor-core tuple GEMMs: nparts partial arrays part_stride
+// elements apart, W3 = their sum) -> M3; N3
 template <typename TW>
-__global__ void tg_prep_kernel(int no, int nv, int nt, const int* __restrict__ tuples, const TW* W, double* M, double* N,
+__global__ void tg_prep_kernel(int no, int nv, int nt, const int* __restrict__ tuples, const TW* W, int nparts,
+                               int64_t part_stride, double* M, double* N,
                                const double* __restrict__ eps, const double* __restrict__ t1,
                                const double* __restrict__ t2, const double* __restrict__ Voovv,
                                const double* __restrict__ fov) {
@@ -73,7 +75,9 @@ __global__ void tg_prep_kernel(int no, int nv, int nt, const int* __restrict__ t
                        t2[ij + (int64_t)a * nv + b] * fov[(int64_t)k * nv + c] +
                        t2[ik + (int64_t)a * nv + c] * fov[(int64_t)j * nv + b] +
                        t2[jk + (int64_t)b * nv + c] * fov[(int64_t)i * nv + a];
-    M[x] = (double)W[x] / D;
+    TW w = W[x];
+    for (int q = 1; q < nparts; q++) w += W[x + q * part_stride];
+    M[x] = (double)w / D;
     N[x] = num / D;
   }
 }
@@ -193,14 +197,17 @@ void run_triples_gradient(Ctx& c) {
   size_t free_b = 0, total_b = 0;
   UCC_CUDA(cudaMemGetInfo(&free_b, &total_b));
   const double budget = std::min<double>(24.0e9, 0.3 * (double)free_b);
-  const double nbuf = full ? 8.0 : 6.0;  // + P3 and a gathered copy for the full Doo/Dvv
+  // FP64 arrays per tuple (+ P3 and a gathered copy for the full Doo/Dvv), plus the mixed
+  // form's three FP32 W3 partials (12 bytes per element)
+  const double nbuf = (full ? 8.0 : 6.0) + (mixed ? 1.5 : 0.0);
   const int nj = (int)std::max<int64_t>(1, std::min<int64_t>(no, (int64_t)(budget / (nbuf * 8.0 * nv3 * no))));
   const int ntmax = nj * no;
   Tensor Acat, Bcat;
   const bool tc = mixed && mixed_triples_prepare(c, ntmax);
   if (!tc) triples_operands_fp64(c, Acat, Bcat);
   std::unique_ptr<Scratch> W32;
-  if (tc) W32 = std::make_unique<Scratch>(c, sizeof(float) * nv3 * ntmax);
+  // the tensor-core tuple GEMMs write W3 as three partial arrays (one per pair of terms)
+  if (tc) W32 = std::make_unique<Scratch>(c, 3 * sizeof(float) * nv3 * ntmax);
   Scratch Mb(c, sizeof(double) * nv3 * ntmax), Nb(c, sizeof(double) * nv3 * ntmax);
   Scratch Qb(c, sizeof(double) * nv3 * ntmax), Zb(c, sizeof(double) * nv3 * ntmax);
   std::unique_ptr<Scratch> Pb, diag;
@@ -239,12 +246,12 @@ void run_triples_gradient(Ctx& c) {
       if (tc) {
         mixed_triples_batch(c, nt, tuples.data(), static_cast<float*>(W32->p));
         tg_prep_kernel<float><<<g, 256, 0, c.stream>>>(no, nv, nt, static_cast<int*>(dtup.p),
-                                                       static_cast<const float*>(W32->p), Mb.d(), Nb.d(), eps, t1.p,
-                                                       t2.p, Voovv, fov);
+                                                       static_cast<const float*>(W32->p), 3, (int64_t)nt * nv3,
+                                                       Mb.d(), Nb.d(), eps, t1.p, t2.p, Voovv, fov);
       } else {
         triples_w3_fp64(c, Acat, Bcat, tuples.data(), nt, Mb.d(), static_cast<GemmPtrs*>(dptr.p));
-        tg_prep_kernel<double><<<g, 256, 0, c.stream>>>(no, nv, nt, static_cast<int*>(dtup.p), Mb.d(), Mb.d(),
-                                                        Nb.d(), eps, t1.p, t2.p, Voovv, fov);
+        tg_prep_kernel<double><<<g, 256, 0, c.stream>>>(no, nv, nt, static_cast<int*>(dtup.p), Mb.d(), 1, 0,
+                                                        Mb.d(), Nb.d(), eps, t1.p, t2.p, Voovv, fov);
       }
       count_kernel_launch();
       UCC_REQUIRE(nt <= 65535, UCC_BAD_ARGS, "(T) gradient: too many tuples per batch");

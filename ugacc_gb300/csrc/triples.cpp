@@ -89,12 +89,16 @@ double run_triples(Ctx& c) {
   size_t free_b = 0, total_b = 0;
   UCC_CUDA(cudaMemGetInfo(&free_b, &total_b));
   const double budget = std::min<double>(8.0e9, 0.25 * (double)free_b);
-  const int batch = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)(budget / (8.0 * nv3)), 4096, ntup}));
+  // W3 bytes per tuple: FP64, or three FP32 partial arrays (one per pair of terms) in the
+  // mixed form
+  const bool want_mixed = c.opt.precision == UCC_MIXED && !c.force_fp64;
+  const double w3_bytes = (want_mixed ? 12.0 : 8.0) * (double)nv3;
+  const int batch = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)(budget / w3_bytes), 4096, ntup}));
 
   Scratch dtup(c, sizeof(int) * tuples.size());
   UCC_CUDA(cudaMemcpyAsync(dtup.p, tuples.data(), sizeof(int) * tuples.size(), cudaMemcpyHostToDevice, c.stream));
-  Scratch W3(c, sizeof(double) * nv3 * batch);
-  const bool mixed = c.opt.precision == UCC_MIXED && !c.force_fp64 && mixed_triples_prepare(c, batch);
+  Scratch W3(c, (size_t)std::ceil(w3_bytes) * batch);
+  const bool mixed = want_mixed && mixed_triples_prepare(c, batch);
   // per-tuple partial sums: one per virtual index a (FP64 kernel) or per virtual tile triple (FP32)
   const int64_t pstride = mixed ? triples_f32_partials(nv) : nv;
   Scratch partial(c, sizeof(double) * (size_t)ntup * pstride);
@@ -111,8 +115,9 @@ double run_triples(Ctx& c) {
     else
       triples_w3_fp64(c, Acat, Bcat, tuples.data() + 3 * t0, nb, W3.d(), dp);
     if (mixed)
-      triples_energy_f32(c, no, nv, nb, static_cast<int*>(dtup.p) + 3 * t0, static_cast<const float*>(W3.p), t1.p,
-                         c.get("Voovv").p, c.get("eps").p, partial.d() + (int64_t)t0 * pstride);
+      triples_energy_f32(c, no, nv, nb, static_cast<int*>(dtup.p) + 3 * t0, static_cast<const float*>(W3.p), 3,
+                         (int64_t)nb * nv3, t1.p, c.get("Voovv").p, c.get("eps").p,
+                         partial.d() + (int64_t)t0 * pstride);
     else
       triples_energy(c, no, nv, nb, static_cast<int*>(dtup.p) + 3 * t0, W3.d(), t1.p, c.get("Voovv").p,
                      c.get("eps").p, partial.d() + (int64_t)t0 * nv);
