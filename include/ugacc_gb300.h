@@ -216,15 +216,22 @@ ucc_status ucc_mlp_guess(ucc_ctx* ctx, ucc_mlp* net);
 typedef struct ucc_batch ucc_batch;
 typedef struct ucc_batch_info {
   int members;
-  int sweeps;              /* graph launches of the last solve */
+  int sweeps;              /* sweeps of the last solve (all of them inside one graph launch) */
   int grouped_ops;         /* recorded residual operations, each one grouped launch per sweep */
   int graph_kernels;       /* kernel nodes in the sweep graph */
   int shape_choice[4];     /* GEMM operations given tile 64x64, 32x32, 64x32, 32x64 by the autotuner */
   double solve_ms;         /* device time of the last solve (CUDA events) */
   double flops;            /* algorithmic CCSD FLOPs of the last solve, summed over members' iterations */
   double arena_bytes;      /* recorded scratch held for the members */
+  int graph_launches;      /* host graph launches of the last solve (1: the sweep loop runs on the device) */
 } ucc_batch_info;
 ucc_status ucc_batch_create(ucc_batch** out, int device);
+/* Device time limit of one ucc_batch_ccsd sweep loop (default 600 s): the loop runs on the
+ * device inside a single graph launch and ends when no member is iterating, every member
+ * has reached MAXITER, or this much globaltimer time has passed since the solve started;
+ * the last case returns UCC_DEVICE_TIMEOUT (members keep their last amplitudes and the
+ * batch stays usable). */
+ucc_status ucc_batch_set_time_limit(ucc_batch* b, double seconds);
 ucc_status ucc_batch_destroy(ucc_batch* b);
 const char* ucc_batch_last_error(ucc_batch* b);
 /* add a member from its Fock matrix [nact][nact] and factors B[naux][nact][nact] */

@@ -65,7 +65,7 @@ class Stats(ctypes.Structure):
 class BatchInfo(ctypes.Structure):
     _fields_ = [("members", ctypes.c_int), ("sweeps", ctypes.c_int), ("grouped_ops", ctypes.c_int),
                 ("graph_kernels", ctypes.c_int), ("shape_choice", ctypes.c_int * 4), ("solve_ms", ctypes.c_double),
-                ("flops", ctypes.c_double), ("arena_bytes", ctypes.c_double)]
+                ("flops", ctypes.c_double), ("arena_bytes", ctypes.c_double), ("graph_launches", ctypes.c_int)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -136,6 +136,7 @@ def load_library(path: str | None = None):
         "ucc_batch_add_df": (i, [vp, i, i, i, dp, dp, P(i)]),
         "ucc_batch_guess_mlp": (i, [vp, i, vp]),
         "ucc_batch_ccsd": (i, [vp, P(_Options), dp, P(i), P(i)]),
+        "ucc_batch_set_time_limit": (i, [vp, d]),
         "ucc_batch_get_info": (i, [vp, P(BatchInfo)]),
         "ucc_batch_get_t2": (i, [vp, i, dp, ctypes.c_size_t]),
         "ucc_batch_features": (i, [vp, i, fp, ctypes.c_size_t, i, fp]),
@@ -580,7 +581,8 @@ def mlp_features(H: "Hamiltonian", with_targets: bool = False):
 # Batched CCSD over many Hamiltonians
 # ------------------------------------------------------------------------------------
 class Batch:
-    """Many small Hamiltonians solved together (ucc_batch_*): one graph launch per sweep."""
+    """Many small Hamiltonians solved together (ucc_batch_*): the whole solve is one graph
+    launch whose sweep loop runs on the device."""
 
     def __init__(self, device: int = 0):
         self.lib = load_library()
@@ -606,6 +608,10 @@ class Batch:
 
     def guess(self, index: int, net: "MLP"):
         self.check(self.lib.ucc_batch_guess_mlp(self.h, index, net.h))
+
+    def set_time_limit(self, seconds: float):
+        """Device time limit of the next solves' sweep loop (UCC_DEVICE_TIMEOUT when it runs out)."""
+        self.check(self.lib.ucc_batch_set_time_limit(self.h, float(seconds)))
 
     def ccsd(self, options: dict | None = None):
         """Energies, iteration counts and convergence flags of every member."""

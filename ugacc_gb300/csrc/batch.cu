@@ -14,10 +14,14 @@
 //
 // The rest of a sweep (Jacobi update, residual norm, convergence mask, DIIS with its
 // B-matrix rows, subspace solve and extrapolation, tau/ttau, energy) is written directly
-// as grouped kernels over (member, chunk).  The whole sweep is captured once as a CUDA
-// graph; the host launches the graph and reads back only the count of members still
-// iterating.  A member whose ||R|| drops below R_CONVERGENCE is masked out of every later
-// kernel, so it ends exactly where the one-member solver would (ccwfn.cc:188-258).
+// as grouped kernels over (member, chunk).  The whole solve is ONE graph launch: a CUDA
+// graph whose while-node repeats the captured sweep on the device; the sweep's last
+// kernel sets the loop condition from the count of members still iterating, so the host
+// neither launches nor waits per sweep.  A member whose ||R|| drops below R_CONVERGENCE is
+// masked out of every later kernel, so it ends exactly where the one-member solver would
+// (ccwfn.cc:188-258).  The loop is bounded twice on the device: by MAXITER (members stop
+// iterating) and by a time limit on the globaltimer, after which the loop ends and the
+// call reports UCC_DEVICE_TIMEOUT with the batch still usable.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -80,7 +84,32 @@ struct SweepState {  // device-side bookkeeping shared by all members
   int active_count;
   double r_conv;
   int maxiter;
+  unsigned long long t0;        // globaltimer at the start of the solve
+  unsigned long long limit_ns;  // device time limit of the sweep loop
+  int timed_out;                // the loop ended on the time limit with members still iterating
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// first node of the solve graph: the clock of the time limit
+__global__ void solve_start_kernel(SweepState* st) {
+  st->t0 = global_ns();
+  st->timed_out = 0;
+}
+
+// last node of every sweep: repeat while members are iterating and time is left
+__global__ void loop_control_kernel(cudaGraphConditionalHandle loop, SweepState* st) {
+  unsigned int again = st->active_count > 0 ? 1u : 0u;
+  if (again && global_ns() - st->t0 > st->limit_ns) {
+    st->timed_out = 1;
+    again = 0u;
+  }
+  cudaGraphSetConditional(loop, again);
+}
 
 __device__ __forceinline__ int find_item(const int64_t* __restrict__ prefix, int n, int64_t t) {
   int lo = 0, hi = n - 1;
@@ -546,6 +575,7 @@ struct ucc_batch {
   cudaGraphExec_t exec = nullptr;
   int graph_kernels = 0;
   int use_diis = -1;
+  double time_limit_s = 600.0;  // device time limit of one solve's sweep loop
   ucc_batch_info info{};
 
   ~ucc_batch() {
@@ -840,6 +870,7 @@ int enqueue_sweep(ucc_batch& B) {
   return k;
 }
 
+// the solve graph: start node -> while(members iterating) { sweep kernels; loop control }
 void capture(ucc_batch& B, bool diis) {
   if (B.exec && B.use_diis == (int)diis) return;
   if (B.exec) cudaGraphExecDestroy(B.exec);
@@ -847,17 +878,39 @@ void capture(ucc_batch& B, bool diis) {
   B.exec = nullptr;
   B.graph = nullptr;
   B.use_diis = diis;
-  UCC_CUDA(cudaStreamBeginCapture(B.stream, cudaStreamCaptureModeThreadLocal));
+  UCC_CUDA(cudaGraphCreate(&B.graph, 0));
+  SweepState* stp = B.state.p;
+  void* start_args[] = {&stp};
+  cudaKernelNodeParams kp = {};
+  kp.func = (void*)solve_start_kernel;
+  kp.gridDim = dim3(1);
+  kp.blockDim = dim3(1);
+  kp.kernelParams = start_args;
+  cudaGraphNode_t start = nullptr, loop = nullptr;
+  UCC_CUDA(cudaGraphAddKernelNode(&start, B.graph, nullptr, 0, &kp));
+  cudaGraphConditionalHandle handle;
+  UCC_CUDA(cudaGraphConditionalHandleCreate(&handle, B.graph, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = handle;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  UCC_CUDA(cudaGraphAddNode(&loop, B.graph, &start, nullptr, 1, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  UCC_CUDA(cudaStreamBeginCaptureToGraph(B.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   int k = 0;
   try {
     k = enqueue_sweep(B);
+    loop_control_kernel<<<1, 1, 0, B.stream>>>(handle, B.state.p);
+    UCC_CUDA(cudaGetLastError());
+    k++;
   } catch (...) {
     cudaGraph_t g = nullptr;
     cudaStreamEndCapture(B.stream, &g);
-    if (g) cudaGraphDestroy(g);
     throw;
   }
-  UCC_CUDA(cudaStreamEndCapture(B.stream, &B.graph));
+  cudaGraph_t captured = nullptr;
+  UCC_CUDA(cudaStreamEndCapture(B.stream, &captured));
   UCC_CUDA(cudaGraphInstantiate(&B.exec, B.graph, 0));
   B.graph_kernels = k;
   B.info.graph_kernels = k;
@@ -966,7 +1019,8 @@ ucc_status ucc_batch_ccsd(ucc_batch* b, const ucc_options* opt, double* e_ccsd, 
     set_all_active(B);
     for (DevArray<int>* a : {&B.iterations, &B.converged, &B.status}) a->zeros((size_t)nm, B.stream);
     std::vector<SweepState> st(1);
-    st[0] = SweepState{0, 0, 0, 0, nm, opt->r_convergence, opt->maxiter};
+    st[0] = SweepState{0, 0, 0, 0, nm, opt->r_convergence, opt->maxiter, 0ull,
+                       (unsigned long long)(B.time_limit_s * 1e9), 0};
     B.state.upload(st, B.stream);
     // energies of the starting amplitudes (what a member that stops at once reports)
     std::vector<double> e0(nm);
@@ -976,16 +1030,16 @@ ucc_status ucc_batch_ccsd(ucc_batch* b, const ucc_options* opt, double* e_ccsd, 
     UCC_CUDA(cudaEventCreate(&t0));
     UCC_CUDA(cudaEventCreate(&t1));
     UCC_CUDA(cudaEventRecord(t0, B.stream));
-    int sweeps = 0, left = nm;
-    for (int it = 0; it < opt->maxiter && left > 0; it++) {
-      UCC_CUDA(cudaGraphLaunch(B.exec, B.stream));
-      sweeps++;
-      for (int k = 0; k < B.graph_kernels; k++) count_kernel_launch();
-      UCC_CUDA(cudaMemcpyAsync(&left, &B.state.p->active_count, sizeof(int), cudaMemcpyDeviceToHost, B.stream));
-      UCC_CUDA(cudaStreamSynchronize(B.stream));
-    }
+    // the whole solve: one graph launch, the sweep loop runs on the device
+    UCC_CUDA(cudaGraphLaunch(B.exec, B.stream));
+    B.info.graph_launches = 1;
     UCC_CUDA(cudaEventRecord(t1, B.stream));
     UCC_CUDA(cudaEventSynchronize(t1));
+    SweepState fin;
+    UCC_CUDA(cudaMemcpy(&fin, B.state.p, sizeof(SweepState), cudaMemcpyDeviceToHost));
+    const int sweeps = fin.iter;
+    count_kernel_launch();  // the start node
+    for (int k = 0; k < sweeps * B.graph_kernels; k++) count_kernel_launch();
     float ms = 0.f;
     cudaEventElapsedTime(&ms, t0, t1);
     cudaEventDestroy(t0);
@@ -1001,6 +1055,17 @@ ucc_status ucc_batch_ccsd(ucc_batch* b, const ucc_options* opt, double* e_ccsd, 
     B.info.sweeps = sweeps;
     B.info.solve_ms = ms;
     B.info.flops = fl;
+    UCC_REQUIRE(!fin.timed_out, UCC_DEVICE_TIMEOUT,
+                "batched solve: the device time limit (" + std::to_string(B.time_limit_s) + " s) ran out after " +
+                    std::to_string(sweeps) + " sweeps with " + std::to_string(fin.active_count) +
+                    " members still iterating");
+  });
+}
+
+ucc_status ucc_batch_set_time_limit(ucc_batch* b, double seconds) {
+  return bguard(b, [&](ucc_batch& B) {
+    UCC_REQUIRE(seconds > 0.0 && seconds <= 86400.0, UCC_BAD_ARGS, "time limit must be in (0, 86400] s");
+    B.time_limit_s = seconds;
   });
 }
 
