@@ -46,6 +46,9 @@ inline int pick_bn(int64_t N) {
   const int64_t nt = (N + 255) / 256;
   return (int)(((N + nt - 1) / nt + 31) / 32 * 32);
 }
+// CTAs per cluster for a launch with mtiles M tiles: pairs that share the B tile whenever
+// there are two M tiles to pair (the B maps then have boxes of bn / 2 rows)
+inline int cluster_m(int mtiles) { return mtiles >= 2 ? 2 : 1; }
 
 // gemm_kernel: an operand ring of 216 KB (four 48 KB stages, or fused stages of
 // A_hi | A_lo | B_hi | B_lo), then the barriers
@@ -109,6 +112,12 @@ __device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
       "l"(a), "l"(b), "r"(IDESC), "r"(acc));
 }
+// CM CTAs per cluster along M (1 or 2).  With CM = 2 the two CTAs of a cluster take M tiles
+// 2j and 2j+1 of the same N tile: each loads half of the B tile's rows and multicasts it
+// into both CTAs' rings (the B tensor maps have boxes of bn / 2 rows), so every B byte
+// crosses from L2 once per pair; a ring stage is refilled only after the MMAs of both CTAs
+// released it (each MMA commit arrives on the stage's empty barrier in both CTAs).
+template <int CM>
 __global__ void __launch_bounds__(THREADS, 1)
     gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
                 const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
@@ -126,11 +135,13 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint32_t* tslot = (uint32_t*)(mdone + 1);
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int nst = p.fused ? p.nst : STAGES;  // ring stages (at most STAGES)
+  const int rank = CM > 1 ? (int)cluster_rank() : 0;
+  constexpr uint16_t kMask = (uint16_t)((1u << CM) - 1u);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&empty[s], CM);  // released by the MMAs of every CTA that reads the multicast B
     }
     for (int a = 0; a < 2; a++) {
       mbar_init(&tfull[a], 1);
@@ -147,9 +158,14 @@ __global__ void __launch_bounds__(THREADS, 1)
   fence_before();
   __syncthreads();
   fence_after();
+  if (CM > 1) cluster_sync();  // the peer's barriers exist before its multicasts or arrivals reach them
   const uint32_t tmem = *tslot;
-  const int tiles_per = p.mtiles * p.ntiles;
+  // M tiles in groups of CM (one per CTA of the cluster); the clusters walk the groups
+  const int mgroups = (p.mtiles + CM - 1) / CM;
+  const int tiles_per = mgroups * p.ntiles;
   const int ntile = tiles_per * (p.nprob ? p.nprob : (p.ksplit > 1 ? p.ksplit : 1));
+  const int cid = blockIdx.x / CM, ncl = gridDim.x / CM;
+  const int bh = p.bn / CM;  // B rows this CTA loads (for every CTA of the cluster)
   // ring items per K block and term: one fused stage, or one stage per split product
   const int nseg = p.fused ? 1 : (p.nparts == 3 ? 6 : 3);
   const uint32_t b_tile = (uint32_t)(p.bn * BK * 2);
@@ -162,11 +178,13 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t phase = 0;
       int64_t issued = 0;
       bool ok = true;
-      for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+      for (int tile = cid; tile < ntile && ok; tile += ncl) {
         const int pb = tile / tiles_per, tl = tile - pb * tiles_per;
-        const int mt = tl % p.mtiles, nt = tl / p.mtiles;
-        const int ar0 = (p.nprob ? p.a_row0[pb] : 0) + mt * BM, br0 = (p.nprob ? p.b_row0[pb] : 0) + nt * p.bn;
-        const int ar1 = p.nterms > 1 ? p.a_row1[pb] + mt * BM : 0, br1 = p.nterms > 1 ? p.b_row1[pb] + nt * p.bn : 0;
+        const int mt = (tl % mgroups) * CM + rank, nt = tl / mgroups;
+        const int ar0 = (p.nprob ? p.a_row0[pb] : 0) + mt * BM;
+        const int br0 = (p.nprob ? p.b_row0[pb] : 0) + nt * p.bn + rank * bh;
+        const int ar1 = p.nterms > 1 ? p.a_row1[pb] + mt * BM : 0;
+        const int br1 = p.nterms > 1 ? p.b_row1[pb] + nt * p.bn + rank * bh : 0;
         for (int ch = 0; ch < nch && ok; ch++) {
           int k0 = 0, kn = p.kblocks;
           if (p.ksplit > 1) {
@@ -183,13 +201,20 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             const int term = kb / (nseg * kn), w = kb - term * nseg * kn;
             const int seg = w / kn, kk = (k0 + w - seg * kn) * BK;
+            // this CTA's share of the B tile (all of it when CM = 1) goes to every CTA of the cluster
+            auto load_b = [&](uint8_t* dst, const CUtensorMap* map, int row) {
+              if (CM == 1)
+                tma_load(dst, map, &full[stage], kk, row);
+              else
+                tma_load_mc(dst + (size_t)rank * bh * BK * 2, map, &full[stage], kk, row, kMask);
+            };
             if (p.fused) {  // A_hi | A_lo | B_hi | B_lo of K block kk
               uint8_t* st = smem + (size_t)stage * p.stage_bytes;
               mbar_expect_tx(&full[stage], (uint32_t)(2 * A_BYTES) + 2 * b_tile);
               tma_load(st, term == 0 ? &mAhi : &mA2hi, &full[stage], kk, term == 0 ? ar0 : ar1);
               tma_load(st + A_BYTES, term == 0 ? &mAlo : &mA2lo, &full[stage], kk, term == 0 ? ar0 : ar1);
-              tma_load(st + 2 * A_BYTES, &mBhi, &full[stage], kk, term == 0 ? br0 : br1);
-              tma_load(st + 2 * A_BYTES + b_tile, &mBlo, &full[stage], kk, term == 0 ? br0 : br1);
+              load_b(st + 2 * A_BYTES, &mBhi, term == 0 ? br0 : br1);
+              load_b(st + 2 * A_BYTES + b_tile, &mBlo, term == 0 ? br0 : br1);
             } else {
               int pa, pbp;
               seg_parts(p.nparts, seg, pa, pbp);
@@ -198,7 +223,7 @@ __global__ void __launch_bounds__(THREADS, 1)
               const CUtensorMap* mb = pbp == 0 ? &mBhi : (pbp == 1 && p.nparts == 3) ? &mBmid : &mBlo;
               mbar_expect_tx(&full[stage], (uint32_t)A_BYTES + b_tile);
               tma_load(sA + stage * A_BYTES, ma, &full[stage], kk, term == 0 ? ar0 : ar1);
-              tma_load(sB + stage * B_BYTES, mb, &full[stage], kk, term == 0 ? br0 : br1);
+              load_b(sB + stage * B_BYTES, mb, term == 0 ? br0 : br1);
             }
             ++issued;
             if (++stage == nst) {
@@ -220,7 +245,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       bool ok = true;
       const uint32_t idesc =
           (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(p.bn >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
-      for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+      for (int tile = cid; tile < ntile && ok; tile += ncl) {
         for (int ch = 0; ch < nch && ok; ch++) {
           int kn = p.kblocks;
           if (p.ksplit > 1)
@@ -256,7 +281,10 @@ __global__ void __launch_bounds__(THREADS, 1)
               for (int k = 0; k < BK / 16; k++)  // +32 bytes along K per 16-element step
                 mma_i(d, ad + (uint64_t)(k * 2), bd + (uint64_t)(k * 2), idesc, (kb | k) != 0);
             }
-            mma_commit(&empty[stage]);
+            if (CM == 1)
+              mma_commit(&empty[stage]);
+            else
+              mma_commit_mc(&empty[stage], kMask);  // the stage is free here and in the peer
             if (++stage == nst) {
               stage = 0;
               phase ^= 1u;
@@ -280,10 +308,10 @@ __global__ void __launch_bounds__(THREADS, 1)
     uint32_t aphase = 0;
     const GemmEpilogue ep = p.epi;
     bool ok = true;
-    for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x)
+    for (int tile = cid; tile < ntile && ok; tile += ncl)
     for (int kch = 0; kch < nch; kch++) {
       const int pb = tile / tiles_per, tl = tile - pb * tiles_per;
-      const int mt = tl % p.mtiles, nt = tl / p.mtiles;
+      const int mt = (tl % mgroups) * CM + rank, nt = tl / mgroups;
       const int64_t coff = p.nprob ? p.c_off[pb] : (p.ksplit > 1 ? (int64_t)pb * p.M * p.N : 0);
       if (!mbar_wait(&tfull[acc], aphase, p.err)) {
         ok = false;
@@ -343,6 +371,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
   fence_before();
   __syncthreads();
+  // no CTA leaves while its peer may still multicast into its ring or arrive on its barriers
+  if (CM > 1) cluster_sync();
   if (warp == 1) {
     fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
@@ -426,6 +456,9 @@ __device__ __forceinline__ double pow2i(int e) {  // 2^e for -1022 <= e <= 1023
 // transpose buffer per epilogue warp
 constexpr size_t SLICED_SMEM_BYTES = SMEM_BYTES + 4 * 32 * 33 * sizeof(float);
 
+// CM = 2: as gemm_kernel<2>, the two CTAs of a cluster take neighbouring M tiles and each
+// multicasts half of every B slice tile into both rings.
+template <int CM>
 __global__ void __launch_bounds__(THREADS, 1)
     sliced_gemm_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, SParams p) {
   extern __shared__ uint8_t smem_raw[];
@@ -439,11 +472,13 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint64_t* mdone = tempty + 2;  // every MMA of this CTA has completed (before TMEM is released)
   uint32_t* tslot = (uint32_t*)(mdone + 1);
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int rank = CM > 1 ? (int)cluster_rank() : 0;
+  constexpr uint16_t kMask = (uint16_t)((1u << CM) - 1u);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&empty[s], CM);
     }
     for (int a = 0; a < 2; a++) {
       mbar_init(&tfull[a], 1);
@@ -460,9 +495,13 @@ __global__ void __launch_bounds__(THREADS, 1)
   fence_before();
   __syncthreads();
   fence_after();
+  if (CM > 1) cluster_sync();
   const uint32_t tmem = *tslot;
-  const int tiles_per = p.mtiles * p.ntiles;
+  const int mgroups = (p.mtiles + CM - 1) / CM;
+  const int tiles_per = mgroups * p.ntiles;
   const int ntile = tiles_per * (p.ksplit > 1 ? p.ksplit : 1);
+  const int cid = blockIdx.x / CM, ncl = gridDim.x / CM;
+  const int bh = p.bn / CM;
   // K range of a tile: the whole K, or chunk z of a split-K launch
   auto krange = [&](int tile, int& k0, int& kn) {
     k0 = 0;
@@ -479,9 +518,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t phase = 0;
       int64_t issued = 0;
       bool ok = true;
-      for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+      for (int tile = cid; tile < ntile && ok; tile += ncl) {
         const int tl = tile % tiles_per;
-        const int m0 = (tl % p.mtiles) * BM, n0 = (tl / p.mtiles) * p.bn;
+        const int m0 = ((tl % mgroups) * CM + rank) * BM, n0 = (tl / mgroups) * p.bn + rank * bh;
         int k0, kn;
         krange(tile, k0, kn);
         const int nu = sunit_count(p.S, p.gex, kn);
@@ -496,7 +535,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
                 mbar_expect_tx(&full[stage], (uint32_t)(A_BYTES + p.bn * BK * 2));
                 tma_load(sA + stage * A_BYTES, &mA, &full[stage], kb * BK, s * p.a_rows + m0);
-                tma_load(sB + stage * B_BYTES, &mB, &full[stage], kb * BK, (g - s) * p.b_rows + n0);
+                if (CM == 1)
+                  tma_load(sB + stage * B_BYTES, &mB, &full[stage], kb * BK, (g - s) * p.b_rows + n0);
+                else
+                  tma_load_mc(sB + stage * B_BYTES + (size_t)rank * bh * BK * 2, &mB, &full[stage], kb * BK,
+                              (g - s) * p.b_rows + n0, kMask);
                 ++issued;
                 if (++stage == STAGES) {
                   stage = 0;
@@ -515,7 +558,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       bool ok = true;
       const uint32_t idesc =
           (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(p.bn >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
-      for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+      for (int tile = cid; tile < ntile && ok; tile += ncl) {
         int k0, kn;
         krange(tile, k0, kn);
         const int nu = sunit_count(p.S, p.gex, kn);
@@ -537,7 +580,10 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
             for (int k = 0; k < BK / 16; k++)
               mma_i(d, ad + (uint64_t)(k * 2), bd + (uint64_t)(k * 2), idesc, (kb | k) != 0);
-            mma_commit(&empty[stage]);
+            if (CM == 1)
+              mma_commit(&empty[stage]);
+            else
+              mma_commit_mc(&empty[stage], kMask);
             if (++stage == STAGES) {
               stage = 0;
               phase ^= 1u;
@@ -560,9 +606,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     const GemmEpilogue ep = p.epi;
     bool ok = true;
     const int nch = p.bn / 32;
-    for (int tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+    for (int tile = cid; tile < ntile && ok; tile += ncl) {
       const int tl = tile % tiles_per;
-      const int mt = tl % p.mtiles, nt = tl / p.mtiles;
+      const int mt = (tl % mgroups) * CM + rank, nt = tl / mgroups;
       const int64_t coff = p.ksplit > 1 ? (int64_t)(tile / tiles_per) * p.M * p.N : 0;
       int k0, kn;
       krange(tile, k0, kn);
@@ -655,6 +701,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
   fence_before();
   __syncthreads();
+  if (CM > 1) cluster_sync();  // the peer no longer multicasts into this ring
   if (warp == 1) {
     fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
@@ -877,7 +924,8 @@ struct Split {
   __nv_bfloat16* mid = nullptr;  // three-part splits only
   std::unique_ptr<Scratch> tmp;  // storage of a temporary (non-constant) operand
   int64_t rows = 0, kp = 0;
-  CUtensorMap mhi, mlo, mmid;
+  CUtensorMap mhi, mlo, mmid;  // tensor maps of the last box_rows asked for (maps_for)
+  int map_rows = 0;
   ~Split() {
     if (tmp) return;
     if (hi) cudaFree(hi);
@@ -893,7 +941,8 @@ struct Sliced {
   std::unique_ptr<Scratch> tmp;  // storage of a temporary (non-constant) operand
   int64_t rows = 0, rows_p = 0, kp = 0;
   int S = 0;
-  CUtensorMap map;
+  CUtensorMap map;  // for boxes of map_rows rows (slice_map)
+  int map_rows = 0;
   ~Sliced() {
     if (!tmp) {
       if (d) cudaFree(d);
@@ -914,10 +963,12 @@ struct Cache {
   int* range = nullptr;    // device flag: a sliced operand row maximum beyond the range (sticky)
   int* pinned = nullptr;   // host copies of err and range, refreshed in stream order after launches
   bool sattr_set = false;
+  int max_pairs_sliced = 0;  // clusters of two sliced_gemm_kernel CTAs resident at once
   std::shared_ptr<Triples> triples;
   int* err = nullptr;
   int sms = 0;
   bool attr_set = false;
+  int max_pairs = 0;  // clusters of two gemm_kernel CTAs resident at once
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   ~Cache() {
     if (err) cudaFree(err);  // err and range share one allocation
@@ -966,16 +1017,28 @@ static Cache& cache(Ctx& c) {
   return *static_cast<Cache*>(c.tc_cache.get());
 }
 
+// the operand's tensor maps for boxes of box_rows x 64
+static Split* maps_for(Split* s, int box_rows, int parts) {
+  if (s->map_rows != box_rows) {
+    make_map(&s->mhi, s->hi, s->rows, s->kp, box_rows);
+    make_map(&s->mlo, s->lo, s->rows, s->kp, box_rows);
+    if (parts == 3) make_map(&s->mmid, s->mid, s->rows, s->kp, box_rows);
+    s->map_rows = box_rows;
+  }
+  return s;
+}
+
 // split (and cache when the source is a constant block) a rows x cols FP64 operand
 static Split* prepare(Ctx& c, const MatView& x, int box_rows, std::unique_ptr<Split>& temp, int parts = 2) {
   Cache& k = cache(c);
   const bool constant = c.is_constant(x.p);
   const int64_t rows = x.rows, cols = x.cols;
   UCC_REQUIRE(rows < INT32_MAX && cols < INT32_MAX, UCC_BAD_ARGS, "tensor-core GEMM: operand too large");
-  const Key key = make_key(x, box_rows, parts);
+  // the split data does not depend on the box a launch reads it with (maps_for)
+  const Key key = make_key(x, 0, parts);
   if (constant) {
     auto it = k.ops.find(key);
-    if (it != k.ops.end()) return it->second.get();
+    if (it != k.ops.end()) return maps_for(it->second.get(), box_rows, parts);
   }
   auto s = std::make_unique<Split>();
   s->rows = rows;
@@ -995,9 +1058,7 @@ static Split* prepare(Ctx& c, const MatView& x, int box_rows, std::unique_ptr<Sp
                  c.stream>>>(x, s->kp, s->hi, s->lo, s->mid);
   count_kernel_launch();
   UCC_CUDA(cudaGetLastError());
-  make_map(&s->mhi, s->hi, rows, s->kp, box_rows);
-  make_map(&s->mlo, s->lo, rows, s->kp, box_rows);
-  if (parts == 3) make_map(&s->mmid, s->mid, rows, s->kp, box_rows);
+  maps_for(s.get(), box_rows, parts);
   Split* raw = s.get();
   if (constant)
     k.ops[key] = std::move(s);
@@ -1006,23 +1067,33 @@ static Split* prepare(Ctx& c, const MatView& x, int box_rows, std::unique_ptr<Sp
   return raw;
 }
 
+// the slices' tensor map for boxes of box_rows x 64
+static Sliced* slice_map(Sliced* s, int box_rows) {
+  if (s->map_rows != box_rows) {
+    make_map(&s->map, s->d, (int64_t)s->S * s->rows_p, s->kp, box_rows);
+    s->map_rows = box_rows;
+  }
+  return s;
+}
+
 // slice (and cache when the source is a constant block and memory allows) a rows x cols
-// FP64 operand; the slice arrays are padded to whole tiles of box_rows rows so that no tile
-// reaches into the next slice.  nullptr when the slices do not fit in free memory.
-static Sliced* slice_prepare(Ctx& c, const MatView& x, int box_rows, int S, std::unique_ptr<Sliced>& temp,
-                             bool allow_cache) {
+// FP64 operand; the slice arrays are padded to whole tiles of pad_rows rows so that no tile
+// reaches into the next slice, and read with boxes of box_rows rows (pad_rows or a half).
+// nullptr when the slices do not fit in free memory.
+static Sliced* slice_prepare(Ctx& c, const MatView& x, int pad_rows, int box_rows, int S,
+                             std::unique_ptr<Sliced>& temp, bool allow_cache) {
   Cache& k = cache(c);
   bool constant = allow_cache && c.is_constant(x.p);
   const int64_t rows = x.rows, cols = x.cols;
   UCC_REQUIRE(rows < INT32_MAX && cols < INT32_MAX, UCC_BAD_ARGS, "sliced GEMM: operand too large");
-  const Key key = make_key(x, box_rows, S);
+  const Key key = make_key(x, pad_rows, S);
   if (constant) {
     auto it = k.sliced.find(key);
-    if (it != k.sliced.end()) return it->second.get();
+    if (it != k.sliced.end()) return slice_map(it->second.get(), box_rows);
   }
   auto s = std::make_unique<Sliced>();
   s->rows = rows;
-  s->rows_p = (rows + box_rows - 1) / box_rows * box_rows;
+  s->rows_p = (rows + pad_rows - 1) / pad_rows * pad_rows;
   s->kp = (cols + BK - 1) / BK * BK;
   s->S = S;
   const size_t nel = (size_t)S * s->rows_p * s->kp;
@@ -1054,7 +1125,7 @@ static Sliced* slice_prepare(Ctx& c, const MatView& x, int box_rows, int S, std:
       x, s->rows_p, s->kp, static_cast<const unsigned long long*>(amax.p), S, s->d, s->e, k.range);
   count_kernel_launch();
   UCC_CUDA(cudaGetLastError());
-  make_map(&s->map, s->d, (int64_t)S * s->rows_p, s->kp, box_rows);
+  slice_map(s.get(), box_rows);
   Sliced* raw = s.get();
   if (constant)
     k.sliced[key] = std::move(s);
@@ -1145,17 +1216,37 @@ static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alp
   cudaEvent_t ev0 = c.take_event(), ev1 = c.take_event();
   UCC_CUDA(cudaEventRecord(ev0, c.stream));  // the time includes the slicing of non-cached operands
   std::unique_ptr<Sliced> ta, tb;
-  Sliced* a = slice_prepare(c, A, BM, S, ta, allow_cache);
-  Sliced* b = a ? slice_prepare(c, B, bn, S, tb, allow_cache) : nullptr;
+  // neighbouring M tiles pair up in clusters that share each B slice tile (boxes of bn / 2)
+  const int cm = cluster_m((int)((M + BM - 1) / BM));
+  Sliced* a = slice_prepare(c, A, BM, BM, S, ta, allow_cache);
+  const CUtensorMap amap = a ? a->map : CUtensorMap{};  // copied: A and B may be one cached operand
+  Sliced* b = a ? slice_prepare(c, B, bn, bn / cm, S, tb, allow_cache) : nullptr;
   if (!a || !b) {
     c.event_pool.push_back(ev0);
     c.event_pool.push_back(ev1);
     return false;
   }
+  const CUtensorMap bmap = b->map;
   wrote = true;
   if (!k.sattr_set) {
-    UCC_CUDA(cudaFuncSetAttribute(sliced_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    UCC_CUDA(cudaFuncSetAttribute(sliced_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)SLICED_SMEM_BYTES));
+    UCC_CUDA(cudaFuncSetAttribute(sliced_gemm_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)SLICED_SMEM_BYTES));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * k.sms);
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = SLICED_SMEM_BYTES;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    UCC_CUDA(cudaOccupancyMaxActiveClusters(&n, sliced_gemm_kernel<2>, &cfg));
+    k.max_pairs_sliced = std::max(1, n);
     k.sattr_set = true;
   }
   SParams p;
@@ -1209,8 +1300,25 @@ static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alp
       p.epi.s_n = 1;
     }
   }
-  const int grid = std::min(tiles * p.ksplit, k.sms);
-  sliced_gemm_kernel<<<grid, THREADS, SLICED_SMEM_BYTES, c.stream>>>(a->map, b->map, p);
+  if (cm == 1) {
+    sliced_gemm_kernel<1><<<std::min(tiles * p.ksplit, k.sms), THREADS, SLICED_SMEM_BYTES, c.stream>>>(amap, bmap,
+                                                                                                        p);
+  } else {
+    const int groups = (p.mtiles + 1) / 2 * p.ntiles * p.ksplit;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * std::min(groups, k.max_pairs_sliced));
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = SLICED_SMEM_BYTES;
+    cfg.stream = c.stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    UCC_CUDA(cudaLaunchKernelEx(&cfg, sliced_gemm_kernel<2>, amap, bmap, p));
+  }
   count_kernel_launch();
   c.stats.sliced_gemm_launches++;
   UCC_CUDA(cudaGetLastError());
@@ -1231,6 +1339,57 @@ static void set_fused(Params& p, bool fused) {
   p.stage_bytes = 2 * A_BYTES + 2 * p.bn * BK * 2;
   p.nst = fused ? (int)std::min<size_t>(STAGES, GEMM_RING / (size_t)p.stage_bytes) : STAGES;
 }
+
+static void set_gemm_attrs(Cache& k) {
+  if (k.attr_set) return;
+  UCC_CUDA(cudaFuncSetAttribute(gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM_BYTES));
+  UCC_CUDA(cudaFuncSetAttribute(gemm_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM_BYTES));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2 * k.sms);
+  cfg.blockDim = dim3(THREADS);
+  cfg.dynamicSmemBytes = GEMM_SMEM_BYTES;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  UCC_CUDA(cudaOccupancyMaxActiveClusters(&n, gemm_kernel<2>, &cfg));
+  k.max_pairs = std::max(1, n);
+  k.attr_set = true;
+}
+
+// one persistent launch over `work` tiles (output tiles x problems or K chunks): one CTA
+// per SM, or pairs of CTAs in clusters when cm = 2
+static void launch_gemm(Ctx& c, Cache& k, int cm, int work, const CUtensorMap& ahi, const CUtensorMap& alo,
+                        const CUtensorMap& bhi, const CUtensorMap& blo, const CUtensorMap& a2hi,
+                        const CUtensorMap& a2lo, const CUtensorMap& amid, const CUtensorMap& bmid, const Params& p) {
+  set_gemm_attrs(k);
+  if (cm == 1) {
+    gemm_kernel<1><<<std::min(work, k.sms), THREADS, GEMM_SMEM_BYTES, c.stream>>>(ahi, alo, bhi, blo, a2hi, a2lo,
+                                                                                  amid, bmid, p);
+  } else {
+    const int groups = (p.mtiles + 1) / 2 * p.ntiles * (p.nprob ? p.nprob : (p.ksplit > 1 ? p.ksplit : 1));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * std::min(groups, k.max_pairs));
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = GEMM_SMEM_BYTES;
+    cfg.stream = c.stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    UCC_CUDA(cudaLaunchKernelEx(&cfg, gemm_kernel<2>, ahi, alo, bhi, blo, a2hi, a2lo, amid, bmid, p));
+  }
+  count_kernel_launch();
+  c.stats.tc_gemm_launches++;
+  UCC_CUDA(cudaGetLastError());
+}
 }  // namespace tc
 
 // A: M x K, B: N x K (rows = the output's columns)
@@ -1241,12 +1400,12 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const Ma
   Cache& k = cache(c);
   std::unique_ptr<Split> ta, tb;
   const int bn = pick_bn(N);
+  const int cm = cluster_m((int)((M + BM - 1) / BM));
+  // the maps are copied at once: A and B may be one cached operand read with two boxes
   Split* a = prepare(c, A, BM, ta, parts);
-  Split* b = prepare(c, B, bn, tb, parts);
-  if (!k.attr_set) {
-    UCC_CUDA(cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM_BYTES));
-    k.attr_set = true;
-  }
+  const CUtensorMap a_hi = a->mhi, a_lo = a->mlo, a_mid = a->mmid;
+  Split* b = prepare(c, B, bn / cm, tb, parts);
+  const CUtensorMap b_hi = b->mhi, b_lo = b->mlo, b_mid = b->mmid;
   Params p;
   p.M = (int)M;
   p.N = (int)N;
@@ -1294,7 +1453,6 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const Ma
       p.epi.s_n = 1;
     }
   }
-  const int grid = std::min(tiles * p.ksplit, k.sms);
   cudaEvent_t ev0 = c.take_event(), ev1 = c.take_event();
   UCC_CUDA(cudaEventRecord(ev0, c.stream));
   p.nterms = 1;
@@ -1302,11 +1460,8 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const Ma
   p.C32 = nullptr;
   p.nparts = parts;
   set_fused(p, parts == 2 && p.kc == 0);
-  gemm_kernel<<<grid, THREADS, GEMM_SMEM_BYTES, c.stream>>>(a->mhi, a->mlo, b->mhi, b->mlo, a->mhi, a->mlo,
-                                                      parts == 3 ? a->mmid : a->mhi, parts == 3 ? b->mmid : b->mhi, p);
-  count_kernel_launch();
-  c.stats.tc_gemm_launches++;
-  UCC_CUDA(cudaGetLastError());
+  launch_gemm(c, k, cm, tiles * p.ksplit, a_hi, a_lo, b_hi, b_lo, a_hi, a_lo, parts == 3 ? a_mid : a_hi,
+              parts == 3 ? b_mid : b_hi, p);
   if (part) splitk_reduce(c, M, N, p.ksplit, part->d(), alpha, beta, C, epi);
   UCC_CUDA(cudaEventRecord(ev1, c.stream));
   // no synchronisation (see sliced_gemm_part)
@@ -1524,16 +1679,15 @@ bool mixed_triples_prepare(Ctx& c, int max_batch) {
   make_map(&T->A2.mhi, T->A2.hi, T->A2.rows, kp, BM);
   make_map(&T->A2.mlo, T->A2.lo, T->A2.rows, kp, BM);
   T->bn = pick_bn(nv);
-  make_map(&T->B.mhi, T->B.hi, T->B.rows, kp, T->bn);
-  make_map(&T->B.mlo, T->B.lo, T->B.rows, kp, T->bn);
+  // M = nv^2 rows per tuple: always two or more M tiles, so the launches pair CTAs that
+  // share the B tile (boxes of bn / 2 rows)
+  make_map(&T->B.mhi, T->B.hi, T->B.rows, kp, T->bn / 2);
+  make_map(&T->B.mlo, T->B.lo, T->B.rows, kp, T->bn / 2);
   UCC_CUDA(cudaMalloc(&T->d_arow, sizeof(int) * 6 * max_batch));  // 3 term pairs x 2 terms
   UCC_CUDA(cudaMalloc(&T->d_brow, sizeof(int) * 6 * max_batch));
   UCC_CUDA(cudaMalloc(&T->d_coff, sizeof(int64_t) * 3 * max_batch));
   k.triples = T;
-  if (!k.attr_set) {
-    UCC_CUDA(cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM_BYTES));
-    k.attr_set = true;
-  }
+  set_gemm_attrs(k);
   return true;
 }
 
@@ -1607,11 +1761,7 @@ bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, float* W3) {
     p.nparts = 2;
     p.kc = 0;
     set_fused(p, true);
-    gemm_kernel<<<std::min(tiles, k.sms), THREADS, GEMM_SMEM_BYTES, c.stream>>>(T.A.mhi, T.A.mlo, T.B.mhi, T.B.mlo,
-                                                                          T.A2.mhi, T.A2.mlo, T.A.mhi, T.B.mhi, p);
-    count_kernel_launch();
-    c.stats.tc_gemm_launches++;
-    UCC_CUDA(cudaGetLastError());
+    launch_gemm(c, k, 2, tiles, T.A.mhi, T.A.mlo, T.B.mhi, T.B.mlo, T.A2.mhi, T.A2.mlo, T.A.mhi, T.B.mhi, p);
   }
   UCC_CUDA(cudaEventRecord(ev1, c.stream));
   // timed with the other GEMMs (resolved lazily); the status flags are read at the next check
