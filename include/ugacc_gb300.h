@@ -121,8 +121,15 @@ ucc_status ucc_hbar(ucc_ctx* ctx);
 /* Replaces: CCLambda::CCLambda + compute_lambda (cclambda.cc:13-45, :93-129). */
 ucc_status ucc_lambda(ucc_ctx* ctx, double* pseudoenergy, int* iterations);
 
-/* Replaces: CCDensity::onepdm + twopdm (ccdensity.cc:89-339). */
+/* Replaces: CCDensity::onepdm + twopdm (ccdensity.cc:89-339).  Afterwards the one- and
+ * two-particle density blocks are tensors of the context: "Doo" "Dvv" "Dov" "Dvo" and
+ * "Goooo" "Gooov" "Gvvvo" "Govov" "Goovv" (the (T) pieces included for WFN=CCSD_T with
+ * DERTYPE=FIRST, as the reference starts them, ccdensity.cc:44-69), plus "Gvvvv" while
+ * nv^4 <= 2^25 (its energy is formed without it). */
 ucc_status ucc_density(ucc_ctx* ctx, double* e_onepdm, double* e_twopdm);
+/* The six two-particle density energies the reference prints (ccdensity.cc:181-335), in
+ * the order OOOO VVVV OOOV VVVO OVOV OOVV; their sum is ucc_density's e_twopdm. */
+ucc_status ucc_twopdm_energies(ucc_ctx* ctx, double* parts6);
 
 /* Replaces: CCPert::CCPert (ccpert.cc:11-77); returns a handle >= 0. */
 ucc_status ucc_pert_create(ucc_ctx* ctx, const double* pert, double omega, int* handle);

@@ -552,10 +552,12 @@ class CCDensity:
         l1, l2 = self.lam.l1, self.lam.l2
         V = H.V
         E = {}
+        self.G = {}  # the six blocks, kept for the element-wise comparison
         Goooo = ein("ijef,klef->ijkl", tau, l2)
         E["oooo"] = 0.5 * ein("ijkl,ijkl->", V("oooo"), Goooo)
         Gvvvv = ein("mnab,mncd->abcd", tau, l2)
         E["vvvv"] = 0.5 * ein("abcd,abcd->", V("vvvv"), Gvvvv)
+        self.G["Goooo"], self.G["Gvvvv"] = Goooo, Gvvvv
         # Gooov, :206-228
         G = -ein("ke,ijea->ijka", l1, 2.0 * tau - tau.swapaxes(2, 3))
         G -= ein("ie,jkae->ijka", t1, l2)
@@ -568,6 +570,7 @@ class CCDensity:
         if tg is not None:
             G += tg["Gooov"]
         E["ooov"] = ein("ijka,ijka->", V("ooov"), G)
+        self.G["Gooov"] = G
         # Gvvvo, :237-259
         G = ein("mc,miab->abci", l1, 2.0 * tau - tau.transpose(1, 0, 2, 3))
         G += ein("ma,imbc->abci", t1, l2)
@@ -579,10 +582,12 @@ class CCDensity:
         if tg is not None:
             G += tg["Gvvvo"]
         E["vvvo"] = ein("abci,abci->", V("vvvo"), G)
+        self.G["Gvvvo"] = G
         # Govov, :268-276
         G = -ein("ia,jb->iajb", t1, l1)
         G -= ein("mibe,jmea->iajb", tau, l2) + ein("imbe,mjea->iajb", t2, l2)
         E["ovov"] = ein("iajb,iajb->", V("ovov"), G)
+        self.G["Govov"] = G
         # Goovv, :285-328
         t2x = 2.0 * t2 - t2.swapaxes(2, 3)
         taux = 2.0 * tau - tau.swapaxes(2, 3)
@@ -604,6 +609,7 @@ class CCDensity:
         if tg is not None:
             G += tg["Goovv"]
         E["oovv"] = 0.5 * ein("ijab,ijab->", V("oovv"), G)
+        self.G["Goovv"] = G
         self.E2 = E
         return sum(E.values())
 

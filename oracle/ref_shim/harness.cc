@@ -238,6 +238,13 @@ int main(int argc, char** argv) {
       out.mat("Dvv", dens->Dvv_, nv, nv);
       out.mat("Dov", dens->Dov_, no, nv);
       out.mat("Dvo", dens->Dvo_, nv, no);
+      // the six two-particle density blocks (ccdensity.cc:153-339)
+      out.t4("Goooo", dens->Goooo_, no, no, no, no);
+      out.t4("Gvvvv", dens->Gvvvv_, nv, nv, nv, nv);
+      out.t4("Gooov", dens->Gooov_, no, no, no, nv);
+      out.t4("Gvvvo", dens->Gvvvo_, nv, nv, nv, no);
+      out.t4("Govov", dens->Govov_, no, nv, no, nv);
+      out.t4("Goovv", dens->Goovv_, no, no, nv, nv);
 
       if (kv["DERTYPE"] == "SECOND") {
         if (in.npert < 6) throw std::runtime_error("response needs 3 dipole + 3 angular momentum matrices");

@@ -34,23 +34,24 @@ from ugacc_gb300.generator import make_hamiltonian, make_perturbations, write_in
 ALL_T = ["t1", "t2"]
 HBAR_T = ["Hov", "Hoo", "Hvv", "Hoooo", "Hvvvv", "Hvovv", "Hooov", "Hovvo", "Hovov", "Hvvvo", "Hovoo"]
 LAM_T = ["l1", "l2", "Doo", "Dvv", "Dov", "Dvo"]
+G2_T = ["Goooo", "Gvvvv", "Gooov", "Gvvvo", "Govov", "Goovv"]  # the two-particle density blocks
 CASES = {
     # H2O/cc-pVDZ shape (no=5, nv=19), seed 0: CCSD, all three (T) forms, Lambda,
     # densities, static right-hand and dynamic left-hand response
     "c1": (5, 19, 0, [
-        ("right_w0", dict(DERTYPE="SECOND", TRIPLES="all", MYHAND="RIGHT", MY_OMEGA="0.0"), ALL_T + LAM_T),
+        ("right_w0", dict(DERTYPE="SECOND", TRIPLES="all", MYHAND="RIGHT", MY_OMEGA="0.0"), ALL_T + LAM_T + G2_T),
         ("left_w", dict(DERTYPE="SECOND", MYHAND="LEFT", MY_OMEGA="0.0656"), []),
         ("right_w", dict(DERTYPE="SECOND", MYHAND="RIGHT", MY_OMEGA="0.0656"), []),
     ]),
     # odd tiny sizes: every intermediate dumped (tile-edge coverage)
     "tiny": (3, 7, 11, [
         ("right_w0", dict(DERTYPE="SECOND", TRIPLES="all", MYHAND="RIGHT", MY_OMEGA="0.0"),
-         ALL_T + HBAR_T + LAM_T + ["X1_MuX", "X2_MuX", "Y1_MuX", "Y2_MuX", "X1_LZ", "X2_LZ"]),
+         ALL_T + HBAR_T + LAM_T + G2_T + ["X1_MuX", "X2_MuX", "Y1_MuX", "Y2_MuX", "X1_LZ", "X2_LZ"]),
         ("left_w", dict(DERTYPE="SECOND", MYHAND="LEFT", MY_OMEGA="0.0656"),
          ["X1_MuY", "X2_MuY", "Y1_MuY", "Y2_MuY", "Y1_LX", "Y2_LX"]),
     ]),
     # single occupied orbital (degenerate i=j=k triples weight)
-    "one_occ": (1, 6, 4, [("ccsd_t", dict(DERTYPE="FIRST", TRIPLES="all"), ALL_T + ["l1", "l2"])]),
+    "one_occ": (1, 6, 4, [("ccsd_t", dict(DERTYPE="FIRST", TRIPLES="all"), ALL_T + ["l1", "l2"] + G2_T)]),
     # prime sizes
     "prime": (7, 13, 7, [("ccsd_t", dict(DERTYPE="FIRST", TRIPLES="all"), ALL_T)]),
     # more virtuals than a 32-wide tile
@@ -60,7 +61,7 @@ CASES = {
     # (OOC=1: tcorr_ooc + tgrad_ooc; OOC=0, the plugin's default: tcorr + tgrad over stored T3/L3)
     "tgrad": (4, 11, 9, [("ccsd_t_first", dict(WFN="CCSD_T", DERTYPE="FIRST"),
                           ["t1", "t2", "s1", "s2", "DooT", "DvvT", "DovT", "GoovvT", "GooovT", "GvvvoT",
-                           "l1", "l2", "Doo", "Dvv", "Dov"]),
+                           "l1", "l2", "Doo", "Dvv", "Dov"] + G2_T),
                          ("ccsd_t_first_incore", dict(WFN="CCSD_T", DERTYPE="FIRST", OOC="0"),
                           ["s1", "s2", "DooT", "DvvT", "DovT", "GoovvT", "GooovT", "GvvvoT",
                            "l1", "l2", "Doo", "Dvv", "Dov"])]),
@@ -69,6 +70,15 @@ BIG = {
     # the plain FP64 CCSD(T) workload itself (no=16, nv=160, seed 1); hours on one core
     "c2": (16, 160, 1, [("ccsd_t", dict(DERTYPE="NONE", TRIPLES="tjl"), ["t1"])]),
 }
+
+
+def parse_twopdm(log: str):
+    """The component energies of the two-particle density as the reference prints them
+    (ccdensity.cc:181-335, %20.14f): OOOO, VVVV, OOOV, VVVO, OVOV, OOVV."""
+    out = {}
+    for m in re.finditer(r"^\t(OOOO|VVVV|OOOV|VVVO|OVOV|OOVV) Energy = \s*(-?\d+\.\d+)\s*$", log, flags=re.M):
+        out[m.group(1)] = float(m.group(2))
+    return out
 
 
 def parse_tables(log: str):
@@ -115,6 +125,9 @@ def run_case(name, spec, binary, reference):
             tens = res.pop("tensors")
             res["options"] = dict(opts, R_CONVERGENCE="1e-10", MAXITER="100")
             res["tables"] = parse_tables(log)
+            e2 = parse_twopdm(log)
+            if e2:
+                res["e_twopdm_parts"] = e2
             meta["runs"][tag] = res
             for k in keep:
                 arrays[f"{tag}/{k}"] = np.fromfile(os.path.join(outdir, k + ".bin")).reshape(tens[k])

@@ -71,6 +71,18 @@ def test_hbar_lambda_density_vs_reference(name):
     for k in ["Doo", "Dvv", "Dov", "Dvo"]:
         if f"{tag}/{k}" in arr:
             np.testing.assert_allclose(dens.block(k), arr[f"{tag}/{k}"], atol=TTOL, rtol=0)
+    _check_twopdm(dens, run, arr, tag)
+
+
+def _check_twopdm(dens, run, arr, tag):
+    """The six two-particle density blocks element by element and each block's energy as
+    the reference prints it (ccdensity.cc:153-339, 14 decimals)."""
+    for k in ["Goooo", "Gvvvv", "Gooov", "Gvvvo", "Govov", "Goovv"]:
+        if f"{tag}/{k}" in arr:
+            np.testing.assert_allclose(dens.block(k), arr[f"{tag}/{k}"], atol=TTOL, rtol=0, err_msg=k)
+    parts = dens.twopdm_parts()
+    for blk, e in run.get("e_twopdm_parts", {}).items():
+        assert abs(parts[blk] - e) < 1e-12, (blk, parts[blk], e)
 
 
 @pytest.mark.parametrize("name", ["c1", "tiny"])
@@ -157,6 +169,7 @@ def test_triples_gradient_vs_reference(tag, ooc):
     assert abs(e1 + e2 - (cc.eccsd + cc.et)) < 1e-10  # E(density) = E_CCSD(T)
     for k in ["Doo", "Dvv", "Dov"]:
         np.testing.assert_allclose(H.ctx.get(k, arr[f"{tag}/{k}"].shape), arr[f"{tag}/{k}"], atol=TTOL, rtol=0)
+    _check_twopdm(dens, run, arr, tag)
 
 
 def test_triples_gradient_vs_oracle_larger():

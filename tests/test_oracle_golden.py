@@ -65,6 +65,13 @@ def test_hbar_lambda_density(name):
     for k in ["Doo", "Dvv", "Dov", "Dvo"]:
         if f"{tag}/{k}" in arr:
             np.testing.assert_allclose(getattr(dens, k), arr[f"{tag}/{k}"], atol=TTOL, rtol=0)
+    # the two-particle density block by block, and each block's energy as the reference
+    # prints it (ccdensity.cc:153-339, 14 decimals)
+    for k in ["Goooo", "Gvvvv", "Gooov", "Gvvvo", "Govov", "Goovv"]:
+        if f"{tag}/{k}" in arr:
+            np.testing.assert_allclose(dens.G[k], arr[f"{tag}/{k}"], atol=TTOL, rtol=0, err_msg=k)
+    for blk, e in run.get("e_twopdm_parts", {}).items():
+        assert abs(dens.E2[blk.lower()] - e) < 1e-13, (blk, dens.E2[blk.lower()], e)
 
 
 @pytest.mark.parametrize("name", ["c1", "tiny"])
@@ -141,5 +148,11 @@ def test_triples_gradient_pieces_lambda_and_densities(tag, ooc):
     assert abs(e1 - run["e_onepdm"]) < ETOL and abs(e2 - run["e_twopdm"]) < ETOL
     # with the (T) pieces the density energy is the CCSD(T) energy
     assert abs(e1 + e2 - run["e_ccsd"]) < 1e-12
+    # the blocks include the (T) pieces the reference starts them from
+    for k in ["Goooo", "Gvvvv", "Gooov", "Gvvvo", "Govov", "Goovv"]:
+        if f"{tag}/{k}" in arr:
+            np.testing.assert_allclose(dens.G[k], arr[f"{tag}/{k}"], atol=TTOL, rtol=0, err_msg=k)
+    for blk, e in run.get("e_twopdm_parts", {}).items():
+        assert abs(dens.E2[blk.lower()] - e) < 1e-13, (blk, dens.E2[blk.lower()], e)
     for k in ["Doo", "Dvv", "Dov"]:
         np.testing.assert_allclose(getattr(dens, k), arr[f"{tag}/{k}"], atol=TTOL, rtol=0)

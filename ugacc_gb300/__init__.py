@@ -107,6 +107,7 @@ def load_library(path: str | None = None):
         "ucc_hbar": (i, [vp]),
         "ucc_lambda": (i, [vp, dp, P(i)]),
         "ucc_density": (i, [vp, dp, dp]),
+        "ucc_twopdm_energies": (i, [vp, dp]),
         "ucc_pert_create": (i, [vp, dp, d, P(i)]),
         "ucc_pert_solve": (i, [vp, i, i, dp, P(i)]),
         "ucc_linresp": (i, [vp, i, i, dp]),
@@ -419,11 +420,21 @@ class CCDensity:
     def twopdm(self) -> float:
         return self._run()[1]
 
+    PARTS = ("OOOO", "VVVV", "OOOV", "VVVO", "OVOV", "OOVV")
+
     def block(self, name: str) -> np.ndarray:
-        no, nv = self.cc.no, self.cc.nv
-        shape = {"Doo": (no, no), "Dvv": (nv, nv), "Dov": (no, nv), "Dvo": (nv, no)}[name]
+        """One- or two-particle density block: Doo Dvv Dov Dvo, Goooo Gvvvv Gooov Gvvvo
+        Govov Goovv (ccdensity.h:32-44 layouts)."""
+        shape = tuple(self.cc.no if ch == "o" else self.cc.nv for ch in name[1:])
         self._run()
         return self.ctx.get(name, shape)
+
+    def twopdm_parts(self) -> dict:
+        """The six two-particle energies the reference prints (ccdensity.cc:181-335)."""
+        self._run()
+        out = np.zeros(6)
+        self.ctx.check(self.ctx.lib.ucc_twopdm_energies(self.ctx.h, _ptr(out)))
+        return dict(zip(self.PARTS, out.tolist()))
 
 
 class CCPert:

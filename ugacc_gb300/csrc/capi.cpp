@@ -275,6 +275,14 @@ ucc_status ucc_density(ucc_ctx* ctx, double* e1, double* e2) {
   });
 }
 
+ucc_status ucc_twopdm_energies(ucc_ctx* ctx, double* parts) {
+  return guard(ctx, [&](Ctx& c) {
+    UCC_REQUIRE(parts, UCC_BAD_ARGS, "null output");
+    UCC_REQUIRE(c.has("Goooo"), UCC_BAD_STATE, "no densities computed (ucc_density first)");
+    for (int k = 0; k < 6; k++) parts[k] = c.e2_parts[k];
+  });
+}
+
 ucc_status ucc_pert_create(ucc_ctx* ctx, const double* pert, double omega, int* handle) {
   return guard(ctx, [&](Ctx& c) {
     UCC_REQUIRE(pert && handle && std::isfinite(omega), UCC_BAD_ARGS, "need pert, handle and a finite omega");

@@ -291,6 +291,9 @@ CCSDResult run_lambda(Ctx& c) {  // :93-129
 // ---------------------------------------------------------------------------------------
 // Densities
 // ---------------------------------------------------------------------------------------
+// Gvvvv is kept for copy-out up to this many elements (256 MB)
+constexpr double kKeepGvvvv = 32.0 * 1024 * 1024;
+
 void run_density(Ctx& c, double* e1, double* e2) {
   UCC_REQUIRE(c.have_lambda, UCC_BAD_STATE, "densities need converged Lambda amplitudes");
   Fp64Scope fp64(c);
@@ -330,18 +333,26 @@ void run_density(Ctx& c, double* e1, double* e2) {
   }
   *e1 = dot_all(c, Fk(c, "oo"), Doo) + dot_all(c, Fk(c, "vv"), Dvv);
 
-  // two-particle density energies, :153-339
+  // two-particle density blocks and energies, :153-339.  The blocks are kept in the
+  // context ("Goooo", "Gooov", "Gvvvo", "Govov", "Goovv", the (T) pieces included);
+  // Gvvvv (nv^4) is kept only while it is small, its energy never needs it.
   double E[6];
   {
-    Temp G(c, {no, no, no, no});
+    Tensor G = c.alloc("Goooo", {no, no, no, no}, false);
     contract(c, "ijef,klef->ijkl", 1.0, tau, l2, 0.0, G);
     E[0] = 0.5 * dot_all(c, V(c, "oooo"), G);
   }
   {
-    // Gvvvv = tau . l2 is never formed: E = 1/2 tau[mn,ab] (sum_cd <ab|cd> l2[mn,cd])
+    // E = 1/2 tau[mn,ab] (sum_cd <ab|cd> l2[mn,cd]) without Gvvvv = tau . l2
     Temp Y(c, {no, no, nv, nv});
     contract(c, "mncd,abcd->mnab", 1.0, l2, V(c, "vvvv"), 0.0, Y);
     E[1] = 0.5 * dot_all(c, tau, Y);
+    if ((double)nv * nv * nv * nv <= kKeepGvvvv) {
+      Tensor G = c.alloc("Gvvvv", {nv, nv, nv, nv}, false);
+      contract(c, "mnab,mncd->abcd", 1.0, tau, l2, 0.0, G);
+    } else if (c.has("Gvvvv")) {
+      c.drop("Gvvvv");
+    }
   }
   Temp taux(c, {no, no, nv, nv});  // 2 tau - tau(ba)
   transpose_add(c, "ijab->ijba", -1.0, tau, 0.0, taux);
@@ -353,7 +364,7 @@ void run_density(Ctx& c, double* e1, double* e2) {
   Temp Q3(c, {no, no, nv, no});  // Q3[k,m,e,j] = l2[k,m,e,f] t1[j,f]
   contract(c, "kmef,jf->kmej", 1.0, l2, t1, 0.0, Q3);
   {
-    Temp G(c, {no, no, no, nv});  // Gooov, :206-228
+    Tensor G = c.alloc("Gooov", {no, no, no, nv}, false);  // :206-228
     contract(c, "ke,ijea->ijka", -1.0, l1, taux, 0.0, G);
     contract(c, "ie,jkae->ijka", -1.0, t1, l2, 1.0, G);
     contract(c, "ki,ja->ijka", -2.0, P, t1, 1.0, G);
@@ -368,10 +379,11 @@ void run_density(Ctx& c, double* e1, double* e2) {
     Temp S2(c, {no, no, no, no});
     contract(c, "kmif,jf->ijkm", 1.0, Q, t1, 0.0, S2);
     contract(c, "ijkm,ma->ijka", 1.0, S2, t1, 1.0, G);
+    if (c.have_tgrad) axpby(c, G.size(), 1.0, c.get("TGooov").p, 1.0, G.p);  // the (T) piece it starts from
     E[2] = dot_all(c, V(c, "ooov"), G);
   }
   {
-    Temp G(c, {nv, nv, nv, no});  // Gvvvo, :237-259
+    Tensor G = c.alloc("Gvvvo", {nv, nv, nv, no}, false);  // :237-259
     Temp taum(c, {no, no, nv, nv});  // 2 tau[m,i,a,b] - tau[i,m,a,b]
     transpose_add(c, "imab->miab", -1.0, tau, 0.0, taum);
     axpby(c, taum->size(), 2.0, tau.p, 1.0, taum->p);
@@ -395,24 +407,25 @@ void run_density(Ctx& c, double* e1, double* e2) {
     Temp A5(c, {no, nv, nv, no});
     contract(c, "nmci,mb->nbci", 1.0, A4, t1, 0.0, A5);
     contract(c, "nbci,na->abci", -1.0, A5, t1, 1.0, G);
+    if (c.have_tgrad) axpby(c, G.size(), 1.0, c.get("TGvvvo").p, 1.0, G.p);
     E[3] = dot_all(c, V(c, "vvvo"), G);
   }
   {
-    Temp G(c, {no, nv, no, nv});  // Govov, :268-276
+    Tensor G = c.alloc("Govov", {no, nv, no, nv}, false);  // :268-276
     contract(c, "ia,jb->iajb", -1.0, t1, l1, 0.0, G);
     contract(c, "mibe,jmea->iajb", -1.0, tau, l2, 1.0, G);
     contract(c, "imbe,mjea->iajb", -1.0, t2, l2, 1.0, G);
     E[4] = dot_all(c, V(c, "ovov"), G);
   }
   {
-    Temp G(c, {no, no, nv, nv});  // Goovv, :285-328
+    Tensor G = c.alloc("Goovv", {no, no, nv, nv}, false);  // :285-328
     Temp t2x(c, {no, no, nv, nv});
     transpose_add(c, "ijab->ijba", -1.0, t2, 0.0, t2x);
     axpby(c, t2x->size(), 2.0, t2.p, 1.0, t2x->p);
     contract(c, "ia,jb->ijab", 4.0, t1, l1, 0.0, G);
-    axpby(c, G->size(), 4.0, tau.p, 1.0, G->p);
+    axpby(c, G.size(), 4.0, tau.p, 1.0, G.p);
     transpose_add(c, "ijab->ijba", -2.0, tau, 1.0, G);
-    axpby(c, G->size(), 1.0, l2.p, 1.0, G->p);
+    axpby(c, G.size(), 1.0, l2.p, 1.0, G.p);
     Temp U(c, {no, nv});
     contract(c, "me,jmbe->jb", 1.0, l1, t2x, 0.0, U);
     contract(c, "ia,jb->ijab", 4.0, t1, U, 1.0, G);
@@ -475,13 +488,10 @@ void run_density(Ctx& c, double* e1, double* e2) {
     Temp W10(c, {no, no, no, nv});
     contract(c, "mnij,ma->nija", 1.0, W2, t1, 0.0, W10);
     contract(c, "nija,nb->ijab", 1.0, W10, t1, 1.0, G);
+    if (c.have_tgrad) axpby(c, G.size(), 1.0, c.get("TGoovv").p, 1.0, G.p);
     E[5] = 0.5 * dot_all(c, V(c, "oovv"), G);
   }
-  if (c.have_tgrad) {  // Eooov, Evvvo, Eoovv of the (T) pieces (ccdensity.cc:225-330)
-    E[2] += dot_all(c, V(c, "ooov"), c.get("TGooov"));
-    E[3] += dot_all(c, V(c, "vvvo"), c.get("TGvvvo"));
-    E[5] += 0.5 * dot_all(c, V(c, "oovv"), c.get("TGoovv"));
-  }
+  for (int k = 0; k < 6; k++) c.e2_parts[k] = E[k];
   *e2 = E[0] + E[1] + E[2] + E[3] + E[4] + E[5];
   if (c.opt.print) {
     const char* nm[6] = {"OOOO", "VVVV", "OOOV", "VVVO", "OVOV", "OOVV"};

@@ -558,8 +558,9 @@ Tensor named_tensor(Ctx& c, const std::string& name) {
                                 {"GoovvT", "TGoovv"}, {"GooovT", "TGooov"}, {"GvvvoT", "TGvvvo"}};
   for (auto& p : tg)
     if (name == p[0]) return c.get(p[1]);
-  static const char* direct[] = {"tau",   "Doo",   "Dvv",   "Dov",   "Dvo",   "Hov",   "Hoo",  "Hvv",
-                                 "Hoooo", "Hvvvv", "Hvovv", "Hooov", "Hovvo", "Hovov", "Hvvvo", "Hovoo"};
+  static const char* direct[] = {"tau",   "Doo",   "Dvv",   "Dov",   "Dvo",   "Hov",   "Hoo",   "Hvv",
+                                 "Hoooo", "Hvvvv", "Hvovv", "Hooov", "Hovvo", "Hovov", "Hvvvo", "Hovoo",
+                                 "Goooo", "Gvvvv", "Gooov", "Gvvvo", "Govov", "Goovv"};
   for (const char* d : direct)
     if (name == d) return c.get(name);
   throw Error(UCC_BAD_ARGS, "unknown tensor " + name);

@@ -191,6 +191,7 @@ struct Ctx {
   void drop(const std::string& name);
 
   bool force_fp64 = false;  // integral construction and refinement sweeps stay FP64
+  double e2_parts[6] = {};  // two-particle density energies OOOO VVVV OOOV VVVO OVOV OOVV
 
   // Anchored refinement of a mixed-precision solve.  In a record sweep (mode 1) every
   // heavy GEMM runs in FP64 and keeps its operands A0, B0 and product P0 = A0 B0; in a
