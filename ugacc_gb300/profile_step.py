@@ -37,6 +37,8 @@ def main(argv=None):
     ap.add_argument("--tgrad", action="store_true", help="with --triples: also the (T) gradient pieces")
     ap.add_argument("--ccsd-fp64", action="store_true",
                     help="with --triples: converge CCSD in FP64, then run (T) at --precision")
+    ap.add_argument("--guess", action="store_true",
+                    help="with --triples: start CCSD from the learned-guess kernel (an untrained network of seed 1)")
     a = ap.parse_args(argv)
 
     import ugacc_gb300 as U
@@ -73,6 +75,8 @@ def main(argv=None):
     if a.triples:
         cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10, "PRECISION": "FP64" if a.ccsd_fp64 else prec, "PRINT": int(a.print),
                          "MIXED_SWITCH": a.switch})
+        if a.guess:
+            U.MLP(seed=1).guess(H)
         e_cc = cc.compute_energy()
         st_cc = H.ctx.stats()
         if a.ccsd_fp64:
