@@ -868,6 +868,7 @@ constexpr int ET = 8;
 // make exact: thread t, iteration k covers element t + TNT*k of each loop.
 constexpr int TNT = 128;
 static_assert(TNT == 2 * ET * ET && (ET * ET * ET) % TNT == 0 && (6 * ET * ET) % TNT == 0, "tile/thread layout");
+template <int NP>  // W3 partial arrays (1 or 3), a compile-time count so that all loads are in flight together
 __global__ void __launch_bounds__(TNT) triples_energy_f32_tiled_kernel(int no, int nv, const int* __restrict__ tuples,
                                                                       const int* __restrict__ tri, int ntri,
                                                                       const float* __restrict__ W3, int nparts,
@@ -901,7 +902,8 @@ __global__ void __launch_bounds__(TNT) triples_energy_f32_tiled_kernel(int no, i
     if (gx < nv && gy < nv && gz < nv) {
       const int64_t o = (int64_t)gx * nv2 + (int64_t)gy * nv + gz;
       w = W[o];
-      for (int q = 1; q < nparts; q++) w += W[o + q * part_stride];
+#pragma unroll
+      for (int q = 1; q < NP; q++) w += W[o + q * part_stride];
     }
     Ws[p][x][ty][tz] = w;
   }
@@ -1103,9 +1105,15 @@ void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples,
   Scratch dtri(c, sizeof(int) * tri.size());
   UCC_CUDA(cudaMemcpyAsync(dtri.p, tri.data(), sizeof(int) * tri.size(), cudaMemcpyHostToDevice, c.stream));
   dim3 grid((unsigned)tri.size(), (unsigned)ntuple);
-  triples_energy_f32_tiled_kernel<<<grid, TNT, 0, c.stream>>>(no, nv, d_tuples, static_cast<const int*>(dtri.p),
-                                                             (int)tri.size(), W3, nparts, part_stride, t1, Voovv,
-                                                             eps, d_partial);
+  UCC_REQUIRE(nparts == 1 || nparts == 3, UCC_BAD_ARGS, "triples_energy: 1 or 3 W3 partial arrays");
+  if (nparts == 3)
+    triples_energy_f32_tiled_kernel<3><<<grid, TNT, 0, c.stream>>>(
+        no, nv, d_tuples, static_cast<const int*>(dtri.p), (int)tri.size(), W3, nparts, part_stride, t1, Voovv, eps,
+        d_partial);
+  else
+    triples_energy_f32_tiled_kernel<1><<<grid, TNT, 0, c.stream>>>(
+        no, nv, d_tuples, static_cast<const int*>(dtri.p), (int)tri.size(), W3, nparts, part_stride, t1, Voovv, eps,
+        d_partial);
   count_launch();
   check_launch("triples_energy_f32");
   UCC_CUDA(cudaStreamSynchronize(c.stream));  // the tile list is freed on return

@@ -112,6 +112,27 @@ __device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
       "l"(a), "l"(b), "r"(IDESC), "r"(acc));
 }
+// Work item -> (problem or K chunk pb, M tile group mg, N tile nt).  Batched problems run
+// M-group-major: all problems and N tiles of one M group before the next, so that the
+// problems of a launch that share an A operand (the (T) tuples of one occupied index) read
+// each A tile from L2 instead of DRAM.  One problem (or its split-K chunks) runs
+// chunk-major with the M groups fastest.
+__device__ __forceinline__ void tile_coords(const Params& p, int mgroups, int tile, int& pb, int& mg, int& nt) {
+  if (p.nprob) {
+    const int per_m = p.nprob * p.ntiles;
+    mg = tile / per_m;
+    const int r = tile - mg * per_m;
+    pb = r / p.ntiles;
+    nt = r - pb * p.ntiles;
+  } else {
+    const int tiles_per = mgroups * p.ntiles;
+    pb = tile / tiles_per;
+    const int tl = tile - pb * tiles_per;
+    mg = tl % mgroups;
+    nt = tl / mgroups;
+  }
+}
+
 // CM CTAs per cluster along M (1 or 2).  With CM = 2 the two CTAs of a cluster take M tiles
 // 2j and 2j+1 of the same N tile: each loads half of the B tile's rows and multicasts it
 // into both CTAs' rings (the B tensor maps have boxes of bn / 2 rows), so every B byte
@@ -179,8 +200,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       int64_t issued = 0;
       bool ok = true;
       for (int tile = cid; tile < ntile && ok; tile += ncl) {
-        const int pb = tile / tiles_per, tl = tile - pb * tiles_per;
-        const int mt = (tl % mgroups) * CM + rank, nt = tl / mgroups;
+        int pb, mg, nt;
+        tile_coords(p, mgroups, tile, pb, mg, nt);
+        const int mt = mg * CM + rank;
         const int ar0 = (p.nprob ? p.a_row0[pb] : 0) + mt * BM;
         const int br0 = (p.nprob ? p.b_row0[pb] : 0) + nt * p.bn + rank * bh;
         const int ar1 = p.nterms > 1 ? p.a_row1[pb] + mt * BM : 0;
@@ -310,8 +332,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     bool ok = true;
     for (int tile = cid; tile < ntile && ok; tile += ncl)
     for (int kch = 0; kch < nch; kch++) {
-      const int pb = tile / tiles_per, tl = tile - pb * tiles_per;
-      const int mt = (tl % mgroups) * CM + rank, nt = tl / mgroups;
+      int pb, mg, nt;
+      tile_coords(p, mgroups, tile, pb, mg, nt);
+      const int mt = mg * CM + rank;
       const int64_t coff = p.nprob ? p.c_off[pb] : (p.ksplit > 1 ? (int64_t)pb * p.M * p.N : 0);
       if (!mbar_wait(&tfull[acc], aphase, p.err)) {
         ok = false;
@@ -333,12 +356,22 @@ __global__ void __launch_bounds__(THREADS, 1)
           if (p.C32) {
             float* Cf = p.C32 + coff + mo;
             const float af = (float)alpha;
-            float old[32];
+            if (ep.s_n == 1 && beta == 0.0 && af == 1.0f && n0 + 32 <= p.N &&
+                ((reinterpret_cast<uintptr_t>(Cf + n0) & 15u) == 0)) {
+              // a lane's 32 columns are contiguous: 16-byte stores, 8 per lane instead of 32
+              float4* dst = reinterpret_cast<float4*>(Cf + n0);
 #pragma unroll
-            for (int j = 0; j < 32; j++) old[j] = (beta != 0.0 && n0 + j < p.N) ? Cf[(n0 + j) * ep.s_n] : 0.f;
+              for (int j = 0; j < 8; j++)
+                dst[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
+                                     __uint_as_float(r[4 * j + 2]), __uint_as_float(r[4 * j + 3]));
+            } else {
+              float old[32];
 #pragma unroll
-            for (int j = 0; j < 32; j++)
-              if (n0 + j < p.N) Cf[(n0 + j) * ep.s_n] = fmaf(af, __uint_as_float(r[j]), old[j]);
+              for (int j = 0; j < 32; j++) old[j] = (beta != 0.0 && n0 + j < p.N) ? Cf[(n0 + j) * ep.s_n] : 0.f;
+#pragma unroll
+              for (int j = 0; j < 32; j++)
+                if (n0 + j < p.N) Cf[(n0 + j) * ep.s_n] = fmaf(af, __uint_as_float(r[j]), old[j]);
+            }
           } else if (alpha == 1.0 && (beta == 0.0 || beta == 1.0)) {
             double* Cb = p.C + coff + mo;
             double old[32];
