@@ -9,6 +9,8 @@ enumeration, once each, inside the tensors."""
 import itertools
 import random
 
+import pytest
+
 
 def canonical(od, is_, os_):
     d, i, o = [], [], []
@@ -124,3 +126,24 @@ def test_triples_energy_closed_form_indices():
         for it in range(ET ** 3 // NT):  # the energy loop
             q = tid + NT * it
             assert (q // (ET * ET), (q // ET) % ET, q % ET) == (tx + 2 * it, ty, tz)
+
+
+def _raster(mgroups, ntiles, tl, band_n=8):
+    """The tensor-core GEMMs' raster order (tc_gemm.cu raster()): bands of band_n N tiles,
+    M groups in order inside a band, the band's N tiles fastest."""
+    band = tl // (mgroups * band_n)
+    w = min(band_n, ntiles - band * band_n)
+    r = tl - band * mgroups * band_n
+    mg = r // w
+    return mg, band * band_n + (r - mg * w)
+
+
+@pytest.mark.parametrize("mgroups,ntiles", [(1, 1), (40, 40), (40, 2), (3, 17), (80, 9), (7, 8), (1, 13)])
+def test_raster_order_visits_every_tile_once(mgroups, ntiles):
+    seen = [_raster(mgroups, ntiles, t) for t in range(mgroups * ntiles)]
+    assert sorted(seen) == [(m, n) for m in range(mgroups) for n in range(ntiles)]
+    # tiles in flight together (a window of 152) share operands: at most ~8 N tiles span it
+    # whenever there are that many M groups
+    if mgroups >= 19 and ntiles >= 8:
+        window = seen[:152]
+        assert len({n for _, n in window}) <= 8 and len({m for m, _ in window}) <= 19

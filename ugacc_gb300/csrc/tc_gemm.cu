@@ -112,11 +112,26 @@ __device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
       "l"(a), "l"(b), "r"(IDESC), "r"(acc));
 }
+// N tiles per raster band: the tiles of one problem run band by band, and inside a band M
+// group by M group with the band's N tiles fastest, so that the ~150 tiles in flight at a
+// time cover about a dozen M groups x RASTER_N N tiles: each A tile is then read by
+// RASTER_N concurrent tiles and each B tile by a dozen, mostly from L2 (walking M fastest
+// over a whole column of tiles shared B only and re-read every A tile from DRAM once per N
+// tile).
+constexpr int RASTER_N = 8;
+__device__ __forceinline__ void raster(int mgroups, int ntiles, int tl, int& mg, int& nt) {
+  const int band = tl / (mgroups * RASTER_N);
+  const int w = min(RASTER_N, ntiles - band * RASTER_N);  // N tiles in this band
+  const int r = tl - band * mgroups * RASTER_N;
+  mg = r / w;
+  nt = band * RASTER_N + (r - mg * w);
+}
+
 // Work item -> (problem or K chunk pb, M tile group mg, N tile nt).  Batched problems run
 // M-group-major: all problems and N tiles of one M group before the next, so that the
 // problems of a launch that share an A operand (the (T) tuples of one occupied index) read
 // each A tile from L2 instead of DRAM.  One problem (or its split-K chunks) runs
-// chunk-major with the M groups fastest.
+// chunk-major, each chunk in raster bands.
 __device__ __forceinline__ void tile_coords(const Params& p, int mgroups, int tile, int& pb, int& mg, int& nt) {
   if (p.nprob) {
     const int per_m = p.nprob * p.ntiles;
@@ -127,9 +142,7 @@ __device__ __forceinline__ void tile_coords(const Params& p, int mgroups, int ti
   } else {
     const int tiles_per = mgroups * p.ntiles;
     pb = tile / tiles_per;
-    const int tl = tile - pb * tiles_per;
-    mg = tl % mgroups;
-    nt = tl / mgroups;
+    raster(mgroups, p.ntiles, tile - pb * tiles_per, mg, nt);
   }
 }
 
@@ -552,8 +565,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       int64_t issued = 0;
       bool ok = true;
       for (int tile = cid; tile < ntile && ok; tile += ncl) {
-        const int tl = tile % tiles_per;
-        const int m0 = ((tl % mgroups) * CM + rank) * BM, n0 = (tl / mgroups) * p.bn + rank * bh;
+        int mg, ntl;
+        raster(mgroups, p.ntiles, tile % tiles_per, mg, ntl);
+        const int m0 = (mg * CM + rank) * BM, n0 = ntl * p.bn + rank * bh;
         int k0, kn;
         krange(tile, k0, kn);
         const int nu = sunit_count(p.S, p.gex, kn);
@@ -640,8 +654,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     bool ok = true;
     const int nch = p.bn / 32;
     for (int tile = cid; tile < ntile && ok; tile += ncl) {
-      const int tl = tile % tiles_per;
-      const int mt = (tl % mgroups) * CM + rank, nt = tl / mgroups;
+      int mg, nt;
+      raster(mgroups, p.ntiles, tile % tiles_per, mg, nt);
+      const int mt = mg * CM + rank;
       const int64_t coff = p.ksplit > 1 ? (int64_t)(tile / tiles_per) * p.M * p.N : 0;
       int k0, kn;
       krange(tile, k0, kn);
