@@ -146,6 +146,14 @@ ucc_status ucc_linresp(ucc_ctx* ctx, int handle_x, int handle_y, double* value);
 ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t M, int64_t N, int64_t K,
                     double alpha, const double* A, const double* B, double beta, double* C);
 
+/* ucc_gemm with precision UCC_FP64_SLICED and `digits` (2 to 9) base-2^6 digits per operand
+ * in place of 9: each operand row is truncated to 6*digits bits relative to its largest
+ * element, so the error per product term is near 2^(-6*digits) of max|A row| * max|B col|.
+ * The mixed-precision solvers use fewer digits for FP64 anchors whose delta sweeps only need
+ * to resolve a residual well above r_convergence; the sweep that ends a solve uses 9. */
+ucc_status ucc_gemm_sliced(ucc_ctx* ctx, int digits, int transa, int transb, int64_t M, int64_t N, int64_t K,
+                           double alpha, const double* A, const double* B, double beta, double* C);
+
 /* Failure-detection self-test (no counterpart in the reference, which has no device
  * code).  Every wait inside the tensor-core pipelines is bounded: when one runs out the
  * kernel raises a device flag and returns, and the call reports UCC_DEVICE_TIMEOUT.  This
@@ -275,6 +283,8 @@ typedef struct ucc_stats {
   double sliced_gemm_flops;  /* their algorithmic FLOPs, 2*M*N*K per GEMM */
   int64_t sliced_gemm_launches;
   double guess_ms;           /* device time of the learned-guess pass (ucc_mlp_guess, CUDA events) */
+  double sliced_gemm_product_flops; /* sliced_gemm_flops weighted by each GEMM's slice products: the tensor
+                                       pipe's work (45 products per output at 9 digits, 21 at 6) */
 } ucc_stats;
 ucc_status ucc_get_stats(ucc_ctx* ctx, ucc_stats* out);
 ucc_status ucc_reset_stats(ucc_ctx* ctx);

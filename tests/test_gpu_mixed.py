@@ -53,8 +53,11 @@ def test_mixed_unrefined_within_one_microhartree():
     assert abs(emx - e64) < 1e-6
 
 
-def test_mixed_triples_matches_fp64():
-    h = make_hamiltonian(6, 80, 13)
+@pytest.mark.parametrize("no,nv,seed", [(6, 80, 13), (5, 84, 7), (6, 78, 13)])
+def test_mixed_triples_matches_fp64(no, nv, seed):
+    """nv = 80 and 84 run the pipelined energy kernel (84: the last 8-wide virtual tile is half
+    outside nv, zero-filled), nv = 78 the padded-tile kernel it falls back to when nv % 4 != 0."""
+    h = make_hamiltonian(no, nv, seed)
     H = U.Hamiltonian.from_synthetic(h)
     cc = U.CCWfn(H, {"R_CONVERGENCE": 1e-10})
     cc.compute_energy()
@@ -188,3 +191,31 @@ def test_sliced_gemm_reports_operands_out_of_range():
     A[5, 3] = 1.0
     got = ctx.gemm(A, B, precision=U.FP64_SLICED)
     np.testing.assert_allclose(got, A @ B, rtol=0, atol=1e-12)
+
+
+def test_sliced_gemm_digits_set_the_error():
+    """ucc_gemm_sliced with d digits per operand: the error per output element stays within
+    the truncation bound ~(d + 5) 2^(2 - 6d) sqrt(K) max|A row| max|B col| (with a factor 4
+    of margin), and each digit taken away raises it by far more than the 8x checked here
+    (nominally 64x), so the digits asked for are the digits used."""
+    M, N, K = 300, 520, 777
+    rng = np.random.default_rng(17)
+    A = rng.standard_normal((M, K)) * np.exp(rng.standard_normal((M, K)))
+    B = rng.standard_normal((K, N))
+    ref = A @ B
+    scale = np.abs(A).max(axis=1)[:, None] * np.abs(B).max(axis=0)[None, :]
+    ctx = U.Context()
+    worst = {}
+    for d in range(4, 10):
+        got = ctx.gemm(A, B, digits=d)
+        rel = np.abs(got - ref) / scale
+        bound = 16.0 * (d + 5) * 2.0 ** (-6 * d) * np.sqrt(K)
+        assert rel.max() <= bound + 1e-15, (d, rel.max(), bound)
+        worst[d] = rel.max()
+    for d in range(4, 8):
+        assert worst[d] >= 8.0 * worst[d + 1], worst
+    np.testing.assert_array_equal(ctx.gemm(A, B, digits=9), ctx.gemm(A, B, precision=U.FP64_SLICED))
+    with pytest.raises(U.UccError) as e:
+        ctx.gemm(A, B, digits=10)
+    assert e.value.status == 4
+    ctx.close()

@@ -56,7 +56,8 @@ class Stats(ctypes.Structure):
                 ("anchored_iterations", ctypes.c_int), ("fp64_gemm_ms", ctypes.c_double),
                 ("fp64_gemm_flops", ctypes.c_double), ("fp64_gemm_launches", ctypes.c_int64),
                 ("sliced_gemm_ms", ctypes.c_double), ("sliced_gemm_flops", ctypes.c_double),
-                ("sliced_gemm_launches", ctypes.c_int64), ("guess_ms", ctypes.c_double)]
+                ("sliced_gemm_launches", ctypes.c_int64), ("guess_ms", ctypes.c_double),
+                ("sliced_gemm_product_flops", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -119,6 +120,7 @@ def load_library(path: str | None = None):
         "ucc_status_string": (cp, [i]),
         "ucc_triples_noalloc": (i, [i, i, vp, vp, vp, vp, vp, vp, dp, vp, cp, ctypes.c_size_t]),
         "ucc_gemm": (i, [vp, i, i, i, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, d, dp, dp, d, dp]),
+        "ucc_gemm_sliced": (i, [vp, i, i, i, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, d, dp, dp, d, dp]),
         "ucc_wait_selftest": (i, [vp, ctypes.c_uint64]),
         "ucc_mlp_create": (i, [P(vp), i, ctypes.c_uint64]),
         "ucc_mlp_destroy": (i, [vp]),
@@ -189,15 +191,20 @@ class Context:
         a = np.ascontiguousarray(arr, dtype=np.float64)
         self.check(self.lib.ucc_set_tensor(self.h, name.encode(), _ptr(a), a.size))
 
-    def gemm(self, A, B, C=None, alpha=1.0, beta=0.0, transa=False, transb=False, precision=FP64):
-        """C = alpha op(A) op(B) + beta C on the GPU (ucc_gemm)."""
+    def gemm(self, A, B, C=None, alpha=1.0, beta=0.0, transa=False, transb=False, precision=FP64, digits=None):
+        """C = alpha op(A) op(B) + beta C on the GPU (ucc_gemm); `digits` (2 to 9) selects the
+        sliced FP64 product with that many base-2^6 digits per operand (ucc_gemm_sliced)."""
         A = np.ascontiguousarray(A, dtype=np.float64)
         B = np.ascontiguousarray(B, dtype=np.float64)
         M, K = (A.shape[1], A.shape[0]) if transa else A.shape
         N = B.shape[0] if transb else B.shape[1]
         C = np.zeros((M, N)) if C is None else np.array(C, dtype=np.float64, order="C")
-        self.check(self.lib.ucc_gemm(self.h, precision, int(transa), int(transb), M, N, K, alpha, _ptr(A), _ptr(B),
-                                     beta, _ptr(C)))
+        if digits is None:
+            self.check(self.lib.ucc_gemm(self.h, precision, int(transa), int(transb), M, N, K, alpha, _ptr(A),
+                                         _ptr(B), beta, _ptr(C)))
+        else:
+            self.check(self.lib.ucc_gemm_sliced(self.h, int(digits), int(transa), int(transb), M, N, K, alpha,
+                                                _ptr(A), _ptr(B), beta, _ptr(C)))
         return C
 
     def wait_selftest(self, limit_s: float = 0.05):

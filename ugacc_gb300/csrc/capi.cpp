@@ -323,10 +323,11 @@ ucc_status ucc_linresp(ucc_ctx* ctx, int hx, int hy, double* value) {
   });
 }
 
-ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t M, int64_t N, int64_t K,
-                    double alpha, const double* A, const double* B, double beta, double* C) {
+static ucc_status gemm_host(ucc_ctx* ctx, int precision, int digits, int transa, int transb, int64_t M, int64_t N,
+                            int64_t K, double alpha, const double* A, const double* B, double beta, double* C) {
   return guard(ctx, [&](Ctx& c) {
     UCC_REQUIRE(A && B && C && M >= 1 && N >= 1 && K >= 1, UCC_BAD_ARGS, "ucc_gemm: bad arguments");
+    UCC_REQUIRE(digits >= 2 && digits <= 9, UCC_BAD_ARGS, "ucc_gemm_sliced: 2 to 9 digits");
     UCC_REQUIRE(precision == UCC_FP64 || precision == UCC_MIXED || precision == UCC_MIXED_FINE ||
                     precision == UCC_FP64_SLICED,
                 UCC_BAD_ARGS, "ucc_gemm: bad precision");
@@ -345,7 +346,7 @@ ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t
     else if (precision == UCC_MIXED_FINE)
       tc_gemm_run(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi, 3, 16);
     else if (precision == UCC_FP64_SLICED)
-      UCC_REQUIRE(sliced_gemm_run(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi, 9),
+      UCC_REQUIRE(sliced_gemm_run(c, M, N, K, alpha, dA.d(), sAm, sAk, dB.d(), sBk, sBn, beta, dC.d(), epi, digits),
                   UCC_BAD_ARGS, "ucc_gemm: operands outside the sliced form's range (row maxima >= 2^498 or |alpha| "
                                 "outside [2^-20, 2^20])");
     else
@@ -353,6 +354,16 @@ ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t
     UCC_CUDA(cudaMemcpyAsync(C, dC.p, sizeof(double) * M * N, cudaMemcpyDeviceToHost, c.stream));
     UCC_CUDA(cudaStreamSynchronize(c.stream));
   });
+}
+
+ucc_status ucc_gemm(ucc_ctx* ctx, int precision, int transa, int transb, int64_t M, int64_t N, int64_t K,
+                    double alpha, const double* A, const double* B, double beta, double* C) {
+  return gemm_host(ctx, precision, 9, transa, transb, M, N, K, alpha, A, B, beta, C);
+}
+
+ucc_status ucc_gemm_sliced(ucc_ctx* ctx, int digits, int transa, int transb, int64_t M, int64_t N, int64_t K,
+                           double alpha, const double* A, const double* B, double beta, double* C) {
+  return gemm_host(ctx, UCC_FP64_SLICED, digits, transa, transb, M, N, K, alpha, A, B, beta, C);
 }
 
 ucc_status ucc_wait_selftest(ucc_ctx* ctx, uint64_t limit_ns) {

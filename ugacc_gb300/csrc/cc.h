@@ -71,12 +71,17 @@ class MixedSweeps {
   bool mixed() const { return mixed_; }
   Kind kind() const { return kind_; }
   int split = 0, record = 0, delta = 0;
+  // digits (bf16 slices) of the coming record sweep's sliced products: enough to resolve the
+  // residual level the delta sweeps after it must reach, 9 (the full 54 bits) for a sweep
+  // that may end the solve or follows a stall
+  int record_digits() const;
 
  private:
   Ctx& c_;
   bool mixed_, refine_, split_phase_, record_next_ = true;
-  int stalls_ = 0, sweeps_ = 0;
+  int stalls_ = 0, sweeps_ = 0, digits_ = 9;
   double rms_prev_ = INFINITY, anchor_rms_ = INFINITY;
+  double record_target_ = 0.0;  // level the deltas after the coming record sweep resolve; 0: full digits
   Kind kind_ = kFp64, last_ = kFp64;
 };
 

@@ -467,14 +467,33 @@ MixedSweeps::MixedSweeps(Ctx& c)
 
 MixedSweeps::~MixedSweeps() { c_.anchors.clear(); }
 
+// Truncating each operand to S base-2^6 digits leaves a relative error near 2^-6S in every
+// product term; the digits cover the target level's bits plus a margin of kDigitMarginBits
+// for the sum over K and the spread of the operands' magnitudes (an anchor error shows as a
+// delta residual that stalls above the target, which re-anchors with all digits).
+constexpr int kDigitMarginBits = 14;
+
+int MixedSweeps::record_digits() const {
+  if (!(record_target_ > 0.0)) return 9;
+  const int d = (int)std::ceil((std::log2(1.0 / record_target_) + kDigitMarginBits) / 6.0);
+  return std::min(9, std::max(4, d));
+}
+
 MixedSweeps::Kind MixedSweeps::begin() {
   kind_ = !mixed_ ? kFp64 : split_phase_ ? kSplit : record_next_ ? kRecord : kDelta;
-  if (kind_ == kRecord) c_.anchors.begin(1);
+  if (kind_ == kRecord) {
+    c_.anchors.begin(1);
+    digits_ = record_digits();
+    c_.anchors.digits = digits_;
+  }
   if (kind_ == kDelta) c_.anchors.begin(2);
   return kind_;
 }
 
-void MixedSweeps::end() { c_.anchors.mode = 0; }
+void MixedSweeps::end() {
+  c_.anchors.mode = 0;
+  c_.anchors.digits = 9;
+}
 
 bool MixedSweeps::after(double rms, bool* restart_diis) {
   *restart_diis = false;
@@ -492,6 +511,8 @@ bool MixedSweeps::after(double rms, bool* restart_diis) {
     if (!done && refine_ && (rms < level || (sweeps_ > 2 && rms < 1e3 * level && rms > 0.5 * rms_prev_))) {
       split_phase_ = false;
       record_next_ = true;
+      // the deltas after this anchor run down to the re-anchoring level, or to r_convergence
+      record_target_ = rms > kReanchor * rc ? kReanchor * rc : rc;
       *restart_diis = true;  // the split-sweep history extrapolates a different map
     }
   } else if (kind_ == kRecord) {
@@ -499,7 +520,12 @@ bool MixedSweeps::after(double rms, bool* restart_diis) {
     record_next_ = false;
     stalls_ = 0;
     anchor_rms_ = rms;
-    done = rms < rc && record >= c_.opt.refine_sweeps;
+    // only a residual from products with all digits ends the solve
+    done = rms < rc && record >= c_.opt.refine_sweeps && digits_ == 9;
+    if (!done && rms < rc && digits_ < 9) {
+      record_next_ = true;
+      record_target_ = 0.0;
+    }
     // the FP64 residual is well above what the last delta sweep reported: those sweeps'
     // anchor was too far away and their vectors would mislead the extrapolation
     if (!done && last_ == kDelta && rms > 2.0 * rms_prev_) *restart_diis = true;
@@ -507,10 +533,15 @@ bool MixedSweeps::after(double rms, bool* restart_diis) {
     delta++;
     if (rms < rc) {
       record_next_ = true;  // confirm with an FP64 residual
+      record_target_ = 0.0;
     } else if (anchor_rms_ > kReanchor * rc && rms < kReanchor * rc) {
       record_next_ = true;  // the anchor is too far for the deltas to resolve rc: re-anchor here
+      record_target_ = rc;
     } else if (rms > 0.7 * rms_prev_) {
-      if (++stalls_ >= 2) record_next_ = true;  // corrections no longer resolved: re-anchor
+      if (++stalls_ >= 2) {  // corrections no longer resolved: re-anchor
+        record_next_ = true;
+        record_target_ = 0.0;
+      }
     } else {
       stalls_ = 0;
     }

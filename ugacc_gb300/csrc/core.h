@@ -204,7 +204,8 @@ struct Ctx {
     std::unique_ptr<PoolBuffer> a0, b0, p0;  // dense [M][K], [K][N], [M][N]
   };
   struct Anchors {
-    int mode = 0;  // 0 off, 1 record, 2 delta
+    int mode = 0;     // 0 off, 1 record, 2 delta
+    int digits = 9;   // bf16 slices per operand of the record sweep's sliced products
     size_t next = 0;
     std::vector<AnchorTerm> terms;
     void begin(int m) {
@@ -230,6 +231,7 @@ struct Ctx {
     cudaEvent_t a, b;
     double flops;
     int kind = 0;  // 0 FP64 GEMM, 1 split tensor-core GEMM, 2 sliced FP64 GEMM
+    double products = 1.0;  // sliced: the slice products per output (S(S+1)/2 for S digits)
   };
   std::vector<TimedLaunch> gemm_timers;
   std::vector<cudaEvent_t> event_pool;

@@ -171,6 +171,7 @@ void Ctx::resolve_timers() {
     } else if (t.kind == 2) {
       stats.sliced_gemm_ms += ms;
       stats.sliced_gemm_flops += t.flops;
+      stats.sliced_gemm_product_flops += t.flops * t.products;
     } else {
       stats.fp64_gemm_ms += ms;
       stats.fp64_gemm_flops += t.flops;
@@ -261,8 +262,8 @@ void anchored_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const 
     const double t0 = c.stats.sliced_gemm_ms;
     const bool sliced = sliced_gemm(c, M, N, K, 1.0, A, sAm, sAk, B, sBk, sBn, 0.0, t.p0->p, N, 1);
     if (sliced && c.opt.print >= 3)
-      std::printf("\tsliced GEMM (anchor)  M=%lld N=%lld K=%lld  %.3f ms\n", (long long)M, (long long)N, (long long)K,
-                  c.stats.sliced_gemm_ms - t0);
+      std::printf("\tsliced GEMM (anchor, %d digits)  M=%lld N=%lld K=%lld  %.3f ms\n", c.anchors.digits, (long long)M,
+                  (long long)N, (long long)K, c.stats.sliced_gemm_ms - t0);
     if (!sliced) {
       GemmEpilogue epi;
       epi.s_mhi = N;

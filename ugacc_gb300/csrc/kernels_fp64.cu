@@ -960,6 +960,169 @@ __global__ void __launch_bounds__(TNT) triples_energy_f32_tiled_kernel(int no, i
   const double tot = block_sum(s);
   if (threadIdx.x == 0) partial[(int64_t)t * ntri + r] = tot;
 }
+// Pipelined form of the FP32 energy for nv % 4 == 0 (W3 rows of 16-byte chunks): a
+// persistent block walks items (tuple t, tile triple r), item = t * ntri + r, in steps of
+// the grid.  While it computes item n from one shared-memory stage, the W3 tiles of item
+// n + G land in the other stage by 16-byte cp.async (no registers held, out-of-range rows
+// zero-filled) and the Voovv / t1 / eps values of item n + G wait in registers, to be
+// stored as floats once item n is done.  The NP partial arrays stay separate in shared
+// memory and are added where an element is read.  Tile rows swap their two 16-byte halves
+// on odd y, and the threads take the elements of a tile in a bit-permuted order: with those
+// two choices the six permuted reads of an element cost 1.33 shared-memory wavefronts on
+// average (1.67 for the padded tiles above) and the Voovv reads none extra.
+constexpr int EP_THREADS = 128;
+constexpr int EP_WROW = 8;            // floats per tile row
+constexpr int EP_WX = 72;             // floats per tile x plane: 8 rows and 8 of padding
+constexpr int EP_WTILE = ET * EP_WX;  // floats per tile
+template <int NP>
+struct EpStage {
+  float W[NP][6][EP_WTILE];
+  float V[3][6][ET * ET];  // Vij, Vik, Vjk on the 6 ordered role pairs, rows of 8
+  float t1[3][3][ET];
+  float ev[3][ET];
+  double red[EP_THREADS / 32];
+};
+static_assert(sizeof(EpStage<3>) % 16 == 0 && sizeof(EpStage<1>) % 16 == 0, "16-byte stage alignment");
+
+__device__ __forceinline__ void ep_cp16(void* dst, const void* src, bool valid) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void ep_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void ep_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+template <int NP>
+__global__ void __launch_bounds__(EP_THREADS, 2)
+    triples_energy_pipe_kernel(int no, int nv, const int* __restrict__ tuples, const int* __restrict__ tri, int ntri,
+                               int64_t nitems, const float* __restrict__ W3, int64_t part_stride,
+                               const double* __restrict__ t1, const double* __restrict__ Voovv,
+                               const double* __restrict__ eps, double* __restrict__ partial) {
+  extern __shared__ __align__(16) unsigned char ep_smem[];
+  EpStage<NP>* st = reinterpret_cast<EpStage<NP>*>(ep_smem);
+  const int tid = threadIdx.x;
+  const int64_t nv2 = (int64_t)nv * nv, nv3 = nv2 * nv;
+  constexpr uint64_t kPerm = 0x24ull | (0x18ull << 6) | (0x21ull << 12) | (0x09ull << 18) | (0x12ull << 24) |
+                             (0x06ull << 30);
+  // this thread's W3 chunk in every tile: row (cx, cy), 16-byte half ch
+  const int cx = tid >> 4, cy = (tid >> 1) & 7, ch = tid & 1;
+  double vreg[9];
+  double treg = 0.0;
+  auto ranges = [&](int64_t item, int& Ra, int& Rb, int& Rc, int& t) {
+    t = (int)(item / ntri);
+    const int code = tri[item - (int64_t)t * ntri];
+    Ra = (code & 1023) * ET;
+    Rb = ((code >> 10) & 1023) * ET;
+    Rc = (code >> 20) * ET;
+  };
+  auto issue = [&](int64_t item, int s) {  // W3 tiles by cp.async, the rest into registers
+    int Ra, Rb, Rc, t;
+    ranges(item, Ra, Rb, Rc, t);
+    auto R0 = [&](int role) { return role == 0 ? Ra : (role == 1 ? Rb : Rc); };
+    const float* Wt = W3 + (int64_t)t * nv3;
+#pragma unroll
+    for (int p = 0; p < 6; p++) {
+      const uint64_t c6 = kPerm >> (6 * p);
+      const int gx = R0((int)(c6 & 3)) + cx, gy = R0((int)((c6 >> 2) & 3)) + cy, gz = R0((int)((c6 >> 4) & 3)) + 4 * ch;
+      const bool ok = gx < nv && gy < nv && gz < nv;
+      const float* src = Wt + (ok ? ((int64_t)gx * nv + gy) * nv + gz : 0);
+      float* dst = &st[s].W[0][p][cx * EP_WX + cy * EP_WROW + ((ch ^ (cy & 1)) << 2)];
+#pragma unroll
+      for (int q = 0; q < NP; q++) ep_cp16(dst + q * 6 * EP_WTILE, src + q * part_stride, ok);
+    }
+    const int i = tuples[3 * t], j = tuples[3 * t + 1], k = tuples[3 * t + 2];
+#pragma unroll
+    for (int q = 0; q < 9; q++) {  // element e = tid + 128 q of [3][6][8][8]
+      const int e = tid + EP_THREADS * q;
+      const int m = e / 384, pid = (e / 64) % 6, x = (e / 8) % 8, y = e % 8;
+      const int u = pid / 2, v0 = pid % 2, v = v0 < u ? v0 : v0 + 1;
+      const int gx = R0(u) + x, gy = R0(v) + y;
+      const double* Vm = Voovv + ((m == 2 ? (int64_t)j : (int64_t)i) * no + (m == 0 ? j : k)) * nv2;
+      vreg[q] = (gx < nv && gy < nv) ? Vm[(int64_t)gx * nv + gy] : 0.0;
+    }
+    if (tid < 72) {
+      const int m = tid / 24, role = (tid / 8) % 3, g = R0(role) + tid % 8;
+      const int row = m == 0 ? i : (m == 1 ? j : k);
+      treg = g < nv ? t1[(int64_t)row * nv + g] : 0.0;
+    } else if (tid < 96) {
+      const int g = R0((tid - 72) / 8) + tid % 8;
+      treg = g < nv ? eps[no + g] : 0.0;
+    }
+  };
+  auto store = [&](int s) {
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+      const int e = tid + EP_THREADS * q;
+      st[s].V[e / 384][(e / 64) % 6][e % 64] = (float)vreg[q];
+    }
+    if (tid < 72)
+      st[s].t1[tid / 24][(tid / 8) % 3][tid % 8] = (float)treg;
+    else if (tid < 96)
+      st[s].ev[(tid - 72) / 8][tid % 8] = (float)treg;
+  };
+
+  const int64_t G = gridDim.x;
+  int64_t item = blockIdx.x;
+  if (item >= nitems) return;
+  issue(item, 0);
+  ep_commit();
+  store(0);
+  for (int s = 0; item < nitems; item += G, s ^= 1) {
+    const int64_t nxt = item + G;
+    if (nxt < nitems) issue(nxt, s ^ 1);
+    ep_commit();  // an empty group on the last item keeps the count of one group in flight
+    ep_wait1();
+    __syncthreads();
+    int Ra, Rb, Rc, t;
+    ranges(item, Ra, Rb, Rc, t);
+    const int i = tuples[3 * t], j = tuples[3 * t + 1], k = tuples[3 * t + 2];
+    const float eijk = (float)(eps[i] + eps[j] + eps[k]);
+    const float fac = 2.0f - (float)((i == j) + (i == k) + (j == k));
+    const EpStage<NP>& S = st[s];
+    auto W = [&](int p, int x, int y, int z) {
+      const int o = x * EP_WX + y * EP_WROW + ((((z >> 2) ^ (y & 1)) << 2) | (z & 3));
+      float w = S.W[0][p][o];
+#pragma unroll
+      for (int q = 1; q < NP; q++) w += S.W[q][p][o];
+      return w;
+    };
+    auto pid = [](int u, int v) { return u * 2 + (v > u ? v - 1 : v); };
+    auto Vp = [&](float w, int r0, int l0, int r1, int l1, int r2, int l2) {
+      return w + S.V[0][pid(r0, r1)][l0 * ET + l1] * S.t1[2][r2][l2] +
+             S.V[1][pid(r0, r2)][l0 * ET + l2] * S.t1[1][r1][l1] + S.V[2][pid(r1, r2)][l1 * ET + l2] * S.t1[0][r0][l0];
+    };
+    float sf = 0.f;
+#pragma unroll
+    for (int it = 0; it < ET * ET * ET / EP_THREADS; it++) {
+      const int la = ((tid >> 1) & 1) | (((tid >> 5) & 1) << 1) | (((it >> 1) & 1) << 2);
+      const int lb = ((tid >> 4) & 1) | (((tid >> 3) & 1) << 1) | (((tid >> 6) & 1) << 2);
+      const int lc = ((tid >> 2) & 1) | ((tid & 1) << 1) | ((it & 1) << 2);
+      const int a = Ra + la, b = Rb + lb, c = Rc + lc;
+      if (a >= nv || b > a || c > b) continue;
+      const float wabc = W(0, la, lb, lc), wacb = W(1, la, lc, lb), wbac = W(2, lb, la, lc);
+      const float wbca = W(3, lb, lc, la), wcab = W(4, lc, la, lb), wcba = W(5, lc, lb, la);
+      const float vabc = Vp(wabc, 0, la, 1, lb, 2, lc), vacb = Vp(wacb, 0, la, 2, lc, 1, lb);
+      const float vbac = Vp(wbac, 1, lb, 0, la, 2, lc), vbca = Vp(wbca, 1, lb, 2, lc, 0, la);
+      const float vcab = Vp(wcab, 2, lc, 0, la, 1, lb), vcba = Vp(wcba, 2, lc, 1, lb, 0, la);
+      const float X3 = wabc * vabc + wacb * vacb + wbac * vbac + wbca * vbca + wcab * vcab + wcba * vcba;
+      const float Y3 = vabc + vbca + vcab;
+      const float Z3 = vacb + vbac + vcba;
+      // V = numerator / (1 + number of equal index pairs), the same count for all six orders
+      const int neq = (a == b) + (a == c) + (b == c);
+      const float deg = neq == 0 ? 1.0f : (neq == 1 ? 0.5f : 0.25f);
+      const float denom = eijk - (S.ev[0][la] + S.ev[1][lb] + S.ev[2][lc]);
+      sf += ((Y3 - 2.0f * Z3) * (wabc + wbca + wcab) + (Z3 - 2.0f * Y3) * (wacb + wbac + wcba) + 3.0f * X3) * deg *
+            fac / denom;
+    }
+    double d = (double)sf;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if ((tid & 31) == 0) st[s].red[tid >> 5] = d;
+    if (nxt < nitems) store(s ^ 1);
+    __syncthreads();
+    if (tid == 0) partial[item] = ((S.red[0] + S.red[1]) + S.red[2]) + S.red[3];
+  }
+}
+
 }  // namespace
 
 int64_t triples_f32_partials(int nv) {
@@ -1104,8 +1267,44 @@ void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples,
       for (int C = 0; C <= B; C++) tri.push_back(A | (B << 10) | (C << 20));
   Scratch dtri(c, sizeof(int) * tri.size());
   UCC_CUDA(cudaMemcpyAsync(dtri.p, tri.data(), sizeof(int) * tri.size(), cudaMemcpyHostToDevice, c.stream));
-  dim3 grid((unsigned)tri.size(), (unsigned)ntuple);
   UCC_REQUIRE(nparts == 1 || nparts == 3, UCC_BAD_ARGS, "triples_energy: 1 or 3 W3 partial arrays");
+  const bool pipe = nv % 4 == 0 && part_stride % 4 == 0 && reinterpret_cast<uintptr_t>(W3) % 16 == 0;
+  if (pipe) {
+    // persistent blocks, as many as fit (two per SM by their two 47 KB stages)
+    static thread_local int sms[64] = {0}, per_sm[2][64] = {{0}};
+    const int dev = c.device & 63, np = nparts == 3 ? 0 : 1;
+    const size_t smem = nparts == 3 ? 2 * sizeof(EpStage<3>) : 2 * sizeof(EpStage<1>);
+    if (!sms[dev]) UCC_CUDA(cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, c.device));
+    if (!per_sm[np][dev]) {
+      if (nparts == 3) {
+        UCC_CUDA(cudaFuncSetAttribute(triples_energy_pipe_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        UCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[np][dev], triples_energy_pipe_kernel<3>,
+                                                               EP_THREADS, smem));
+      } else {
+        UCC_CUDA(cudaFuncSetAttribute(triples_energy_pipe_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        UCC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[np][dev], triples_energy_pipe_kernel<1>,
+                                                               EP_THREADS, smem));
+      }
+      per_sm[np][dev] = std::max(1, per_sm[np][dev]);
+    }
+    const int64_t nitems = (int64_t)ntuple * (int64_t)tri.size();
+    const unsigned grid = (unsigned)std::min<int64_t>(nitems, (int64_t)sms[dev] * per_sm[np][dev]);
+    if (nparts == 3)
+      triples_energy_pipe_kernel<3><<<grid, EP_THREADS, smem, c.stream>>>(
+          no, nv, d_tuples, static_cast<const int*>(dtri.p), (int)tri.size(), nitems, W3, part_stride, t1, Voovv,
+          eps, d_partial);
+    else
+      triples_energy_pipe_kernel<1><<<grid, EP_THREADS, smem, c.stream>>>(
+          no, nv, d_tuples, static_cast<const int*>(dtri.p), (int)tri.size(), nitems, W3, part_stride, t1, Voovv,
+          eps, d_partial);
+    count_launch();
+    check_launch("triples_energy_f32");
+    UCC_CUDA(cudaStreamSynchronize(c.stream));  // the tile list is freed on return
+    return;
+  }
+  dim3 grid((unsigned)tri.size(), (unsigned)ntuple);
   if (nparts == 3)
     triples_energy_f32_tiled_kernel<3><<<grid, TNT, 0, c.stream>>>(
         no, nv, d_tuples, static_cast<const int*>(dtri.p), (int)tri.size(), W3, nparts, part_stride, t1, Voovv, eps,

@@ -465,6 +465,7 @@ struct SUnit {
 };
 
 constexpr int SB = 6;                                           // bits per digit
+constexpr int kSlices = 9;  // digits per operand of the full-precision product (9 x 6 = 54 bits)
 constexpr int SEXACT_KB = (1 << (24 - 2 * (SB - 1))) / BK;     // K blocks of one pair per exact unit
 
 // K blocks per exact unit of order g: (g+1) pairs x kc blocks x 64 <= 2^(24 - 2(SB-1)) products
@@ -1127,17 +1128,20 @@ static Sliced* slice_map(Sliced* s, int box_rows) {
 // slice (and cache when the source is a constant block and memory allows) a rows x cols
 // FP64 operand; the slice arrays are padded to whole tiles of pad_rows rows so that no tile
 // reaches into the next slice, and read with boxes of box_rows rows (pad_rows or a half).
-// nullptr when the slices do not fit in free memory.
+// A cached operand always holds all kSlices digits: a product with S < kSlices digits reads
+// the leading S of them (they differ from x by less than one unit of digit S-1, like an
+// S-digit split).  nullptr when the slices do not fit in free memory.
 static Sliced* slice_prepare(Ctx& c, const MatView& x, int pad_rows, int box_rows, int S,
                              std::unique_ptr<Sliced>& temp, bool allow_cache) {
   Cache& k = cache(c);
   bool constant = allow_cache && c.is_constant(x.p);
   const int64_t rows = x.rows, cols = x.cols;
   UCC_REQUIRE(rows < INT32_MAX && cols < INT32_MAX, UCC_BAD_ARGS, "sliced GEMM: operand too large");
-  const Key key = make_key(x, pad_rows, S);
+  const Key key = make_key(x, pad_rows, kSlices);
   if (constant) {
     auto it = k.sliced.find(key);
     if (it != k.sliced.end()) return slice_map(it->second.get(), box_rows);
+    S = kSlices;
   }
   auto s = std::make_unique<Sliced>();
   s->rows = rows;
@@ -1184,8 +1188,7 @@ static Sliced* slice_prepare(Ctx& c, const MatView& x, int pad_rows, int box_row
 
 }  // namespace tc
 
-// slices per operand of the sliced FP64 GEMM (9 x 6 = 54 bits) and the smallest GEMM it takes
-constexpr int kSlices = 9;
+// the smallest GEMM the sliced FP64 GEMM takes
 constexpr double kSlicedMinWork = 3e7;
 
 static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const MatView& A,
@@ -1225,7 +1228,9 @@ static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alp
   Cache& k = cache(c);
   {
     const int64_t Mp = (M + BM - 1) / BM * BM, Np = (N + bn - 1) / bn * bn, kp = (K + BK - 1) / BK * BK;
-    auto cached = [&](const MatView& x, int box) { return allow_cache && k.sliced.count(make_key(x, box, S)) != 0; };
+    auto cached = [&](const MatView& x, int box) {
+      return allow_cache && k.sliced.count(make_key(x, box, kSlices)) != 0;
+    };
     const double needA = cached(A, BM) ? 0.0 : 2.0 * S * (double)Mp * kp;
     const double needB = cached(B, bn) ? 0.0 : 2.0 * S * (double)Np * kp;
     size_t free_b = 0, total_b = 0;
@@ -1374,7 +1379,7 @@ static bool sliced_gemm_part(Ctx& c, int64_t M, int64_t N, int64_t K, double alp
   UCC_CUDA(cudaEventRecord(ev1, c.stream));
   // no synchronisation: temporaries are freed in stream order, the time is resolved with the
   // other GEMM timers and the status flags are read at the next synchronisation (tc_check)
-  c.gemm_timers.push_back({ev0, ev1, 2.0 * (double)M * (double)N * (double)K, 2});
+  c.gemm_timers.push_back({ev0, ev1, 2.0 * (double)M * (double)N * (double)K, 2, 0.5 * S * (S + 1)});
   if (c.gemm_timers.size() >= 4096) c.resolve_timers();
   UCC_CUDA(cudaMemcpyAsync(k.pinned, k.err, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
   return true;
@@ -1602,14 +1607,16 @@ bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const Ma
   if (16.0 * (double)lo * hi < (double)((hi + 127) / 128 * 128) * (double)((lo + 31) / 32 * 32)) return false;
   GemmEpilogue epi;
   epi.msplit = 0;
+  // a record sweep's products carry the digits its anchor needs; everything else all of them
+  const int digits = c.anchors.mode == 1 ? std::min(tc::kSlices, std::max(2, c.anchors.digits)) : tc::kSlices;
   if (M <= 256 && N > M) {  // the short side becomes the (narrow) N tile
     epi.s_mhi = sCn;
     epi.s_n = sCm;
-    return sliced_gemm_run(c, N, M, K, alpha, B, A, beta, C, epi, kSlices);
+    return sliced_gemm_run(c, N, M, K, alpha, B, A, beta, C, epi, digits);
   }
   epi.s_mhi = sCm;
   epi.s_n = sCn;
-  return sliced_gemm_run(c, M, N, K, alpha, A, B, beta, C, epi, kSlices);
+  return sliced_gemm_run(c, M, N, K, alpha, A, B, beta, C, epi, digits);
 }
 
 bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t sAm, int64_t sAk,
