@@ -147,3 +147,94 @@ def test_raster_order_visits_every_tile_once(mgroups, ntiles):
     if mgroups >= 19 and ntiles >= 8:
         window = seen[:152]
         assert len({n for _, n in window}) <= 8 and len({m for m, _ in window}) <= 19
+
+
+# ---- blocked W3 layout of the mixed (T) path (core.h w3_block_offset) ----------------
+def w3_block_offset(a, b, c, T):
+    x, y, z = a & 7, b & 7, c & 7
+    return (((a >> 3) * T + (b >> 3)) * T + (c >> 3)) * 512 + 64 * x + 8 * (y ^ x) + (z ^ ((5 * y) & 7))
+
+
+@pytest.mark.parametrize("nv", [8, 20, 84])
+def test_w3_block_layout_is_a_bijection_onto_whole_blocks(nv):
+    T = (nv + 7) // 8
+    offs = [w3_block_offset(a, b, c, T) for a in range(8 * T) for b in range(8 * T) for c in range(8 * T)]
+    assert sorted(offs) == list(range(T ** 3 * 512))
+    # a tile (A, B, C) of the energy kernel is exactly block (A, B, C): 512 contiguous floats
+    for A, B, C in [(0, 0, 0), (T - 1, 0, T - 1), (T - 1, T - 1, T - 1)]:
+        blk = {w3_block_offset(8 * A + x, 8 * B + y, 8 * C + z, T)
+               for x in range(8) for y in range(8) for z in range(8)}
+        base = ((A * T + B) * T + C) * 512
+        assert blk == set(range(base, base + 512))
+
+
+def test_w3_epilogue_fast_path_matches_the_layout():
+    """The GEMM epilogue stores 32 columns c = n0 .. n0 + 31 of one (a, b) row as four
+    8-wide c blocks, after v[p] <- v[p ^ k] with k = 5 (b % 8) % 8, at base + block * 512."""
+    T = 5
+    for a, b, n0 in [(0, 0, 0), (13, 29, 0), (39, 7, 32), (22, 31, 0)]:
+        x, y, k = a & 7, b & 7, (5 * (b & 7)) & 7
+        base = (((a >> 3) * T + (b >> 3)) * T) * 512 + 64 * x + 8 * (y ^ x)
+        for g in range(4):
+            v = list(range(n0 + 8 * g, n0 + 8 * g + 8))  # the column each register holds
+            for bit in (1, 2, 4):  # xor_swap8: three conditional swaps
+                if k & bit:
+                    for e in range(8):
+                        if not e & bit:
+                            v[e], v[e | bit] = v[e | bit], v[e]
+            for pos, col in enumerate(v):
+                assert base + ((n0 >> 3) + g) * 512 + pos == w3_block_offset(a, b, col, T)
+
+
+def test_energy_thread_order_reads_blocks_without_bank_conflicts():
+    """triples_energy_pipe_kernel: 256 threads x 2 iterations cover a tile once, and every
+    warp's read of each of the six index orders, and of the Voovv rows, is one wavefront:
+    no bank holds two different words (words at 64 x + 8 (y ^ x) + (z ^ 5y), 4-byte banks;
+    lanes reading the same word share it)."""
+    def wavefronts(words):
+        banks = {}
+        for x in set(words):
+            banks.setdefault(x % 32, set()).add(x)
+        return max(len(v) for v in banks.values())
+
+    def elem(tid, it):
+        la = (tid & 1) | (((tid >> 6) & 1) << 1) | (((tid >> 7) & 1) << 2)
+        lb = ((tid >> 2) & 1) | (((tid >> 1) & 1) << 1) | (((tid >> 5) & 1) << 2)
+        lc = ((tid >> 4) & 1) | (((tid >> 3) & 1) << 1) | ((it & 1) << 2)
+        return la, lb, lc
+    assert len({elem(t, i) for t in range(256) for i in range(2)}) == 512
+    orders = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+    for it in range(2):
+        for w in range(8):
+            E = [elem(32 * w + lane, it) for lane in range(32)]
+            for o in orders:
+                assert wavefronts([w3_block_offset(e[o[0]], e[o[1]], e[o[2]], 1) for e in E]) == 1, (it, w, o)
+            for u, v in [(0, 1), (0, 2), (1, 0), (1, 2), (2, 0), (2, 1)]:  # Voovv rows of 8
+                assert wavefronts([8 * e[u] + e[v] for e in E]) == 1
+
+
+def test_w3_epilogue_block_walk_matches_the_layout():
+    """Columns that are a or b (or c past the float4 path): block part linear in the
+    8-wide block, plus one of eight in-block offsets fixed by the row."""
+    T = 5
+    for rn in range(3):  # role of the column index: 0 a, 1 b, 2 c
+        for rh in range(3):
+            if rh == rn:
+                continue
+            rl = 3 - rn - rh
+            for hi, lo, n0 in [(0, 0, 0), (13, 29, 32), (39, 7, 0), (22, 31, 32)]:
+                fa = hi if rh == 0 else (lo if rl == 0 else 0)
+                fb = hi if rh == 1 else (lo if rl == 1 else 0)
+                fc = hi if rh == 2 else (lo if rl == 2 else 0)
+                nb0 = n0 >> 3
+                bA, bB, bC = (nb0 if rn == 0 else fa >> 3), (nb0 if rn == 1 else fb >> 3), (nb0 if rn == 2 else fc >> 3)
+                blk0 = ((bA * T + bB) * T + bC) * 512
+                gstride = (T * T if rn == 0 else (T if rn == 1 else 1)) * 512
+                for j in range(32):
+                    e = j & 7
+                    x, y, z = (e if rn == 0 else fa & 7), (e if rn == 1 else fb & 7), (e if rn == 2 else fc & 7)
+                    loc = 64 * x + 8 * (y ^ x) + (z ^ ((5 * y) & 7))
+                    n = n0 + j
+                    abc = [fa, fb, fc]
+                    abc[rn] = n
+                    assert blk0 + (j >> 3) * gstride + loc == w3_block_offset(*abc, T)

@@ -68,6 +68,13 @@ void reset_state(Ctx& c) {
   c.store.clear();
   c.shapes.clear();
   c.loaded = c.have_ccsd = c.have_hbar = c.have_lambda = c.have_tgrad = false;
+  // the old blocks went back to the stream-ordered pool, which keeps what it is given; hand
+  // it to the device so that the cached tensor-core operands of the next Hamiltonian
+  // (cudaMalloc) find it free (a second no=32/nv=320 load on one context otherwise spent
+  // 4.4 s in its first record sweep)
+  cudaMemPool_t pool;
+  if (cudaStreamSynchronize(c.stream) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, c.device) == cudaSuccess)
+    cudaMemPoolTrimTo(pool, 0);
 }
 }  // namespace
 

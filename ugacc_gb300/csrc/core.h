@@ -289,6 +289,16 @@ struct GemmEpilogue {  // C offset of element (m, n): (m / msplit) * s_mhi + (m 
   int64_t s_mhi = 0, s_mlo = 0, s_n = 1;
 };
 
+// Blocked W3 layout of the mixed (T) path: W[a][b][c] of one tuple in 8 x 8 x 8 blocks,
+// block (a/8, b/8, c/8) at ((a/8 * T + b/8) * T + c/8) * 512 (T = ceil(nv/8) blocks per
+// index), element (x, y, z) = (a%8, b%8, c%8) of a block at 64 x + 8 (y ^ x) + (z ^ (5y % 8)).
+// Every tile the energy reads is then one contiguous 2 KB block, and the swizzle makes its
+// six index orders conflict-free shared-memory reads for the energy kernel's thread order.
+__host__ __device__ __forceinline__ int64_t w3_block_offset(int64_t a, int64_t b, int64_t c, int64_t T) {
+  const int x = (int)(a & 7), y = (int)(b & 7), z = (int)(c & 7);
+  return (((a >> 3) * T + (b >> 3)) * T + (c >> 3)) * 512 + 64 * x + 8 * (y ^ x) + (z ^ ((5 * y) & 7));
+}
+
 struct GemmPtrs {
   const double* A;
   const double* B;
@@ -352,10 +362,20 @@ void triples_energy(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, con
 // The same from an FP32 W3 (mixed form) held as nparts partial arrays part_stride floats
 // apart (W3 = their sum): per-element arithmetic in FP32, the energy sum in FP64
 // (compensated).
+// With f32in (FP32 copies of Voovv, t1 and eps made once per (T) call by triples_f32_inputs,
+// laid out by triples_f32_layout; nv % 4 == 0) the pipelined kernel runs on W3 in the
+// blocked layout of w3_block_offset, part_stride floats per array; without it the
+// padded-tile kernel on the plain [a][b][c] layout.
 int64_t triples_f32_partials(int nv);  // partial sums per tuple written by triples_energy_f32
+struct TriplesF32Layout {
+  int64_t off_t1, off_ev, off_eo, total;  // float offsets of t1, virtual and occupied energies; total floats
+};
+TriplesF32Layout triples_f32_layout(int no, int nv);
+void triples_f32_inputs(Ctx& c, int no, int nv, const double* t1, const double* Voovv, const double* eps,
+                        float* out);
 void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, int nparts,
                         int64_t part_stride, const double* t1, const double* Voovv, const double* eps,
-                        double* d_partial);
+                        double* d_partial, const float* f32in = nullptr);
 
 // Pair-symmetric particle ladder (sum_ef W_abef tau_ijef = S + sign A over packed pairs,
 // W and tau invariant under the simultaneous pair swap):

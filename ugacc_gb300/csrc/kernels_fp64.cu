@@ -960,29 +960,35 @@ __global__ void __launch_bounds__(TNT) triples_energy_f32_tiled_kernel(int no, i
   const double tot = block_sum(s);
   if (threadIdx.x == 0) partial[(int64_t)t * ntri + r] = tot;
 }
-// Pipelined form of the FP32 energy for nv % 4 == 0 (W3 rows of 16-byte chunks): a
-// persistent block walks items (tuple t, tile triple r), item = t * ntri + r, in steps of
-// the grid.  While it computes item n from one shared-memory stage, the W3 tiles of item
-// n + G land in the other stage by 16-byte cp.async (no registers held, out-of-range rows
-// zero-filled) and the Voovv / t1 / eps values of item n + G wait in registers, to be
-// stored as floats once item n is done.  The NP partial arrays stay separate in shared
-// memory and are added where an element is read.  Tile rows swap their two 16-byte halves
-// on odd y, and the threads take the elements of a tile in a bit-permuted order: with those
-// two choices the six permuted reads of an element cost 1.33 shared-memory wavefronts on
-// average (1.67 for the padded tiles above) and the Voovv reads none extra.
-constexpr int EP_THREADS = 128;
-constexpr int EP_WROW = 8;            // floats per tile row
-constexpr int EP_WX = 72;             // floats per tile x plane: 8 rows and 8 of padding
-constexpr int EP_WTILE = ET * EP_WX;  // floats per tile
+// Pipelined form of the FP32 energy for nv % 4 == 0, W3 in the blocked layout of
+// w3_block_offset: a persistent block walks items (tuple t, tile triple r), item =
+// t * ntri + r, in steps of the grid.  While it computes item n from one shared-memory
+// stage, every input of item n + G lands in the other stage by 16-byte cp.async (no
+// registers held): the 18 W3 tiles (6 index orders x 3 partial arrays), each one
+// contiguous 2 KB block, and FP32 copies of the Voovv blocks, t1 rows and virtual orbital
+// energies (made once per (T) call; rows outside nv zero-filled).  The partial arrays stay
+// separate in shared memory and are added where an element is read.  The blocks' swizzle
+// and the threads' bit-permuted order over a tile make every shared-memory read of the
+// energy loop conflict-free (one wavefront per warp read).  No FP64 instruction runs per
+// element (the FP64 pipe of this part is narrow): the item's sum is formed in FP32 per
+// warp and in FP64 across the warps.
+constexpr int EP_THREADS = 256;
+constexpr int EP_WTILE = ET * ET * ET;  // floats per tile (one block)
 template <int NP>
 struct EpStage {
   float W[NP][6][EP_WTILE];
   float V[3][6][ET * ET];  // Vij, Vik, Vjk on the 6 ordered role pairs, rows of 8
-  float t1[3][3][ET];
-  float ev[3][ET];
+  float t1[3][3][ET];      // t1 rows i, j, k on the 3 role ranges
+  float ev[3][ET];         // virtual orbital energies on the 3 role ranges
   double red[EP_THREADS / 32];
 };
 static_assert(sizeof(EpStage<3>) % 16 == 0 && sizeof(EpStage<1>) % 16 == 0, "16-byte stage alignment");
+static_assert(offsetof(EpStage<3>, V) % 16 == 0 && offsetof(EpStage<3>, t1) % 16 == 0 &&
+                  offsetof(EpStage<3>, ev) % 16 == 0 && offsetof(EpStage<1>, V) % 16 == 0 &&
+                  offsetof(EpStage<1>, t1) % 16 == 0 && offsetof(EpStage<1>, ev) % 16 == 0,
+              "16-byte cp.async destinations");
+// the 288 + 18 + 6 chunks of the Voovv blocks, t1 rows and energies of one item
+constexpr int EP_SIDE_CHUNKS = 3 * 6 * ET * 2 + 3 * 3 * 2 + 3 * 2;
 
 __device__ __forceinline__ void ep_cp16(void* dst, const void* src, bool valid) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -991,22 +997,42 @@ __device__ __forceinline__ void ep_cp16(void* dst, const void* src, bool valid) 
 __device__ __forceinline__ void ep_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void ep_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
+// FP32 copies for the pipelined energy: Voovv [no][no][nv][nv] at 0, t1 [no][nv] at off_t1,
+// the virtual energies [nv] at off_ev, the occupied ones [no] at off_eo
+__global__ void triples_f32_inputs_kernel(int no, int nv, const double* __restrict__ t1,
+                                          const double* __restrict__ Voovv, const double* __restrict__ eps,
+                                          float* __restrict__ out, int64_t off_t1, int64_t off_ev, int64_t off_eo) {
+  const int64_t nV = (int64_t)no * no * nv * nv, nT = (int64_t)no * nv, n = nV + nT + nv + no;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    if (x < nV)
+      out[x] = (float)Voovv[x];
+    else if (x < nV + nT)
+      out[off_t1 + (x - nV)] = (float)t1[x - nV];
+    else if (x < nV + nT + nv)
+      out[off_ev + (x - nV - nT)] = (float)eps[no + (x - nV - nT)];
+    else
+      out[off_eo + (x - nV - nT - nv)] = (float)eps[x - nV - nT - nv];
+  }
+}
+
 template <int NP>
 __global__ void __launch_bounds__(EP_THREADS, 2)
     triples_energy_pipe_kernel(int no, int nv, const int* __restrict__ tuples, const int* __restrict__ tri, int ntri,
-                               int64_t nitems, const float* __restrict__ W3, int64_t part_stride,
-                               const double* __restrict__ t1, const double* __restrict__ Voovv,
-                               const double* __restrict__ eps, double* __restrict__ partial) {
+                               int64_t nitems, const float* __restrict__ W3, int64_t part_stride, int T,
+                               const float* __restrict__ f32, int64_t off_t1, int64_t off_ev, int64_t off_eo,
+                               double* __restrict__ partial) {
   extern __shared__ __align__(16) unsigned char ep_smem[];
   EpStage<NP>* st = reinterpret_cast<EpStage<NP>*>(ep_smem);
   const int tid = threadIdx.x;
-  const int64_t nv2 = (int64_t)nv * nv, nv3 = nv2 * nv;
+  const int64_t nv2 = (int64_t)nv * nv, per = (int64_t)T * T * T * EP_WTILE;  // W3 floats per tuple
+  const float* Vf = f32;
+  const float* t1f = f32 + off_t1;
+  const float* evf = f32 + off_ev;
+  const float* eof = f32 + off_eo;
   constexpr uint64_t kPerm = 0x24ull | (0x18ull << 6) | (0x21ull << 12) | (0x09ull << 18) | (0x12ull << 24) |
                              (0x06ull << 30);
-  // this thread's W3 chunk in every tile: row (cx, cy), 16-byte half ch
-  const int cx = tid >> 4, cy = (tid >> 1) & 7, ch = tid & 1;
-  double vreg[9];
-  double treg = 0.0;
+  // this thread's W3 chunk: 16 bytes at 4 c16 floats into the blocks of tiles 3 h .. 3 h + 2
+  const int c16 = tid & 127, h = tid >> 7;
   auto ranges = [&](int64_t item, int& Ra, int& Rb, int& Rc, int& t) {
     t = (int)(item / ntri);
     const int code = tri[item - (int64_t)t * ntri];
@@ -1014,50 +1040,47 @@ __global__ void __launch_bounds__(EP_THREADS, 2)
     Rb = ((code >> 10) & 1023) * ET;
     Rc = (code >> 20) * ET;
   };
-  auto issue = [&](int64_t item, int s) {  // W3 tiles by cp.async, the rest into registers
+  auto issue = [&](int64_t item, int s) {
     int Ra, Rb, Rc, t;
     ranges(item, Ra, Rb, Rc, t);
     auto R0 = [&](int role) { return role == 0 ? Ra : (role == 1 ? Rb : Rc); };
-    const float* Wt = W3 + (int64_t)t * nv3;
+    const float* Wt = W3 + (int64_t)t * per;
 #pragma unroll
-    for (int p = 0; p < 6; p++) {
+    for (int pp = 0; pp < 3; pp++) {
+      const int p = 3 * h + pp;
       const uint64_t c6 = kPerm >> (6 * p);
-      const int gx = R0((int)(c6 & 3)) + cx, gy = R0((int)((c6 >> 2) & 3)) + cy, gz = R0((int)((c6 >> 4) & 3)) + 4 * ch;
-      const bool ok = gx < nv && gy < nv && gz < nv;
-      const float* src = Wt + (ok ? ((int64_t)gx * nv + gy) * nv + gz : 0);
-      float* dst = &st[s].W[0][p][cx * EP_WX + cy * EP_WROW + ((ch ^ (cy & 1)) << 2)];
+      const int64_t X = R0((int)(c6 & 3)) / ET, Y = R0((int)((c6 >> 2) & 3)) / ET, Z = R0((int)((c6 >> 4) & 3)) / ET;
+      const float* src = Wt + ((X * T + Y) * T + Z) * EP_WTILE + 4 * c16;
+      float* dst = &st[s].W[0][p][4 * c16];
 #pragma unroll
-      for (int q = 0; q < NP; q++) ep_cp16(dst + q * 6 * EP_WTILE, src + q * part_stride, ok);
+      for (int q = 0; q < NP; q++) ep_cp16(dst + q * 6 * EP_WTILE, src + q * part_stride, true);
     }
     const int i = tuples[3 * t], j = tuples[3 * t + 1], k = tuples[3 * t + 2];
-#pragma unroll
-    for (int q = 0; q < 9; q++) {  // element e = tid + 128 q of [3][6][8][8]
-      const int e = tid + EP_THREADS * q;
-      const int m = e / 384, pid = (e / 64) % 6, x = (e / 8) % 8, y = e % 8;
-      const int u = pid / 2, v0 = pid % 2, v = v0 < u ? v0 : v0 + 1;
-      const int gx = R0(u) + x, gy = R0(v) + y;
-      const double* Vm = Voovv + ((m == 2 ? (int64_t)j : (int64_t)i) * no + (m == 0 ? j : k)) * nv2;
-      vreg[q] = (gx < nv && gy < nv) ? Vm[(int64_t)gx * nv + gy] : 0.0;
+    for (int c = tid; c < EP_SIDE_CHUNKS; c += EP_THREADS) {
+      const float* src;
+      float* dst;
+      bool ok;
+      if (c < 288) {  // Voovv block m on role pair pid, row x, half hf
+        const int m = c / 96, pid = (c / 16) % 6, x = (c / 2) % 8, hf = c % 2;
+        const int u = pid / 2, v0 = pid % 2, v = v0 < u ? v0 : v0 + 1;
+        const int gx = R0(u) + x, gy = R0(v) + 4 * hf;
+        ok = gx < nv && gy < nv;
+        src = Vf + ((m == 2 ? (int64_t)j : (int64_t)i) * no + (m == 0 ? j : k)) * nv2 + (ok ? (int64_t)gx * nv + gy : 0);
+        dst = &st[s].V[m][pid][x * ET + 4 * hf];
+      } else if (c < 306) {  // t1 row m on role range
+        const int d = c - 288, m = d / 6, role = (d / 2) % 3, hf = d % 2;
+        const int row = m == 0 ? i : (m == 1 ? j : k), g = R0(role) + 4 * hf;
+        ok = g < nv;
+        src = t1f + (int64_t)row * nv + (ok ? g : 0);
+        dst = &st[s].t1[m][role][4 * hf];
+      } else {  // virtual energies on role range
+        const int d = c - 306, role = d / 2, hf = d % 2, g = R0(role) + 4 * hf;
+        ok = g < nv;
+        src = evf + (ok ? g : 0);
+        dst = &st[s].ev[role][4 * hf];
+      }
+      ep_cp16(dst, src, ok);
     }
-    if (tid < 72) {
-      const int m = tid / 24, role = (tid / 8) % 3, g = R0(role) + tid % 8;
-      const int row = m == 0 ? i : (m == 1 ? j : k);
-      treg = g < nv ? t1[(int64_t)row * nv + g] : 0.0;
-    } else if (tid < 96) {
-      const int g = R0((tid - 72) / 8) + tid % 8;
-      treg = g < nv ? eps[no + g] : 0.0;
-    }
-  };
-  auto store = [&](int s) {
-#pragma unroll
-    for (int q = 0; q < 9; q++) {
-      const int e = tid + EP_THREADS * q;
-      st[s].V[e / 384][(e / 64) % 6][e % 64] = (float)vreg[q];
-    }
-    if (tid < 72)
-      st[s].t1[tid / 24][(tid / 8) % 3][tid % 8] = (float)treg;
-    else if (tid < 96)
-      st[s].ev[(tid - 72) / 8][tid % 8] = (float)treg;
   };
 
   const int64_t G = gridDim.x;
@@ -1065,7 +1088,6 @@ __global__ void __launch_bounds__(EP_THREADS, 2)
   if (item >= nitems) return;
   issue(item, 0);
   ep_commit();
-  store(0);
   for (int s = 0; item < nitems; item += G, s ^= 1) {
     const int64_t nxt = item + G;
     if (nxt < nitems) issue(nxt, s ^ 1);
@@ -1075,11 +1097,11 @@ __global__ void __launch_bounds__(EP_THREADS, 2)
     int Ra, Rb, Rc, t;
     ranges(item, Ra, Rb, Rc, t);
     const int i = tuples[3 * t], j = tuples[3 * t + 1], k = tuples[3 * t + 2];
-    const float eijk = (float)(eps[i] + eps[j] + eps[k]);
+    const float eijk = eof[i] + eof[j] + eof[k];
     const float fac = 2.0f - (float)((i == j) + (i == k) + (j == k));
     const EpStage<NP>& S = st[s];
     auto W = [&](int p, int x, int y, int z) {
-      const int o = x * EP_WX + y * EP_WROW + ((((z >> 2) ^ (y & 1)) << 2) | (z & 3));
+      const int o = 64 * x + 8 * (y ^ x) + (z ^ ((5 * y) & 7));  // w3_block_offset within a block
       float w = S.W[0][p][o];
 #pragma unroll
       for (int q = 1; q < NP; q++) w += S.W[q][p][o];
@@ -1093,9 +1115,10 @@ __global__ void __launch_bounds__(EP_THREADS, 2)
     float sf = 0.f;
 #pragma unroll
     for (int it = 0; it < ET * ET * ET / EP_THREADS; it++) {
-      const int la = ((tid >> 1) & 1) | (((tid >> 5) & 1) << 1) | (((it >> 1) & 1) << 2);
-      const int lb = ((tid >> 4) & 1) | (((tid >> 3) & 1) << 1) | (((tid >> 6) & 1) << 2);
-      const int lc = ((tid >> 2) & 1) | ((tid & 1) << 1) | ((it & 1) << 2);
+      // the order over the tile that makes the six permuted reads conflict-free
+      const int la = (tid & 1) | (((tid >> 6) & 1) << 1) | (((tid >> 7) & 1) << 2);
+      const int lb = ((tid >> 2) & 1) | (((tid >> 1) & 1) << 1) | (((tid >> 5) & 1) << 2);
+      const int lc = ((tid >> 4) & 1) | (((tid >> 3) & 1) << 1) | ((it & 1) << 2);
       const int a = Ra + la, b = Rb + lb, c = Rc + lc;
       if (a >= nv || b > a || c > b) continue;
       const float wabc = W(0, la, lb, lc), wacb = W(1, la, lc, lb), wbac = W(2, lb, la, lc);
@@ -1113,13 +1136,16 @@ __global__ void __launch_bounds__(EP_THREADS, 2)
       sf += ((Y3 - 2.0f * Z3) * (wabc + wbca + wcab) + (Z3 - 2.0f * Y3) * (wacb + wbac + wcba) + 3.0f * X3) * deg *
             fac / denom;
     }
-    double d = (double)sf;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-    if ((tid & 31) == 0) st[s].red[tid >> 5] = d;
-    if (nxt < nitems) store(s ^ 1);
+    for (int o = 16; o > 0; o >>= 1) sf += __shfl_xor_sync(0xffffffffu, sf, o);
+    if ((tid & 31) == 0) st[s].red[tid >> 5] = (double)sf;
     __syncthreads();
-    if (tid == 0) partial[item] = ((S.red[0] + S.red[1]) + S.red[2]) + S.red[3];
+    if (tid == 0) {
+      double tot = 0.0;
+#pragma unroll
+      for (int w = 0; w < EP_THREADS / 32; w++) tot += S.red[w];
+      partial[item] = tot;
+    }
   }
 }
 
@@ -1255,9 +1281,29 @@ void unpack_ladder(Ctx& c, int no, int nv, double alpha, const double* S, const 
   check_launch("unpack_ladder");
 }
 
+TriplesF32Layout triples_f32_layout(int no, int nv) {
+  auto up4 = [](int64_t n) { return (n + 3) / 4 * 4; };
+  TriplesF32Layout L;
+  L.off_t1 = up4((int64_t)no * no * nv * nv);
+  L.off_ev = L.off_t1 + up4((int64_t)no * nv);
+  L.off_eo = L.off_ev + up4(nv);
+  L.total = L.off_eo + up4(no);
+  return L;
+}
+
+void triples_f32_inputs(Ctx& c, int no, int nv, const double* t1, const double* Voovv, const double* eps,
+                        float* out) {
+  const TriplesF32Layout L = triples_f32_layout(no, nv);
+  const int64_t n = (int64_t)no * no * nv * nv + (int64_t)no * nv + nv + no;
+  triples_f32_inputs_kernel<<<grid_for(n), 256, 0, c.stream>>>(no, nv, t1, Voovv, eps, out, L.off_t1, L.off_ev,
+                                                              L.off_eo);
+  count_launch();
+  check_launch("triples_f32_inputs");
+}
+
 void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples, const float* W3, int nparts,
                         int64_t part_stride, const double* t1, const double* Voovv, const double* eps,
-                        double* d_partial) {
+                        double* d_partial, const float* f32in) {
   UCC_REQUIRE(ntuple <= 65535, UCC_BAD_ARGS, "triples_energy: too many tuples per batch");
   const int T = (nv + ET - 1) / ET;
   UCC_REQUIRE(T <= 1024, UCC_BAD_ARGS, "triples_energy: too many virtual tiles");
@@ -1268,9 +1314,12 @@ void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples,
   Scratch dtri(c, sizeof(int) * tri.size());
   UCC_CUDA(cudaMemcpyAsync(dtri.p, tri.data(), sizeof(int) * tri.size(), cudaMemcpyHostToDevice, c.stream));
   UCC_REQUIRE(nparts == 1 || nparts == 3, UCC_BAD_ARGS, "triples_energy: 1 or 3 W3 partial arrays");
-  const bool pipe = nv % 4 == 0 && part_stride % 4 == 0 && reinterpret_cast<uintptr_t>(W3) % 16 == 0;
-  if (pipe) {
-    // persistent blocks, as many as fit (two per SM by their two 47 KB stages)
+  if (f32in) {  // W3 in the blocked layout
+    UCC_REQUIRE(nv % 4 == 0 && part_stride % 4 == 0 && reinterpret_cast<uintptr_t>(W3) % 16 == 0 &&
+                    reinterpret_cast<uintptr_t>(f32in) % 16 == 0,
+                UCC_BAD_ARGS, "triples_energy: the blocked W3 form needs nv % 4 == 0 and 16-byte aligned arrays");
+    const TriplesF32Layout L = triples_f32_layout(no, nv);
+    // persistent blocks, as many as fit (two per SM by their two 42 KB stages)
     static thread_local int sms[64] = {0}, per_sm[2][64] = {{0}};
     const int dev = c.device & 63, np = nparts == 3 ? 0 : 1;
     const size_t smem = nparts == 3 ? 2 * sizeof(EpStage<3>) : 2 * sizeof(EpStage<1>);
@@ -1293,12 +1342,12 @@ void triples_energy_f32(Ctx& c, int no, int nv, int ntuple, const int* d_tuples,
     const unsigned grid = (unsigned)std::min<int64_t>(nitems, (int64_t)sms[dev] * per_sm[np][dev]);
     if (nparts == 3)
       triples_energy_pipe_kernel<3><<<grid, EP_THREADS, smem, c.stream>>>(
-          no, nv, d_tuples, static_cast<const int*>(dtri.p), (int)tri.size(), nitems, W3, part_stride, t1, Voovv,
-          eps, d_partial);
+          no, nv, d_tuples, static_cast<const int*>(dtri.p), (int)tri.size(), nitems, W3, part_stride, T, f32in,
+          L.off_t1, L.off_ev, L.off_eo, d_partial);
     else
       triples_energy_pipe_kernel<1><<<grid, EP_THREADS, smem, c.stream>>>(
-          no, nv, d_tuples, static_cast<const int*>(dtri.p), (int)tri.size(), nitems, W3, part_stride, t1, Voovv,
-          eps, d_partial);
+          no, nv, d_tuples, static_cast<const int*>(dtri.p), (int)tri.size(), nitems, W3, part_stride, T, f32in,
+          L.off_t1, L.off_ev, L.off_eo, d_partial);
     count_launch();
     check_launch("triples_energy_f32");
     UCC_CUDA(cudaStreamSynchronize(c.stream));  // the tile list is freed on return

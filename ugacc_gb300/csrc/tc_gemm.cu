@@ -93,7 +93,26 @@ struct Params {
   // and the three products are issued from it (a third less operand traffic than one
   // stage per product); nst stages of stage_bytes each
   int fused, nst, stage_bytes;
+  // tblk > 0 (FP32 output of the (T) tuple GEMMs, alpha 1, beta 0): W3 in the blocked
+  // layout of w3_block_offset with tblk blocks per index; the strides s_mhi, s_mlo, s_n
+  // (nv^2, nv or 1, msplit = nv) say which of a, b, c each index is
+  int tblk = 0;
 };
+
+// v[p] <- v[p ^ k] for 0 <= k < 8: three conditional swaps (selects, no indexed registers)
+__device__ __forceinline__ void xor_swap8(float (&v)[8], int k) {
+#pragma unroll
+  for (int bit = 1; bit < 8; bit <<= 1) {
+    const bool s = (k & bit) != 0;
+#pragma unroll
+    for (int e = 0; e < 8; e++)
+      if ((e & bit) == 0) {
+        const float lo = v[e], hi = v[e | bit];
+        v[e] = s ? hi : lo;
+        v[e | bit] = s ? lo : hi;
+      }
+  }
+}
 
 // the split products of one K block: (A part, B part), part 0 = hi, 1 = lo (2 parts) or
 // 0 = hi, 1 = mid, 2 = lo (3 parts)
@@ -366,7 +385,49 @@ __global__ void __launch_bounds__(THREADS, 1)
           // with beta != 0 all 32 old values are loaded before the first store, so the
           // loads are in flight together instead of each waiting behind a store that
           // might alias it
-          if (p.C32) {
+          if (p.C32 && p.tblk) {
+            // blocked W3: each index placed by its linear stride (nv^2 a, nv b, 1 c)
+            const int64_t nvv = ep.msplit, hi = m / nvv, lo = m % nvv, T = p.tblk;
+            const int rn = ep.s_n == 1 ? 2 : (ep.s_n == nvv ? 1 : 0);
+            const int rh = ep.s_mhi == 1 ? 2 : (ep.s_mhi == nvv ? 1 : 0);
+            float* Cw = p.C32 + coff;
+            if (rn == 2 && n0 + 32 <= p.N) {
+              // the 32 columns are c: four 8-wide c blocks, each a contiguous 32 bytes
+              // holding element z at z ^ k, stored as two float4 after the same swap
+              const int64_t a = rh == 0 ? hi : lo, b = rh == 0 ? lo : hi;
+              const int x = (int)(a & 7), y = (int)(b & 7), k = (5 * y) & 7;
+              float* base = Cw + (((a >> 3) * T + (b >> 3)) * T) * 512 + 64 * x + 8 * (y ^ x);
+#pragma unroll
+              for (int g = 0; g < 4; g++) {
+                float v[8];
+#pragma unroll
+                for (int e = 0; e < 8; e++) v[e] = __uint_as_float(r[8 * g + e]);
+                xor_swap8(v, k);
+                float4* dst = reinterpret_cast<float4*>(base + ((n0 >> 3) + g) * 512);
+                dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+                dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+              }
+            } else {
+              // the 32 columns are four 8-wide blocks of one index (n0 % 32 == 0): the
+              // offset is a block part, linear in the block, plus one of eight in-block
+              // offsets fixed by the row (32-bit: a tuple's blocks hold < 2^31 floats)
+              const int rl = 3 - rn - rh;
+              const int fa = (int)(rh == 0 ? hi : (rl == 0 ? lo : 0)), fb = (int)(rh == 1 ? hi : (rl == 1 ? lo : 0));
+              const int fc = (int)(rh == 2 ? hi : (rl == 2 ? lo : 0)), nb0 = (int)(n0 >> 3), Ti = (int)T;
+              const int bA = rn == 0 ? nb0 : fa >> 3, bB = rn == 1 ? nb0 : fb >> 3, bC = rn == 2 ? nb0 : fc >> 3;
+              const int blk0 = ((bA * Ti + bB) * Ti + bC) * 512;
+              const int gstride = (rn == 0 ? Ti * Ti : (rn == 1 ? Ti : 1)) * 512;
+              int loc[8];
+#pragma unroll
+              for (int e = 0; e < 8; e++) {
+                const int x = rn == 0 ? e : (fa & 7), y = rn == 1 ? e : (fb & 7), z = rn == 2 ? e : (fc & 7);
+                loc[e] = 64 * x + 8 * (y ^ x) + (z ^ ((5 * y) & 7));
+              }
+#pragma unroll
+              for (int j = 0; j < 32; j++)
+                if (n0 + j < p.N) Cw[blk0 + (j >> 3) * gstride + loc[j & 7]] = __uint_as_float(r[j]);
+            }
+          } else if (p.C32) {
             float* Cf = p.C32 + coff + mo;
             const float af = (float)alpha;
             if (ep.s_n == 1 && beta == 0.0 && af == 1.0f && n0 + 32 <= p.N &&
@@ -1752,14 +1813,17 @@ void mixed_triples_release(Ctx& c) {
 }
 
 // W3 of nb tuples as three FP32 partial arrays, one per pair of terms: pair pq writes
-// W3 + (pq * nb + b) * nv^3 for tuple b with beta 0 (no read-modify-write of W3 in the
-// epilogue); triples_energy_f32 adds the three while staging its tiles.  The three launches
-// go out back to back with their own row tables; the caller synchronises.
-bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, float* W3) {
+// W3 + (pq * nb + b) * S for tuple b with beta 0 (no read-modify-write of W3 in the
+// epilogue), S = nv^3 in the plain [a][b][c] layout (tblk = 0) or tblk^3 * 512 in the
+// blocked layout of w3_block_offset; triples_energy_f32 adds the three while staging its
+// tiles.  The three launches go out back to back with their own row tables; the caller
+// synchronises.
+bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, float* W3, int tblk) {
   using namespace tc;
   Cache& k = cache(c);
   Triples& T = *k.triples;
   const int64_t no = c.no, nv = c.nv, nv2 = nv * nv, nv3 = nv2 * nv;
+  const int64_t per = tblk ? (int64_t)tblk * tblk * tblk * 512 : nv3;  // floats per tuple and partial
   TriplesTerm terms[6];
   triples_terms(nv, terms);
   // The six terms in pairs that write the same W3 layout: the first term of a pair uses
@@ -1770,7 +1834,7 @@ bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, float* W3) {
   std::vector<int> arow(6 * nb), brow(6 * nb);
   std::vector<int64_t> coff(3 * nb);
   for (int pq = 0; pq < 3; pq++) {
-    for (int b = 0; b < nb; b++) coff[pq * nb + b] = ((int64_t)pq * nb + b) * nv3;
+    for (int b = 0; b < nb; b++) coff[pq * nb + b] = ((int64_t)pq * nb + b) * per;
     for (int t = 0; t < 2; t++) {
       const TriplesTerm& tm = terms[pairs[pq][t]];
       for (int b = 0; b < nb; b++) {
@@ -1798,6 +1862,7 @@ bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, float* W3) {
     p.beta = 0.0;
     p.C = nullptr;
     p.C32 = W3;  // W3 in FP32: its rounding (~6e-8) is far below the split products' (~5e-6)
+    p.tblk = tblk;
     p.epi.msplit = nv;
     p.epi.s_mhi = t0.su;
     p.epi.s_mlo = t0.sv;

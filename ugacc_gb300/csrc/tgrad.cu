@@ -40,7 +40,7 @@
 namespace ucc {
 
 void count_kernel_launch();
-bool mixed_triples_batch(Ctx& c, int nbatch, const int* h_tuples, float* W3);
+bool mixed_triples_batch(Ctx& c, int nbatch, const int* h_tuples, float* W3, int tblk = 0);
 bool mixed_triples_prepare(Ctx& c, int max_batch);
 void mixed_triples_release(Ctx& c);
 void triples_operands_fp64(Ctx& c, Tensor& Acat, Tensor& Bcat);

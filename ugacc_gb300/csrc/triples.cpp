@@ -12,6 +12,7 @@
 // forms V3, X3, Y3, Z3 and the a>=b>=c weighted sum per tuple.
 #include <algorithm>
 #include <cmath>
+#include <memory>
 
 #include "cc.h"
 
@@ -20,7 +21,7 @@ namespace ucc {
 double flops_triples(double no, double nv) { return 2.0 * no * (no + 1) * (no + 2) * nv * nv * nv * (nv + no); }
 
 // mixed-precision tuple GEMMs (tc_gemm.cu); false if not available for this shape
-bool mixed_triples_batch(Ctx& c, int nbatch, const int* h_tuples, float* W3);
+bool mixed_triples_batch(Ctx& c, int nbatch, const int* h_tuples, float* W3, int tblk = 0);
 bool mixed_triples_prepare(Ctx& c, int max_batch);
 void mixed_triples_release(Ctx& c);
 
@@ -94,7 +95,11 @@ double run_triples(Ctx& c) {
   // W3 bytes per tuple: FP64, or three FP32 partial arrays (one per pair of terms) in the
   // mixed form
   const bool want_mixed = c.opt.precision == UCC_MIXED && !c.force_fp64;
-  const double w3_bytes = (want_mixed ? 12.0 : 8.0) * (double)nv3;
+  // nv % 4 == 0: the pipelined energy kernel, which reads W3 in 8 x 8 x 8 blocks
+  // (w3_block_offset; nv rounded up to whole blocks)
+  const int tblk = want_mixed && nv % 4 == 0 ? (nv + 7) / 8 : 0;
+  const int64_t w3_per = tblk ? (int64_t)tblk * tblk * tblk * 512 : nv3;  // elements per tuple and array
+  const double w3_bytes = (want_mixed ? 12.0 : 8.0) * (double)w3_per;
   const int batch = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)(budget / w3_bytes), 4096, ntup}));
 
   Scratch dtup(c, sizeof(int) * tuples.size());
@@ -108,18 +113,24 @@ double run_triples(Ctx& c) {
   // FP64 path: concatenated operands A_x and B_yz
   Tensor Acat, Bcat;
   if (!mixed) triples_operands_fp64(c, Acat, Bcat);
+  // mixed path: FP32 copies of the energy's integral inputs (pipelined energy kernel)
+  std::unique_ptr<Scratch> f32in;
+  if (mixed && tblk) {
+    f32in = std::make_unique<Scratch>(c, sizeof(float) * (size_t)triples_f32_layout(no, nv).total);
+    triples_f32_inputs(c, no, nv, t1.p, c.get("Voovv").p, c.get("eps").p, static_cast<float*>(f32in->p));
+  }
   Scratch dptr(c, sizeof(GemmPtrs) * batch * 6);
   GemmPtrs* dp = static_cast<GemmPtrs*>(dptr.p);
   for (int t0 = 0; t0 < ntup; t0 += batch) {
     const int nb = std::min(batch, ntup - t0);
     if (mixed)
-      mixed_triples_batch(c, nb, tuples.data() + 3 * t0, static_cast<float*>(W3.p));
+      mixed_triples_batch(c, nb, tuples.data() + 3 * t0, static_cast<float*>(W3.p), f32in ? tblk : 0);
     else
       triples_w3_fp64(c, Acat, Bcat, tuples.data() + 3 * t0, nb, W3.d(), dp);
     if (mixed)
       triples_energy_f32(c, no, nv, nb, static_cast<int*>(dtup.p) + 3 * t0, static_cast<const float*>(W3.p), 3,
-                         (int64_t)nb * nv3, t1.p, c.get("Voovv").p, c.get("eps").p,
-                         partial.d() + (int64_t)t0 * pstride);
+                         (int64_t)nb * (f32in ? w3_per : nv3), t1.p, c.get("Voovv").p, c.get("eps").p,
+                         partial.d() + (int64_t)t0 * pstride, f32in ? static_cast<const float*>(f32in->p) : nullptr);
     else
       triples_energy(c, no, nv, nb, static_cast<int*>(dtup.p) + 3 * t0, W3.d(), t1.p, c.get("Voovv").p,
                      c.get("eps").p, partial.d() + (int64_t)t0 * nv);
