@@ -12,8 +12,9 @@ blocks already resident in HBM.  Reported beside it, in the same run:
 * the same mixed solve from the MP2 guess, so that the sweeps the learned guess saves are
   measured on the workload itself;
 * the guess network's training cost (outside the timed region): it is trained on the GPU
-  by the library's own kernels on converged amplitudes of smaller Hamiltonians of the same
-  generator (no=16 / nv=160, seeds 11-14), never on the benchmark Hamiltonian.
+  by the library's own kernels on converged amplitudes of other Hamiltonians of the same
+  generator and shape (no=32 / nv=320, seeds 11 and 12), never on the benchmark
+  Hamiltonian.
 
 value = algorithmic TFLOP/s of the whole job: (CCSD iterations of the FP64 form, i.e. the
 reference's own iteration count) x 2(no^2 nv^4 + 2 no^4 nv^2 + 10 no^3 nv^3 + 8 no^2 nv^3)
@@ -47,8 +48,11 @@ WORKLOADS = {"c2": (16, 160, 1), "c3": (32, 320, 2)}
 NO, NV, SEED = WORKLOADS["c3"]
 WORKLOAD = "ccsd_t_no32_nv320_seed2"
 METRIC = "CCSD(T) wall-s & TFLOP/s vs plain FP64 GPU at |dE|<=1 uEh; iterations saved"
-# training Hamiltonians of the guess network: the same generator, smaller, other seeds
-GUESS_TRAIN = {"no": 16, "nv": 160, "seeds": [11, 12, 13, 14], "row_fraction": 0.25, "epochs": 4, "batch": 8192,
+# training Hamiltonians of the guess network: the same generator and shape as the workload,
+# other seeds (about 6.5e6 sampled rows).  Trained on no=16/nv=160 instead, the network's
+# prediction error on the no=32/nv=320 amplitudes was 0.44 of their size (0.15 when trained
+# at that shape) and it saved one sweep at most.
+GUESS_TRAIN = {"no": 32, "nv": 320, "seeds": [11, 12], "row_fraction": 0.03, "epochs": 4, "batch": 8192,
                "lr": 1e-3, "r_convergence": 1e-8}
 
 
@@ -58,6 +62,7 @@ def select_workload(name):
     WORKLOAD = "ccsd_t_no%d_nv%d_seed%d" % (NO, NV, SEED)
     if name == "c2":
         METRIC = "CCSD(T) TFLOP/s (algorithmic) at no=16/nv=160"
+        GUESS_TRAIN.update({"no": 16, "nv": 160, "seeds": [11, 12, 13, 14], "row_fraction": 0.25})
 
 
 def flops_ccsd_iter(no, nv):

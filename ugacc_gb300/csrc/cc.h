@@ -79,7 +79,7 @@ class MixedSweeps {
  private:
   Ctx& c_;
   bool mixed_, refine_, split_phase_, record_next_ = true;
-  int stalls_ = 0, sweeps_ = 0, digits_ = 9;
+  int stalls_ = 0, sweeps_ = 0, digits_ = 9, split_slow_ = 0;
   double rms_prev_ = INFINITY, anchor_rms_ = INFINITY;
   double record_target_ = 0.0;  // level the deltas after the coming record sweep resolve; 0: full digits
   Kind kind_ = kFp64, last_ = kFp64;

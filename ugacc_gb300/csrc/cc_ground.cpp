@@ -506,9 +506,12 @@ bool MixedSweeps::after(double rms, bool* restart_diis) {
     split++;
     if (!refine_ && rms < rc) done = true;
     // hand over near the split-product noise floor, or when the residual stops falling
-    // within three decades of it (early sweeps of a hard system fall slowly too)
+    // within three decades of it: two sweeps in a row that do not halve it (one slow sweep
+    // is common early on: from a learned guess at no=32/nv=320 the norm went 1.0e-2 ->
+    // 5.3e-3, and handing over there left 10 delta sweeps to do instead of 7)
     const double level = std::max(rc, std::max(c_.opt.mixed_switch, kMixedFloor));
-    if (!done && refine_ && (rms < level || (sweeps_ > 2 && rms < 1e3 * level && rms > 0.5 * rms_prev_))) {
+    split_slow_ = (sweeps_ > 2 && rms < 1e3 * level && rms > 0.5 * rms_prev_) ? split_slow_ + 1 : 0;
+    if (!done && refine_ && (rms < level || split_slow_ >= 2)) {
       split_phase_ = false;
       record_next_ = true;
       // the deltas after this anchor run down to the re-anchoring level, or to r_convergence

@@ -1625,8 +1625,11 @@ void tc_gemm_run(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const do
 }
 
 bool tc_eligible(int64_t M, int64_t N, int64_t K) {
-  // small problems stay on the FP64 path; the tensor tile is 128 x 256 x 64
-  if (std::max(M, N) < 64 || K < 16 || (double)M * N * K < 1e7) return false;
+  // small problems stay on the FP64 path; the tensor tile is 128 x 256 x 64.  A small
+  // output with a long K (a reduction such as Fmi, 32 x 32 x 3.3e6 at no=32/nv=320:
+  // 6.7 GFLOP, ~6 ms on the FP64 pipe) runs split-K over the SMs despite its mostly empty tile
+  const bool reduction = K >= 65536 && (double)M * N * K >= 1e9;
+  if ((std::max(M, N) < 64 && !reduction) || K < 16 || (double)M * N * K < 1e7) return false;
   return M <= INT32_MAX && N <= INT32_MAX;
 }
 
@@ -1661,7 +1664,9 @@ bool sliced_gemm(Ctx& c, int64_t M, int64_t N, int64_t K, double alpha, const Ma
   // a short K (a few occupied indices) leaves too little work per slice and output: routing
   // the K = 16 contractions of a no=16/nv=160 CCSD solve here instead of the DFMA kernel
   // (operands sliced per call, 45 padded products, the 9-order epilogue) made its sweeps
-  // slower (203 -> 220 ms per solve)
+  // slower (203 -> 220 ms per solve), and the K = 32 ones of no=32/nv=320 (outputs of 1e8,
+  // 6.7 GFLOP) made its record sweeps slower too (606 -> 625 ms at 6 digits, 877 -> 946 ms
+  // at 8): the per-order epilogue passes over the output cost more than the DFMA work
   if (K < 48 || (double)M * N * K < kSlicedMinWork || M > INT32_MAX || N > INT32_MAX) return false;
   // the output must fill at least 1/16 of its 128 x (N rounded to 32) tiles
   const int64_t lo = std::min(M, N), hi = std::max(M, N);
