@@ -65,6 +65,18 @@ def select_workload(name):
         GUESS_TRAIN.update({"no": 16, "nv": 160, "seeds": [11, 12, 13, 14], "row_fraction": 0.25})
 
 
+# DRAM bytes (read + write) per launch of the roofline kernels at no=32/nv=320, from one
+# ncu launch list of the same solve (profiles/ccsd_t_mixed_no32_nv320_launches.md):
+# split GEMM 1331 launches, sliced GEMM 91, DFMA GEMM 87
+TRAFFIC_C3 = {"split": 4.66e9, "sliced": 78.1e9, "dfma": 0.38e9}
+TRAFFIC_SOURCE = ("ncu launch list of the same workload, DRAM read + write per launch averaged over the "
+                  "solve (profiles/ccsd_t_mixed_no32_nv320_launches.md)")
+
+
+def traffic_of(kind, workload):
+    return TRAFFIC_C3[kind] if workload == "c3" else None
+
+
 def flops_ccsd_iter(no, nv):
     return 2.0 * (no**2 * nv**4 + 2 * no**4 * nv**2 + 10 * no**3 * nv**3 + 8 * no**2 * nv**3)
 
@@ -439,7 +451,8 @@ def main():
     if st["tc_gemm_launches"]:
         ach = st["tc_gemm_flops"] / (st["tc_gemm_ms"] * 1e-3) / 1e12
         tc = {"bound": "tensor", "achieved": ach, "peak": bf16s, "unit": "TFLOP/s",
-              "frac": (ach / bf16s) if bf16s else None, "traffic": None,
+              "frac": (ach / bf16s) if bf16s else None, "traffic": traffic_of("split", args.workload),
+              "traffic_unit": "bytes per launch", "traffic_source": TRAFFIC_SOURCE,
               "kernel": "tcgen05 BF16 hi+lo split GEMM (ucc::tc::gemm_kernel), all launches of the step",
               "flops": "algorithmic 2*M*N*K per launch over its CUDA-event time; the tensor pipe executes 3x "
                        "that (hi.hi + hi.lo + lo.hi)",
@@ -452,7 +465,8 @@ def main():
     if st["fp64_gemm_launches"]:
         ach = st["fp64_gemm_flops"] / (st["fp64_gemm_ms"] * 1e-3) / 1e12
         f64g = {"bound": "tensor", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": (ach / fp64_peak) if fp64_peak else None, "traffic": None,
+                "frac": (ach / fp64_peak) if fp64_peak else None, "traffic": traffic_of("dfma", args.workload),
+                "traffic_unit": "bytes per launch", "traffic_source": TRAFFIC_SOURCE,
                 "kernel": "FP64 DFMA GEMM (dgemm_kernel), all launches of the step (contractions below the tensor-"
                           "core thresholds)",
                 "compute_unit": "FP64 pipe (compute bound, not the tensor cores)",
@@ -466,7 +480,8 @@ def main():
         fp64eq = st["sliced_gemm_flops"] / (st["sliced_gemm_ms"] * 1e-3) / 1e12
         ach = st["sliced_gemm_product_flops"] / (st["sliced_gemm_ms"] * 1e-3) / 1e12
         sl = {"bound": "tensor", "achieved": ach, "peak": bf16s, "unit": "TFLOP/s",
-              "frac": (ach / bf16s) if bf16s else None, "traffic": None,
+              "frac": (ach / bf16s) if bf16s else None, "traffic": traffic_of("sliced", args.workload),
+              "traffic_unit": "bytes per launch", "traffic_source": TRAFFIC_SOURCE,
               "kernel": "tcgen05 sliced FP64 GEMM (ucc::tc::sliced_gemm_kernel): products of exact bf16 slices "
                         "per operand (9 for FP64 accuracy; fewer for anchors whose deltas resolve a residual well "
                         "above r_convergence), all launches of the step (record sweeps of the mixed solve)",

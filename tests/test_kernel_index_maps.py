@@ -238,3 +238,52 @@ def test_w3_epilogue_block_walk_matches_the_layout():
                     abc = [fa, fb, fc]
                     abc[rn] = n
                     assert blk0 + (j >> 3) * gstride + loc == w3_block_offset(*abc, T)
+
+
+@pytest.mark.parametrize("nx,nv", [(3, 5), (2, 33), (4, 70)])
+def test_pack_pairs_tiled_writes_every_packed_element_once(nx, nv):
+    """pack_pairs_tiled_kernel: block (tile pair E <= F, row pair x <= y), lanes over e,
+    rows over f; every element of P[x<=y][e<=f] and M[x<y][e<f] written once, from the
+    right t[e][f] and t[f][e]."""
+    import numpy as np
+    rng = np.random.default_rng(nx * 100 + nv)
+    src = rng.standard_normal((nx, nx, nv, nv))
+    vp, vm = nv * (nv + 1) // 2, nv * (nv - 1) // 2
+    npr, nmr = nx * (nx + 1) // 2, nx * (nx - 1) // 2
+    P, M = np.full((npr, vp), np.nan), np.full((max(nmr, 1), max(vm, 1)), np.nan)
+    cnt_p, cnt_m = np.zeros_like(P), np.zeros_like(M)
+    nt = (nv + 31) // 32
+    h = 0.5
+    for bx in range(nt * (nt + 1) // 2):
+        F = 0
+        while (F + 1) * (F + 2) // 2 <= bx:
+            F += 1
+        E = bx - F * (F + 1) // 2
+        for R in range(npr):
+            y = int((np.sqrt(np.float32(8.0 * R + 1.0)) - 1.0) * 0.5)
+            while (y + 1) * (y + 2) // 2 <= R:
+                y += 1
+            while y * (y + 1) // 2 > R:
+                y -= 1
+            x = R - y * (y + 1) // 2
+            t = src[x, y]
+            for c in range(32):
+                for tx in range(32):
+                    f, e = F * 32 + c, E * 32 + tx
+                    if f >= nv or e > f:
+                        continue
+                    a, b = t[e, f], t[f, e]
+                    P[R, f * (f + 1) // 2 + e] = a if e == f else h * (a + b)
+                    cnt_p[R, f * (f + 1) // 2 + e] += 1
+                    if x < y and e < f:
+                        M[y * (y - 1) // 2 + x, f * (f - 1) // 2 + e] = h * (a - b)
+                        cnt_m[y * (y - 1) // 2 + x, f * (f - 1) // 2 + e] += 1
+    assert np.all(cnt_p == 1)
+    if nmr and vm:
+        assert np.all(cnt_m == 1)
+    for y in range(nx):
+        for x in range(y + 1):
+            for f in range(nv):
+                for e in range(f + 1):
+                    want = src[x, y, e, e] if e == f else h * (src[x, y, e, f] + src[x, y, f, e])
+                    assert P[y * (y + 1) // 2 + x, f * (f + 1) // 2 + e] == want

@@ -1230,6 +1230,49 @@ __global__ void pack_tau_kernel(int no, int nv, const double* __restrict__ tau, 
   }
 }
 
+// Tiled form of the two packings for a source whose (x, y) slice is one contiguous
+// nv x nv block t = src + (x * nx + y) * nv^2 (tau: x, y = i, j; <ab|ef>: x, y = a, b):
+//   P[x<=y][e<=f] = h (t[e][f] + t[f][e]) (e < f), t[e][e] (e == f)
+//   M[x<y][e<f]   = h (t[e][f] - t[f][e])
+// with h = 1/2 (tau) or 1 (<ab|ef>).  Block (tile pair, x<=y pair) stages the 32 x 32 tile
+// (E, F) of t and the transposed tile (F, E) in shared memory, both read along rows, and
+// writes the packed elements along e (contiguous in both outputs for fixed f); the pair
+// indices come from a per-block decode instead of an FP64 square root per element (GB300's
+// FP64 pipe made the per-element form run at 0.44-0.77 TB/s).
+__global__ void pack_pairs_tiled_kernel(int nx, int nv, double h, const double* __restrict__ src, double* P,
+                                        double* M) {
+  __shared__ double A[32][33], B[32][33];
+  const int64_t vp = (int64_t)nv * (nv + 1) / 2, vm = (int64_t)nv * (nv - 1) / 2;
+  // tile pair (E <= F) from blockIdx.x: F (F + 1) / 2 + E
+  int F = 0;
+  while ((F + 1) * (F + 2) / 2 <= (int)blockIdx.x) F++;
+  const int E = (int)blockIdx.x - F * (F + 1) / 2;
+  // row pair (x <= y) from blockIdx.y: y (y + 1) / 2 + x
+  const int64_t R = blockIdx.y;
+  int y = (int)((sqrtf(8.0f * (float)R + 1.0f) - 1.0f) * 0.5f);
+  while ((int64_t)(y + 1) * (y + 2) / 2 <= R) y++;
+  while ((int64_t)y * (y + 1) / 2 > R) y--;
+  const int x = (int)(R - (int64_t)y * (y + 1) / 2);
+  const double* t = src + ((int64_t)x * nx + y) * (int64_t)nv * nv;
+  const int e0 = E * 32, f0 = F * 32, tx = threadIdx.x, ty = threadIdx.y;
+  for (int r = ty; r < 32; r += 8) {
+    const int ea = e0 + r, fa = f0 + tx;  // A[r][tx] = t[e0 + r][f0 + tx]
+    A[r][tx] = (ea < nv && fa < nv) ? t[(int64_t)ea * nv + fa] : 0.0;
+    const int fb = f0 + r, eb = e0 + tx;  // B[tx][r] = t[f0 + r][e0 + tx]: B[e][f] = t[f][e]
+    B[tx][r] = (fb < nv && eb < nv) ? t[(int64_t)fb * nv + eb] : 0.0;
+  }
+  __syncthreads();
+  double* Prow = P + R * vp;
+  double* Mrow = x < y ? M + ((int64_t)y * (y - 1) / 2 + x) * vm : nullptr;
+  for (int c = ty; c < 32; c += 8) {  // f = f0 + c, e = e0 + tx along the lanes
+    const int f = f0 + c, e = e0 + tx;
+    if (f >= nv || e > f) continue;
+    const double a = A[tx][c], b = B[tx][c];
+    Prow[(int64_t)f * (f + 1) / 2 + e] = e == f ? a : h * (a + b);
+    if (Mrow && e < f) Mrow[(int64_t)f * (f - 1) / 2 + e] = h * (a - b);
+  }
+}
+
 // R2[ijab] += S[(i,j) sorted][(a,b) sorted] + sign * A[...], sign = (-1)^[i>j] (-1)^[a>b],
 // A = 0 on i == j or a == b
 template <class I>
@@ -1257,6 +1300,14 @@ __global__ void unpack_ladder_kernel(int no, int nv, double alpha, const double*
 void pack_vvvv(Ctx& c, int nv, int mode, const double* H, double* Vp, double* Vm) {
   UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
   const int64_t np = (int64_t)nv * (nv + 1) / 2, nm = (int64_t)nv * (nv - 1) / 2;
+  const int nt = (nv + 31) / 32;
+  if (mode == 0 && np <= 65535) {  // <ab|ef>: the (a, b) slice is one contiguous block
+    pack_pairs_tiled_kernel<<<dim3((unsigned)(nt * (nt + 1) / 2), (unsigned)np), dim3(32, 8), 0, c.stream>>>(
+        nv, nv, 1.0, H, Vp, Vm);
+    count_launch();
+    check_launch("pack_vvvv");
+    return;
+  }
   pack_vvvv_kernel<<<grid_for(np * np + nm * nm), 256, 0, c.stream>>>(nv, mode, H, Vp, Vm);
   count_launch();
   check_launch("pack_vvvv");
@@ -1264,6 +1315,15 @@ void pack_vvvv(Ctx& c, int nv, int mode, const double* H, double* Vp, double* Vm
 
 void pack_tau(Ctx& c, int no, int nv, const double* tau, double* Tp, double* Tm) {
   UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
+  const int64_t op = (int64_t)no * (no + 1) / 2;
+  const int nt = (nv + 31) / 32;
+  if (op <= 65535) {
+    pack_pairs_tiled_kernel<<<dim3((unsigned)(nt * (nt + 1) / 2), (unsigned)op), dim3(32, 8), 0, c.stream>>>(
+        no, nv, 0.5, tau, Tp, Tm);
+    count_launch();
+    check_launch("pack_tau");
+    return;
+  }
   const int64_t n = (int64_t)no * (no + 1) / 2 * nv * (nv + 1) / 2 + (int64_t)no * (no - 1) / 2 * nv * (nv - 1) / 2;
   pack_tau_kernel<<<grid_for(n), 256, 0, c.stream>>>(no, nv, tau, Tp, Tm);
   count_launch();
