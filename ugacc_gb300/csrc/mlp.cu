@@ -226,12 +226,18 @@ unsigned grid1(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64
 // Shared memory (1024-aligned): the second layer's weights as the MMA's B operand, W2^T
 // [256 n][256 k] in four 64-wide K blocks (K-major, 128-byte swizzle: the 16-byte chunk c
 // of row r sits at chunk c ^ (r & 7)); the tile's activations as the A operand [128][256]
-// in the same layout; W1, b1, b2, w3 in FP32; the partial outputs of the column halves.
+// in the same layout; the tile's features [128][16] and MP2 amplitudes; b1, b2, w3 in
+// FP32; the partial outputs of the column halves.  The first layer runs register-blocked:
+// lane l of warp w holds W1 for the hidden units 8l .. 8l+7 for the whole kernel and
+// computes them for the rows 16w .. 16w+15, reading each row's features once as a
+// broadcast (one shared-memory load per 8 multiply-adds; loading W1 from shared memory per
+// multiply-add made the pass load-bound, 107 ms at no=32/nv=320).
 // SiLU is z * sigmoid(z) with sigmoid(z) = (1 + tanh(z/2)) / 2 (one tanh.approx).
 // ------------------------------------------------------------------------------------
-constexpr int kGuessRows = 128, kGuessThreads = 256;
-constexpr size_t kGW2 = 0, kGA1 = kGW2 + 4 * 256 * 128, kGW1 = kGA1 + 4 * 128 * 128;
-constexpr size_t kGB1 = kGW1 + (size_t)kFeat * kHid * 4, kGB2 = kGB1 + kHid * 4, kGW3 = kGB2 + kHid * 4;
+constexpr int kGuessRows = 128, kGuessThreads = 256, kGFeatStride = 16;
+constexpr size_t kGW2 = 0, kGA1 = kGW2 + 4 * 256 * 128, kGF = kGA1 + 4 * 128 * 128;
+constexpr size_t kGT2 = kGF + (size_t)kGuessRows * kGFeatStride * 4, kGB1 = kGT2 + (size_t)kGuessRows * 8;
+constexpr size_t kGB2 = kGB1 + kHid * 4, kGW3 = kGB2 + kHid * 4;
 constexpr size_t kGYP = kGW3 + kHid * 4, kGBAR = kGYP + kGuessRows * 4;
 constexpr size_t kGuessSmem = 1024 + kGBAR + 64;
 // instruction descriptor, kind::f16: D f32 (bit 4), A and B f16 (format 0 at bits 7-9 and
@@ -275,7 +281,8 @@ __global__ void __launch_bounds__(kGuessThreads, 1)
                     double* __restrict__ t2out, int* err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  float* W1s = reinterpret_cast<float*>(smem + kGW1);
+  float* Fs = reinterpret_cast<float*>(smem + kGF);
+  double* T2m = reinterpret_cast<double*>(smem + kGT2);
   float* b1s = reinterpret_cast<float*>(smem + kGB1);
   float* b2s = reinterpret_cast<float*>(smem + kGB2);
   float* w3s = reinterpret_cast<float*>(smem + kGW3);
@@ -294,7 +301,15 @@ __global__ void __launch_bounds__(kGuessThreads, 1)
     *reinterpret_cast<uint4*>(smem + kGW2 + (size_t)kb * 256 * 128 + (size_t)nn * 128 + ((c ^ (nn & 7)) << 4)) =
         *reinterpret_cast<const uint4*>(hv);
   }
-  for (int x = tid; x < kFeat * kHid; x += kGuessThreads) W1s[x] = __half2float(wh[oW1 + x]);
+  // this thread's first-layer weights, held for the whole kernel
+  const int u0 = 8 * lane, rg = warp;  // hidden units u0 .. u0+7, tile rows 16 rg .. 16 rg + 15
+  float w1r[kFeat][8], b1r[8];
+#pragma unroll
+  for (int k = 0; k < kFeat; k++)
+#pragma unroll
+    for (int e = 0; e < 8; e++) w1r[k][e] = __half2float(wh[oW1 + (int64_t)k * kHid + u0 + e]);
+#pragma unroll
+  for (int e = 0; e < 8; e++) b1r[e] = w[ob1 + u0 + e];
   for (int x = tid; x < kHid; x += kGuessThreads) {
     b1s[x] = w[ob1 + x];
     b2s[x] = w[ob2 + x];
@@ -324,6 +339,7 @@ __global__ void __launch_bounds__(kGuessThreads, 1)
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t x = tile * kGuessRows + lr;
     const bool valid = x < n;
+    if (half == 0) {  // the features and MP2 amplitude of row lr
     float f[kFeat];
     double t2mp2 = 0.0;
     if (valid) {
@@ -353,21 +369,36 @@ __global__ void __launch_bounds__(kGuessThreads, 1)
 #pragma unroll
       for (int k = 0; k < kFeat; k++) f[k] = 0.f;
     }
-    // layer 1 for this thread's 128 hidden units, SiLU, FP16, into the A operand: unit u is
-    // K index u of the second layer (K block u / 64, chunk (u % 64) / 8)
-    for (int u0 = half * 128; u0 < half * 128 + 128; u0 += 8) {
-      __align__(16) __half hv[8];
 #pragma unroll
-      for (int e = 0; e < 8; e++) {
-        const int u = u0 + e;
-        float z = b1s[u];
-#pragma unroll
-        for (int k = 0; k < kFeat; k++) z = fmaf(f[k], W1s[k * kHid + u], z);
-        hv[e] = __float2half_rn(valid ? silu_tanh(z) : 0.f);
-      }
+    for (int k = 0; k < kFeat; k++) Fs[lr * kGFeatStride + k] = f[k];
+    Fs[lr * kGFeatStride + kFeat] = valid ? 1.f : 0.f;
+    T2m[lr] = t2mp2;
+    }
+    __syncthreads();
+    // layer 1: units u0 .. u0+7 of rows 16 rg .. 16 rg + 15, SiLU, FP16, into the A operand
+    // (unit u is K index u of the second layer: K block u / 64, chunk (u % 64) / 8)
+    {
       const int kb = u0 / 64, c = (u0 % 64) / 8;
-      *reinterpret_cast<uint4*>(smem + kGA1 + (size_t)kb * 128 * 128 + (size_t)lr * 128 + ((c ^ (lr & 7)) << 4)) =
-          *reinterpret_cast<const uint4*>(hv);
+#pragma unroll 2
+      for (int rr = 0; rr < 16; rr++) {
+        const int row = 16 * rg + rr;
+        const float* fr = Fs + row * kGFeatStride;
+        float z[8];
+#pragma unroll
+        for (int e = 0; e < 8; e++) z[e] = b1r[e];
+#pragma unroll
+        for (int k = 0; k < kFeat; k++) {
+          const float fk = fr[k];
+#pragma unroll
+          for (int e = 0; e < 8; e++) z[e] = fmaf(fk, w1r[k][e], z[e]);
+        }
+        const bool rv = fr[kFeat] != 0.f;
+        __align__(16) __half hv[8];
+#pragma unroll
+        for (int e = 0; e < 8; e++) hv[e] = __float2half_rn(rv ? silu_tanh(z[e]) : 0.f);
+        *reinterpret_cast<uint4*>(smem + kGA1 + (size_t)kb * 128 * 128 + (size_t)row * 128 +
+                                  ((c ^ (row & 7)) << 4)) = *reinterpret_cast<const uint4*>(hv);
+      }
     }
     tc::fence_proxy_async();
     tc::fence_before();
@@ -404,7 +435,7 @@ __global__ void __launch_bounds__(kGuessThreads, 1)
     if (half == 1) yp[lr] = part;
     tc::fence_before();
     __syncthreads();
-    if (half == 0 && valid) t2out[x] = t2mp2 + (double)(part + yp[lr] + b3) / kTarget;
+    if (half == 0 && valid) t2out[x] = T2m[lr] + (double)(part + yp[lr] + b3) / kTarget;
   }
   if (tid == 0 && *stop) tc::mbar_wait_deadline(bar, phase);  // no MMA in flight when TMEM is released
   tc::fence_before();
