@@ -901,65 +901,80 @@ __device__ __forceinline__ long long slice_fixed(double x, int e, int bits) {
 
 // digits: slices[s][r][k] = bf16(d_s 2^-SB(s+1)) for r < rows_p (zero past rows), k < kp
 // (zero past cols), the balanced base-2^SB digits of x 2^(SB S - e) (least significant s = S-1);
-// e[r] written by the blocks of the first K tile.  32 x 32 tiles through shared memory:
-// reads coalesced along whichever stride is 1, writes along k.
+// e[r] written by the blocks of the first K tile.  32 x 64 tiles through shared memory:
+// reads coalesced along whichever stride is 1; each thread then slices two neighbouring
+// elements of a row and stores each digit pair as one bf16x2 (a warp writes 128
+// contiguous bytes of a slice plane per store; kp is a multiple of 64).
 __global__ void slice_digits_kernel(MatView x, int64_t rows_p, int64_t kp, const unsigned long long* __restrict__ amax,
                                     int S, __nv_bfloat16* slices, int* e_out, int* range) {
-  __shared__ double t[32][33];
+  __shared__ double t[32][65];
   const int64_t rows = x.rows, cols = x.cols;
-  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
+  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 64;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const bool kc = mv_kcontig(x);
-  for (int i = ty; i < 32; i += 8) {
-    const int64_t r = kc ? r0 + i : r0 + tx, k = kc ? k0 + tx : k0 + i;
-    const double v = (r < rows && k < cols) ? mv_at(x, r, k) : 0.0;
-    if (kc)
-      t[i][tx] = v;
-    else
-      t[tx][i] = v;
+  if (mv_kcontig(x)) {
+    for (int i = ty; i < 32; i += 8)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int64_t r = r0 + i, k = k0 + tx + 32 * h;
+        t[i][tx + 32 * h] = (r < rows && k < cols) ? mv_at(x, r, k) : 0.0;
+      }
+  } else {
+    for (int j = ty; j < 64; j += 8) {
+      const int64_t r = r0 + tx, k = k0 + j;
+      t[tx][j] = (r < rows && k < cols) ? mv_at(x, r, k) : 0.0;
+    }
   }
   __syncthreads();
-  const size_t plane = (size_t)rows_p * kp;
+  const size_t plane2 = (size_t)rows_p * kp / 2;  // a slice plane in bf16 pairs
+  constexpr int H = 1 << (SB - 1);
   for (int i = ty; i < 32; i += 8) {
-    const int64_t r = r0 + i, k = k0 + tx;
-    if (r >= rows_p || k >= kp) continue;
+    const int64_t r = r0 + i, k = k0 + 2 * tx;
+    if (r >= rows_p) continue;
     const int e = r < rows ? slice_exponent(amax[r], range) : 0;
     if (k == 0 && r < rows) e_out[r] = e;
-    long long X = r < rows ? slice_fixed(t[i][tx], e, SB * S) : 0;
-    __nv_bfloat16* dst = slices + (size_t)r * kp + k;
-    constexpr int H = 1 << (SB - 1);
+    long long X0 = r < rows ? slice_fixed(t[i][2 * tx], e, SB * S) : 0;
+    long long X1 = r < rows ? slice_fixed(t[i][2 * tx + 1], e, SB * S) : 0;
+    __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(slices + (size_t)r * kp + k);
     // digit s (|d| <= 2^(SB-1)): a 32-bit conversion, exact, and exact in bf16 after the
     // power-of-2 scale
-    auto put = [&](int s, int d) {
-      dst[(size_t)s * plane] = __float2bfloat16_rn((float)d * __int_as_float((127 - SB * (s + 1)) << 23));
+    auto put = [&](int s, int d0, int d1) {
+      const float sc = __int_as_float((127 - SB * (s + 1)) << 23);
+      dst[(size_t)s * plane2] = __floats2bfloat162_rn((float)d0 * sc, (float)d1 * sc);
     };
     if (S >= 6) {
       // balanced digits in 32-bit arithmetic: the low 30 bits hold the 5 least significant
       // digits, whose carry out (0 or 1) joins the high part for the other S - 5
-      int lo = (int)(X & 0x3FFFFFFFll), hi = (int)(X >> 30);
+      int lo0 = (int)(X0 & 0x3FFFFFFFll), hi0 = (int)(X0 >> 30);
+      int lo1 = (int)(X1 & 0x3FFFFFFFll), hi1 = (int)(X1 >> 30);
       int s = S - 1;
       for (int q = 0; q < 5; q++, s--) {
-        const int d = ((lo + H) & (2 * H - 1)) - H;  // balanced digit in [-H, H)
-        lo = (lo - d) >> SB;
-        put(s, d);
+        const int d0 = ((lo0 + H) & (2 * H - 1)) - H, d1 = ((lo1 + H) & (2 * H - 1)) - H;  // in [-H, H)
+        lo0 = (lo0 - d0) >> SB;
+        lo1 = (lo1 - d1) >> SB;
+        put(s, d0, d1);
       }
-      hi += lo;
+      hi0 += lo0;
+      hi1 += lo1;
       for (; s > 0; s--) {
-        const int d = ((hi + H) & (2 * H - 1)) - H;
-        hi = (hi - d) >> SB;
-        put(s, d);
+        const int d0 = ((hi0 + H) & (2 * H - 1)) - H, d1 = ((hi1 + H) & (2 * H - 1)) - H;
+        hi0 = (hi0 - d0) >> SB;
+        hi1 = (hi1 - d1) >> SB;
+        put(s, d0, d1);
       }
-      put(0, hi);  // what remains: |d| <= H
+      put(0, hi0, hi1);  // what remains: |d| <= H
     } else {
       for (int s = S - 1; s >= 0; s--) {
-        long long d;
+        long long d0, d1;
         if (s > 0) {
-          d = ((X + H) & (2 * H - 1)) - H;  // balanced digit in [-H, H)
-          X = (X - d) >> SB;
+          d0 = ((X0 + H) & (2 * H - 1)) - H;  // balanced digit in [-H, H)
+          d1 = ((X1 + H) & (2 * H - 1)) - H;
+          X0 = (X0 - d0) >> SB;
+          X1 = (X1 - d1) >> SB;
         } else {
-          d = X;  // what remains: |d| <= H
+          d0 = X0;  // what remains: |d| <= H
+          d1 = X1;
         }
-        put(s, (int)d);
+        put(s, (int)d0, (int)d1);
       }
     }
   }
@@ -967,45 +982,53 @@ __global__ void slice_digits_kernel(MatView x, int64_t rows_p, int64_t kp, const
 
 // FP64 rows x cols view (strides sr, sk) -> bf16 hi/lo [rows][kp], zero padded to kp
 // (mid != null: three parts, x = hi + mid + lo, each the bf16 rounding of what remains)
-// 32 x 32 tiles through shared memory: reads coalesced along whichever stride is 1 (sk == 1:
-// along k, otherwise along the rows), writes along k.  Two parts are formed in FP32 (x
-// truncated to FP32 first, from its bit fields: 2^-23, far below the lo part's 2^-17),
-// three parts in FP64.
+// 32 x 64 tiles through shared memory: reads coalesced along whichever stride is 1 (sk == 1:
+// along k, otherwise along the rows); each thread splits two neighbouring elements of a row
+// and stores each part as one bf16x2 (128 contiguous bytes per warp store; kp is a
+// multiple of 64).  Two parts are formed in FP32 (x truncated to FP32 first, from its bit
+// fields: 2^-23, far below the lo part's 2^-17), three parts in FP64.
 __global__ void split_kernel(MatView x, int64_t kp, __nv_bfloat16* hi, __nv_bfloat16* lo, __nv_bfloat16* mid) {
-  __shared__ double t[32][33];
+  __shared__ double t[32][65];
   const int64_t rows = x.rows, cols = x.cols;
-  const int64_t k0 = (int64_t)blockIdx.x * 32;
+  const int64_t k0 = (int64_t)blockIdx.x * 64;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const bool kc = mv_kcontig(x);
   for (int64_t r0 = (int64_t)blockIdx.y * 32; r0 < rows; r0 += (int64_t)gridDim.y * 32) {  // row tiles
   __syncthreads();
-  for (int i = ty; i < 32; i += 8) {
-    const int64_t r = kc ? r0 + i : r0 + tx, k = kc ? k0 + tx : k0 + i;
-    const double v = (r < rows && k < cols) ? mv_at(x, r, k) : 0.0;
-    if (kc)
-      t[i][tx] = v;
-    else
-      t[tx][i] = v;
+  if (kc) {
+    for (int i = ty; i < 32; i += 8)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int64_t r = r0 + i, k = k0 + tx + 32 * h;
+        t[i][tx + 32 * h] = (r < rows && k < cols) ? mv_at(x, r, k) : 0.0;
+      }
+  } else {
+    for (int j = ty; j < 64; j += 8) {
+      const int64_t r = r0 + tx, k = k0 + j;
+      t[tx][j] = (r < rows && k < cols) ? mv_at(x, r, k) : 0.0;
+    }
   }
   __syncthreads();
   for (int i = ty; i < 32; i += 8) {
-    const int64_t r = r0 + i, k = k0 + tx;
-    if (r >= rows || k >= kp) continue;
-    const int64_t o = r * kp + k;
-    const double v = t[i][tx];
+    const int64_t r = r0 + i, k = k0 + 2 * tx;
+    if (r >= rows) continue;
+    const int64_t o2 = (r * kp + k) / 2;  // bf16 pair index
+    const double v0 = t[i][2 * tx], v1 = t[i][2 * tx + 1];
     if (mid) {
-      const __nv_bfloat16 h = __double2bfloat16(v);
-      double rest = v - (double)__bfloat162float(h);
-      const __nv_bfloat16 m = __double2bfloat16(rest);
-      rest -= (double)__bfloat162float(m);
-      hi[o] = h;
-      mid[o] = m;
-      lo[o] = __double2bfloat16(rest);
+      const __nv_bfloat16 h0 = __double2bfloat16(v0), h1 = __double2bfloat16(v1);
+      double r0d = v0 - (double)__bfloat162float(h0), r1d = v1 - (double)__bfloat162float(h1);
+      const __nv_bfloat16 m0 = __double2bfloat16(r0d), m1 = __double2bfloat16(r1d);
+      r0d -= (double)__bfloat162float(m0);
+      r1d -= (double)__bfloat162float(m1);
+      reinterpret_cast<__nv_bfloat162*>(hi)[o2] = __halves2bfloat162(h0, h1);
+      reinterpret_cast<__nv_bfloat162*>(mid)[o2] = __halves2bfloat162(m0, m1);
+      reinterpret_cast<__nv_bfloat162*>(lo)[o2] = __halves2bfloat162(__double2bfloat16(r0d), __double2bfloat16(r1d));
     } else {
-      const float f = f64_to_f32_trunc(v);
-      const __nv_bfloat16 h = __float2bfloat16_rn(f);
-      hi[o] = h;
-      lo[o] = __float2bfloat16_rn(f - __bfloat162float(h));
+      const float f0 = f64_to_f32_trunc(v0), f1 = f64_to_f32_trunc(v1);
+      const __nv_bfloat16 h0 = __float2bfloat16_rn(f0), h1 = __float2bfloat16_rn(f1);
+      reinterpret_cast<__nv_bfloat162*>(hi)[o2] = __halves2bfloat162(h0, h1);
+      reinterpret_cast<__nv_bfloat162*>(lo)[o2] =
+          __halves2bfloat162(__float2bfloat16_rn(f0 - __bfloat162float(h0)), __float2bfloat16_rn(f1 - __bfloat162float(h1)));
     }
   }
   }
@@ -1164,7 +1187,7 @@ static Split* prepare(Ctx& c, const MatView& x, int box_rows, std::unique_ptr<Sp
     s->lo = reinterpret_cast<__nv_bfloat16*>(static_cast<char*>(s->tmp->p) + plane);
     if (parts == 3) s->mid = reinterpret_cast<__nv_bfloat16*>(static_cast<char*>(s->tmp->p) + 2 * plane);
   }
-  split_kernel<<<dim3((unsigned)(s->kp / 32), (unsigned)std::min<int64_t>((rows + 31) / 32, 65535)), dim3(32, 8), 0,
+  split_kernel<<<dim3((unsigned)(s->kp / 64), (unsigned)std::min<int64_t>((rows + 31) / 32, 65535)), dim3(32, 8), 0,
                  c.stream>>>(x, s->kp, s->hi, s->lo, s->mid);
   count_kernel_launch();
   UCC_CUDA(cudaGetLastError());
@@ -1234,7 +1257,7 @@ static Sliced* slice_prepare(Ctx& c, const MatView& x, int pad_rows, int box_row
   slice_absmax_kernel<<<dim3((unsigned)((cols + kchunk - 1) / kchunk), (unsigned)rblocks), blk, 0, c.stream>>>(
       x, kchunk, static_cast<unsigned long long*>(amax.p));
   count_kernel_launch();
-  slice_digits_kernel<<<dim3((unsigned)(s->kp / 32), (unsigned)(s->rows_p / 32)), blk, 0, c.stream>>>(
+  slice_digits_kernel<<<dim3((unsigned)(s->kp / 64), (unsigned)(s->rows_p / 32)), blk, 0, c.stream>>>(
       x, s->rows_p, s->kp, static_cast<const unsigned long long*>(amax.p), S, s->d, s->e, k.range);
   count_kernel_launch();
   UCC_CUDA(cudaGetLastError());
