@@ -282,8 +282,12 @@ void build_W(Ctx& c, const Tensor& t1, const Tensor& t2, const Tensor& tau) {
   contract(c, "ie,mnej->mnij", 1.0, t1, V(c, "oovo"), 1.0, Woooo);
   contract(c, "ijef,mnef->mnij", 1.0, tau, V(c, "oovv"), 1.0, Woooo);
   Temp X(c, {no, no, nv, nv});
-  axpby(c, X->size(), 0.5, t2.p, 0.0, X->p);
-  contract(c, "jf,nb->jnfb", 1.0, t1, t1, 1.0, X);
+  if (!recorder()) {  // X = t2/2 + t1_jf t1_nb in one elementwise pass (as a K = 1 GEMM: DFMA tiles)
+    build_tau(c, no, nv, t1.p, t2.p, 1.0, X->p, 0.0, nullptr, 0.5);
+  } else {
+    axpby(c, X->size(), 0.5, t2.p, 0.0, X->p);
+    contract(c, "jf,nb->jnfb", 1.0, t1, t1, 1.0, X);
+  }
   permute_add(c, V(c, "ovov"), -1.0, 0.0, Wovov);
   contract(c, "jf,mbfe->mbje", -1.0, t1, V(c, "ovvv"), 1.0, Wovov);
   contract(c, "nb,mnje->mbje", 1.0, t1, V(c, "ooov"), 1.0, Wovov);

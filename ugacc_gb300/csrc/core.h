@@ -342,9 +342,9 @@ double dot(Ctx& c, int64_t n, const double* x, const double* y);
 // Several dot products x_k . y at once (DIIS B-matrix row), results on the device.
 void multidot_async(Ctx& c, int nvec, const double* const* d_xs, const double* y, int64_t n, double* d_out);
 
-// tau = t2 + f1 * t1(i,a) t1(j,b); ttau = t2 + f2 * t1 t1  (ttau may be null)
+// tau = g t2 + f1 * t1(i,a) t1(j,b); ttau = g t2 + f2 * t1 t1  (ttau may be null; g = 1 or 1/2)
 void build_tau(Ctx& c, int no, int nv, const double* t1, const double* t2, double f1, double* tau, double f2,
-               double* ttau);
+               double* ttau, double g = 1.0);
 
 // Jacobi update t_new = t_old + R / (D + shift), D built on the fly from the diagonals
 // do[no], dv[nv] in the reference's order ((d_i + d_j) - d_a) - d_b; the sum of R^2

@@ -708,7 +708,7 @@ void multidot_async(Ctx& c, int nvec, const double* const* d_xs, const double* y
 namespace {
 template <class I>
 __global__ void tau_kernel(int no, int nv, const double* t1, const double* t2, double f1, double* tau, double f2,
-                           double* ttau) {
+                           double* ttau, double g) {
   const I n = (I)no * no * nv * nv, v_ = (I)nv, o_ = (I)no;
   for (I x = (I)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (I)gridDim.x * blockDim.x) {
     const I b = x % v_;
@@ -718,7 +718,7 @@ __global__ void tau_kernel(int no, int nv, const double* t1, const double* t2, d
     const I j = r % o_;
     const I i = r / o_;
     const double tt = t1[i * v_ + a] * t1[j * v_ + b];
-    const double v = t2[x];
+    const double v = g * t2[x];  // g = 1 or 1/2: exact
     tau[x] = fma(f1, tt, v);
     if (ttau) ttau[x] = fma(f2, tt, v);
   }
@@ -767,13 +767,14 @@ __global__ void lincomb_kernel(int nvec, const double* const* vecs, const double
 }  // namespace
 
 void build_tau(Ctx& c, int no, int nv, const double* t1, const double* t2, double f1, double* tau, double f2,
-               double* ttau) {
+               double* ttau, double g) {
   UCC_REQUIRE(!recorder(), UCC_UNSUPPORTED, "not recordable");
+  UCC_REQUIRE(g == 1.0 || g == 0.5, UCC_BAD_ARGS, "build_tau: t2 scale 1 or 1/2");
   const int64_t n = (int64_t)no * no * nv * nv;
   if (n + 152 * 32 * 256 < ((int64_t)1 << 31))
-    tau_kernel<uint32_t><<<grid_for(n), 256, 0, c.stream>>>(no, nv, t1, t2, f1, tau, f2, ttau);
+    tau_kernel<uint32_t><<<grid_for(n), 256, 0, c.stream>>>(no, nv, t1, t2, f1, tau, f2, ttau, g);
   else
-    tau_kernel<int64_t><<<grid_for(n), 256, 0, c.stream>>>(no, nv, t1, t2, f1, tau, f2, ttau);
+    tau_kernel<int64_t><<<grid_for(n), 256, 0, c.stream>>>(no, nv, t1, t2, f1, tau, f2, ttau, g);
   count_launch();
   check_launch("tau");
 }
