@@ -1,6 +1,7 @@
 // Equation layer of the RHF-CC solver: integral blocks, DIIS and the solver stages.
 #pragma once
 
+#include <cmath>
 #include <string>
 #include <vector>
 
