@@ -67,8 +67,8 @@ def select_workload(name):
 
 # DRAM bytes (read + write) per launch of the roofline kernels at no=32/nv=320, from one
 # ncu launch list of the same solve (the no=32/nv=320 launch-list summary under profiles/):
-# split GEMM 1331 launches, sliced GEMM 91, DFMA GEMM 87
-TRAFFIC_C3 = {"split": 4.66e9, "sliced": 78.1e9, "dfma": 0.38e9}
+# split GEMM 1331 launches, sliced GEMM 91, DFMA GEMM 69
+TRAFFIC_C3 = {"split": 4.68e9, "sliced": 84.2e9, "dfma": 0.28e9}
 TRAFFIC_SOURCE = ("ncu launch list of the same workload, DRAM read + write per launch averaged over the "
                   "solve (the no=32/nv=320 launch-list summary under profiles/)")
 
