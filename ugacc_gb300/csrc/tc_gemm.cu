@@ -1852,6 +1852,8 @@ bool mixed_triples_batch(Ctx& c, int nb, const int* tuples, float* W3, int tblk)
   Triples& T = *k.triples;
   const int64_t no = c.no, nv = c.nv, nv2 = nv * nv, nv3 = nv2 * nv;
   const int64_t per = tblk ? (int64_t)tblk * tblk * tblk * 512 : nv3;  // floats per tuple and partial
+  UCC_REQUIRE(!tblk || (tblk >= (nv + 7) / 8 && per < ((int64_t)1 << 31)), UCC_BAD_ARGS,
+              "mixed (T): blocked W3 needs whole 8-wide blocks and < 2^31 floats per tuple");
   TriplesTerm terms[6];
   triples_terms(nv, terms);
   // The six terms in pairs that write the same W3 layout: the first term of a pair uses

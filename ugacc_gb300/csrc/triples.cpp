@@ -96,8 +96,10 @@ double run_triples(Ctx& c) {
   // mixed form
   const bool want_mixed = c.opt.precision == UCC_MIXED && !c.force_fp64;
   // nv % 4 == 0: the pipelined energy kernel, which reads W3 in 8 x 8 x 8 blocks
-  // (w3_block_offset; nv rounded up to whole blocks)
-  const int tblk = want_mixed && nv % 4 == 0 ? (nv + 7) / 8 : 0;
+  // (w3_block_offset; nv rounded up to whole blocks; the GEMM epilogue addresses a tuple's
+  // blocks with 32-bit offsets, so up to 2^31 floats per tuple, nv <= 1288)
+  const int64_t tb = (nv + 7) / 8;
+  const int tblk = want_mixed && nv % 4 == 0 && tb * tb * tb * 512 < ((int64_t)1 << 31) ? (int)tb : 0;
   const int64_t w3_per = tblk ? (int64_t)tblk * tblk * tblk * 512 : nv3;  // elements per tuple and array
   const double w3_bytes = (want_mixed ? 12.0 : 8.0) * (double)w3_per;
   const int batch = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)(budget / w3_bytes), 4096, ntup}));
